@@ -1,0 +1,156 @@
+// he4g_internal.cuh — device data layout, kernel parameter blocks and kernel
+// launchers of the sm_103a time step. Fields live in HBM in Fortran order
+// (x fastest, the order the Fortran driver and the C ABI use); half spectra
+// are (nx/2+1, ny, nz) complex with x fastest.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/he4g.h"
+
+namespace he4g {
+
+constexpr int kMaxFactors = 10;
+constexpr int kMaxN = 320;        // largest tstgrid.f90 size
+constexpr int kStencilHalf = 6;   // 13-point stencils
+constexpr int kRedBlock = 256;    // threads of the reduction blocks
+
+// One 1D transform length with its mixed-radix factorisation and its
+// forward twiddles tw[t] = exp(-2 pi i t / n), t < n (device memory).
+struct FftAxis {
+  int n;
+  int nf;
+  int fac[kMaxFactors];
+  const double2* tw;
+};
+
+// Geometry of one run.
+struct Grid {
+  int nx, ny, nz, nxh;
+  long long n;   // nx*ny*nz
+  long long nh;  // nxh*ny*nz
+  double hx, hy, hz, dxyz, renor;
+  double xmax, ymax, zmax;
+};
+
+// Stencil coefficients c_k / h^id for offsets k = 1..6 (and the centre),
+// per axis; d1: antisymmetric (centre 0), d2: symmetric.
+struct Stencil {
+  double d1[3][kStencilHalf + 1];
+  double d2[3][kStencilHalf + 1];
+  double d2c;  // sum over axes of the centre coefficient of d2
+};
+
+// Constants of the H.psi / functional evaluation.
+struct Functional {
+  double h2o2m4, cp4, cpp4, a0, a1;  // a0 = cp4/2, a1 = cpp4/3 (poten.f90:56-57)
+  double c_solid, beta_solid, den_m;
+  double den0s, alphas;
+  int lsolid, otc;
+};
+
+// Device-resident classical impurity and integrator scalars
+// (classicimp, modules.f90:282-320; rkpc).
+struct ImpState {
+  double rimp[3], vimp[3], aimp[3];
+  double rimpold[3][3], vimpold[3][3], aimpold[2][3];
+  double pcr[3], pcv[3], qr[3], qv[3];
+  int ioldr[3], ioldv[3], iolda[2];
+  int pad0;
+  double center[3];  // centre of the current uimp (last potenimp)
+  double force[3];   // last forceimp result
+  double errHe, errimp;
+  long long ring_head;  // rows written to the trajectory ring
+  int health;           // bit 0: den <= 0, bit 1: non-finite, bit 2: table overflow
+  int pad1;
+};
+
+constexpr int kRingRows = 8192;
+constexpr int kRingCols = 10;
+
+// kernel launch helpers (fft.cu)
+struct FftPlan {
+  FftAxis xh;   // packed half-length nx/2 along x
+  FftAxis y, z;
+  const double2* twx;  // exp(-2 pi i k / nx), k < nx/2 (r2c/c2r packing)
+};
+
+void fft_x_r2c(const Grid& g, const FftPlan& p, const double* in, double2* out, cudaStream_t s);
+// r2c of g = den*dencg*(cp4 + cpp4*dencg) (poten.f90:62-64), fused prologue
+void fft_x_r2c_corr(const Grid& g, const FftPlan& p, const double* den, const double* dencg,
+                    double cp4, double cpp4, double2* out, cudaStream_t s);
+// r2c of a*b (term_alfa.f90:32-36)
+void fft_x_r2c_prod(const Grid& g, const FftPlan& p, const double* a, const double* b, double2* out,
+                    cudaStream_t s);
+void fft_y(const Grid& g, const FftPlan& p, double2* const* specs, int nspec, int sign, cudaStream_t s);
+// forward z, multiply by nout tables (each scaled by `scale`), inverse z
+void fft_z_conv(const Grid& g, const FftPlan& p, const double2* in, double2* const* outs,
+                const double* const* factors, int nout, double scale, cudaStream_t s);
+void fft_x_c2r(const Grid& g, const FftPlan& p, const double2* const* ins, double* const* outs,
+               int nspec, cudaStream_t s);
+// c2r of the correlation convolution fused with the pot4 assembly
+// (poten.f90:80-94,110-114)
+void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, const double2* conv, const double* delj4,
+                    const double* dencg, const double* den, const Functional& fn, double* pot4,
+                    cudaStream_t s);
+
+// stencil / pointwise kernels (field.cu)
+struct Slots;
+void launch_pc_predict(const Grid& g, const Stencil& st, const Functional& fn, const double2* psi,
+                       double2* p3_out, double2* h1, double2* h2_out, double2* pc, const double* pot4,
+                       const double* uimp, const float* timec, double* den, double c4o3dt, double c112,
+                       cudaStream_t s);
+void launch_pc_correct(const Grid& g, const Stencil& st, const Functional& fn, const double2* psit,
+                       const double2* p3, const double2* p2, const double2* h1, const double2* h2,
+                       double2* pc, const double* pot4, const double* uimp, const float* timec,
+                       double2* psi_out, double* den, double* partials, double f3, double c9,
+                       int* health, cudaStream_t s);
+void launch_rk_stage(const Grid& g, const Stencil& st, const Functional& fn, const double2* psi,
+                     double2* psi_out, double2* q, double2* f_out, const double* pot4,
+                     const double* uimp, const float* timec, double* den, double ar, double br,
+                     double cr, double dt, int* health, cudaStream_t s);
+void launch_potenimp(const Grid& g, const double* x, const double* y, const double* z,
+                     const double* potion, int npot, double delinter, const ImpState* imp,
+                     int center_sel, double* uimp, cudaStream_t s);
+int force_blocks(const Grid& g);
+void launch_force(const Grid& g, const Stencil& st, const double* den, const double* uimp,
+                  double* dx, double* dy, double* dz, double* partials, cudaStream_t s);
+void launch_grad1(const Grid& g, const Stencil& st, int axis, const double* in, double* out,
+                  cudaStream_t s);
+int energy_blocks(const Grid& g);
+void launch_energy_point(const Grid& g, const Functional& fn, const double* den, const double* dencg,
+                         const double* delj4, const double* uimp, const double* falfs,
+                         const double* dx, const double* dy, const double* dz, const double* ix,
+                         const double* iy, const double* iz, const double* xs, const double* ys,
+                         const double* zs, double* partials, cudaStream_t s);
+void launch_energy_grad(const Grid& g, const Stencil& st, const double2* psi, const double* xs,
+                        const double* ys, const double* zs, const double* cm, double* partials,
+                        cudaStream_t s);
+void launch_reduce(const double* partials, int nblocks, int nvals, double* out, cudaStream_t s);
+int pc_blocks(const Grid& g);
+
+void launch_density(const Grid& g, const double2* psi, double* den, cudaStream_t s);
+
+// OTC pointwise pieces (term_alfa.f90)
+void launch_falfs(const Grid& g, const double* denalf, double den0s, double* falfs, cudaStream_t s);
+void launch_dot3(const Grid& g, const double* ax, const double* ay, const double* az, const double* bx,
+                 const double* by, const double* bz, double* out, cudaStream_t s);
+void launch_ualphas_a(const Grid& g, const double* falfs, const double* ix, const double* iy,
+                      const double* iz, double* u, double* s1, double* s2, double* s3, double den0s,
+                      cudaStream_t s);
+void launch_ualphas_b(const Grid& g, double* u, const double* s4, const double* s5, const double* s6,
+                      double h2o2m4, double alphas, double* pot4, cudaStream_t s);
+
+// impurity scalar kernels (field.cu)
+void launch_imp_rk(ImpState* imp, int stage, double ar, double br, double cr, double dt, cudaStream_t s);
+void launch_imp_pc_predict(ImpState* imp, double c4o3dt, double c112, cudaStream_t s);
+void launch_imp_pc_correct(ImpState* imp, const double* err_partials, int nblocks, double dt,
+                           double c9, double nxyz, cudaStream_t s);
+void launch_imp_force(ImpState* imp, const double* partials, int nblocks, double dxyz, double mass,
+                      int store_accel, cudaStream_t s);
+void launch_imp_record(ImpState* imp, double* ring, long long step, cudaStream_t s);
+
+}  // namespace he4g

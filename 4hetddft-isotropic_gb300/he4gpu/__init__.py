@@ -1,0 +1,200 @@
+"""Host-side mirror of the reference's time-step routines over libhe4g.so.
+
+`Run` carries the names and argument meaning of the reference routines it
+replaces (steprk.f90, steppc.f90, potenimp.f90, poten.f90, energy.f90,
+r_cm.f90, the loop body of DFT4He3d.f90:840-852) and raises `He4gError`
+where the reference would STOP. All arithmetic runs in libhe4g.so on the GPU;
+this module only moves arguments across the C ABI.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .abi import CORE_OT, CORE_OTC, Config  # noqa: F401
+from .initial import (PS_TO_K, KELVIN_PER_PS, woods_saxon_psi, collision_case,  # noqa: F401
+                      config_for_case)
+
+
+class He4gError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"he4g error {code} ({abi.ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+def default_config(nx, ny, nz, xmax, ymax=None, zmax=None, **overrides):
+    """Reference defaults (he4g_default_config) with keyword overrides."""
+    lib = abi.load()
+    cfg = Config()
+    ymax = xmax if ymax is None else ymax
+    zmax = xmax if zmax is None else zmax
+    lib.he4g_default_config(C.byref(cfg), nx, ny, nz, xmax, ymax, zmax)
+    for k, v in overrides.items():
+        if not hasattr(cfg, k):
+            raise KeyError(k)
+        setattr(cfg, k, v)
+    return cfg
+
+
+def build_tables(cfg, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463, with_kalfs=None):
+    """fforma / initcg / kalfs / potenimpini tables of the run (host side)."""
+    lib = abi.load()
+    nh = (cfg.nx // 2 + 1) * cfg.ny * cfg.nz
+    fv = np.empty(nh)
+    wc = np.empty(nh)
+    if with_kalfs is None:
+        with_kalfs = cfg.core == CORE_OTC
+    ka = np.empty(nh) if with_kalfs else None
+    po = np.empty(cfg.npot)
+    rc = lib.he4g_build_tables(C.byref(cfg), selec.encode(), r_cutoff, umax, abi.dptr(fv), abi.dptr(wc),
+                               abi.dptr(ka) if ka is not None else None, abi.dptr(po))
+    if rc:
+        raise He4gError(rc, "build_tables")
+    return {"fvlj4": fv, "wcgk": wc, "kalfs": ka, "potion": po}
+
+
+class Run:
+    """One GPU-resident run (he4g_run)."""
+
+    def __init__(self, cfg, tables=None, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463):
+        self.lib = abi.load()
+        self.cfg = cfg
+        self.tables = tables if tables is not None else build_tables(cfg, selec, r_cutoff, umax)
+        self.shape = (cfg.nz, cfg.ny, cfg.nx)
+        h = C.c_void_p()
+        t = self.tables
+        rc = self.lib.he4g_create(C.byref(cfg), abi.dptr(t["fvlj4"]), abi.dptr(t["wcgk"]),
+                                  abi.dptr(t["kalfs"]) if t.get("kalfs") is not None else None,
+                                  abi.dptr(t["potion"]), C.byref(h))
+        if rc:
+            raise He4gError(rc, "he4g_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.he4g_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        if rc:
+            msg = self.lib.he4g_last_error(self.h)
+            raise He4gError(rc, msg.decode() if msg else "")
+
+    # ---------------------------------------------------------------- state
+    def set_state(self, psi, rimp, vimp):
+        psi = np.ascontiguousarray(psi, dtype=np.complex128).reshape(self.shape)
+        r = np.ascontiguousarray(rimp, dtype=np.float64)
+        v = np.ascontiguousarray(vimp, dtype=np.float64)
+        self._ck(self.lib.he4g_set_state(self.h, abi.dptr(psi), abi.dptr(r), abi.dptr(v)))
+
+    # -------------------------------------------------- reference routines
+    def potenimp(self, rimp):
+        r = np.ascontiguousarray(rimp, dtype=np.float64)
+        self._ck(self.lib.he4g_potenimp(self.h, abi.dptr(r)))
+
+    def poten(self):
+        self._ck(self.lib.he4g_poten(self.h))
+
+    def forceimp(self, rimp=(0.0, 0.0, 0.0)):
+        r = np.ascontiguousarray(rimp, dtype=np.float64)
+        F = np.zeros(3)
+        self._ck(self.lib.he4g_forceimp(self.h, abi.dptr(r), abi.dptr(F)))
+        return F
+
+    def steprk(self, deltat):
+        self._ck(self.lib.he4g_steprk(self.h, deltat))
+
+    def steppc(self, deltat):
+        e = np.zeros(2)
+        self._ck(self.lib.he4g_steppc(self.h, deltat, abi.dptr(e[:1]), abi.dptr(e[1:])))
+        return float(e[0]), float(e[1])
+
+    def step(self, nsteps=1):
+        e = np.zeros(2)
+        self._ck(self.lib.he4g_step(self.h, nsteps, abi.dptr(e[:1]), abi.dptr(e[1:])))
+        return float(e[0]), float(e[1])
+
+    def step_timed(self, nsteps):
+        """he4g_step with CUDA events on the run's stream; returns device ms."""
+        ms = np.zeros(1)
+        self._ck(self.lib.he4g_step_timed(self.h, nsteps, abi.dptr(ms)))
+        return float(ms[0])
+
+    @property
+    def launch_count(self):
+        return int(self.lib.he4g_launch_count(self.h))
+
+    def energy(self):
+        en = abi.Energies()
+        self._ck(self.lib.he4g_energy(self.h, C.byref(en)))
+        return en.as_dict()
+
+    def r_cm(self, npart):
+        cm = np.zeros(3)
+        self._ck(self.lib.he4g_r_cm(self.h, float(npart), abi.dptr(cm)))
+        return cm
+
+    def observables(self, npart):
+        o = abi.Obs()
+        self._ck(self.lib.he4g_observables(self.h, float(npart), C.byref(o)))
+        return {"npart": o.npart, "cm": list(o.cm), "ang": list(o.ang), "ang_im": list(o.ang_im),
+                "r2": list(o.r2)}
+
+    # ------------------------------------------------------------- readback
+    @property
+    def psi(self):
+        out = np.empty(self.shape, dtype=np.complex128)
+        self._ck(self.lib.he4g_get_psi(self.h, abi.dptr(out)))
+        return out
+
+    @property
+    def den(self):
+        out = np.empty(self.shape)
+        self._ck(self.lib.he4g_get_den(self.h, abi.dptr(out)))
+        return out
+
+    FIELDS = {"pot4": 0, "dencg": 1, "delj4": 2, "uimp": 3, "dxden": 4, "dyden": 5, "dzden": 6,
+              "ualphas": 7, "denalf": 8}
+
+    def field(self, name):
+        out = np.empty(self.shape)
+        self._ck(self.lib.he4g_get_field(self.h, self.FIELDS[name], abi.dptr(out)))
+        return out
+
+    def impurity(self):
+        r, v, a = np.zeros(3), np.zeros(3), np.zeros(3)
+        self._ck(self.lib.he4g_get_impurity(self.h, abi.dptr(r), abi.dptr(v), abi.dptr(a)))
+        return r, v, a
+
+    def set_impurity(self, r, v, a):
+        r, v, a = (np.ascontiguousarray(x, dtype=np.float64) for x in (r, v, a))
+        self._ck(self.lib.he4g_set_impurity(self.h, abi.dptr(r), abi.dptr(v), abi.dptr(a)))
+
+    def trajectory(self, cap=8192):
+        rows = np.zeros((cap, 10))
+        n = C.c_int()
+        self._ck(self.lib.he4g_get_trajectory(self.h, abi.dptr(rows), cap, C.byref(n)))
+        return rows[: n.value]
+
+    @property
+    def steps_taken(self):
+        return self.lib.he4g_steps_taken(self.h)
+
+    def enable_timing(self, on=True):
+        self._ck(self.lib.he4g_enable_timing(self.h, 1 if on else 0))
+
+    def kernel_times(self):
+        cap = 32
+        names = (C.c_char_p * cap)()
+        ms = np.zeros(cap)
+        launches = (C.c_int * cap)()
+        k = self.lib.he4g_kernel_times(self.h, names, abi.dptr(ms), launches, cap)
+        if k < 0:
+            self._ck(k)
+        return {names[i].decode(): (float(ms[i]), int(launches[i])) for i in range(k)}

@@ -1,0 +1,210 @@
+/*
+ * he4g.h — C ABI of the GB300 (sm_103a) time step of the Orsay–Trento 4He
+ * TDDFT solver with a classical impurity (bcntls2016/4hetddft-isotropic).
+ *
+ * The reference keeps every field in Fortran module globals (modules.f90) and
+ * its routines take no field arguments. This library owns the same state on
+ * one GPU behind an opaque handle; the Fortran driver (DFT4He3d.f90) keeps its
+ * loop and calls these entry points through ISO_C_BINDING wrappers that carry
+ * the reference routine names (steprk, steppc, potenimp, poten, forceimp,
+ * energy, r_cm).
+ *
+ * Conventions
+ *  - Every int-returning call returns HE4G_OK (0) on success and a negative
+ *    HE4G_E* code on failure; he4g_last_error() gives the message.
+ *  - Field arrays cross the boundary in Fortran order (x fastest): real fields
+ *    are double[nz][ny][nx]; psi is complex(8), i.e. interleaved (re, im)
+ *    doubles, 2*nx*ny*nz of them. Half-grid k-space tables are
+ *    double[nz][ny][nx/2+1] (dimen.f90:32-62).
+ *  - Host buffers are owned by the caller and only touched during the call.
+ *  - One host thread per handle; distinct handles may run concurrently (each
+ *    owns its own CUDA stream).
+ *  - Units follow the reference: lengths in Angstrom, energies in K, time
+ *    step in K^-1 (deltat = deltatps / 7.63822291, DFT4He3d.f90:233-249),
+ *    impurity velocity in Angstrom*K (Angstrom/ps * 7.63822291, :302).
+ */
+#ifndef HE4G_H
+#define HE4G_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define HE4G_OK 0
+#define HE4G_EINVAL (-1)     /* bad argument or configuration                  */
+#define HE4G_ENOMEM (-2)     /* device allocation failed                       */
+#define HE4G_ECUDA (-3)      /* CUDA runtime error                             */
+#define HE4G_EDENSITY (-4)   /* density not > 0 somewhere (steprk.f90:89-92)   */
+#define HE4G_ENAN (-5)       /* non-finite value in the state                  */
+#define HE4G_ETABLE (-6)     /* impurity distance beyond the potential table   */
+#define HE4G_ESTATE (-7)     /* call out of order (e.g. step before set_state) */
+
+/* functional core (lenard4 core4, DFT4He3d.f90:476-509) */
+#define HE4G_CORE_OT 0  /* 'OT ': Orsay–Trento core, no alpha_s term          */
+#define HE4G_CORE_OTC 1 /* 'OTC': full Orsay–Trento with the alpha_s term     */
+
+/* arithmetic of the per-step fields */
+#define HE4G_PREC_FP64 0 /* every field and transform in FP64 (reference)   */
+
+/*
+ * Run configuration. Defaults (he4g_default_config) are the reference's module
+ * defaults (modules.f90 he4 :130-150, lenard4 :204-216, deriva :27-33,
+ * DFT4He3d.f90 :135-137) and the shipped input's absorber.
+ */
+typedef struct he4g_config {
+  int32_t nx, ny, nz;  /* grid points; each in tstgrid.f90's list, nx even   */
+  int32_t npd;         /* stencil points, must be 13 (deriva npd)            */
+  int32_t icon;        /* boundary mode, must be 13 (zero padding)           */
+  int32_t core;        /* HE4G_CORE_OT or HE4G_CORE_OTC                      */
+  int32_t lsolid;      /* solid penalty term (he4 lsolid); forces core OT    */
+  int32_t lrk;         /* 1: Runge–Kutta–Gill every step (DFT4He3d.f90:840)  */
+  int32_t precision;   /* HE4G_PREC_FP64                                     */
+  int32_t npot;        /* potential-table nodes (potenimpini.f90:13)         */
+  double xmax, ymax, zmax; /* box half-extent; h = 2*xmax/nx (:274-276)      */
+  double deltat;       /* time step in K^-1                                  */
+  /* Orsay–Trento functional (modules.f90:138-148) */
+  double cp4, cpp4, h2o2m4, alphas, l_alpha, den0s;
+  double c_solid, beta_solid, den_m;
+  /* Lennard-Jones (modules.f90:204-216) and coarse graining */
+  double eps4, sigma4, h4; /* core radius of the OT core (h4ot)              */
+  double hcg;          /* coarse-graining radius: 1.065*h4 if lsolid else h4 */
+  /* absorbing boundary (DFT4He3d.f90:689-699) */
+  double lambdah, txmean, txsurf, tymean, tysurf, tzmean, tzsurf;
+  /* classical impurity */
+  double mimpur;       /* mass in u; m = mimpur*0.02061484 K^-1 A^-2         */
+  double delinter;     /* potential-table spacing (potenimpini.f90:16)       */
+} he4g_config;
+
+/* energies (energy.f90:112-132) */
+typedef struct he4g_energies {
+  double etot4, ekin4, elj4, ecor4, ealphas, esolid, eext;
+  double ekinx, eHeX, eimpu, etot;
+} he4g_energies;
+
+/* observables (DFT4He3d.f90:869-943, r_cm.f90) */
+typedef struct he4g_observables {
+  double npart;  /* sum(den)*dxyz                                  */
+  double cm[3];  /* centre of mass, divided by the given n4       */
+  double ang[3]; /* <Lx>, <Ly>, <Lz> (real parts)                 */
+  double ang_im[3];
+  double r2[3];  /* <x^2>, <y^2>, <z^2> (times dxyz, not /N)      */
+} he4g_obs;
+
+typedef struct he4g_run he4g_run;
+
+/* ---------------------------------------------------------------- setup */
+
+/* Fills the reference defaults for an nx*ny*nz grid of half-extent xmax.
+ * Replaces the namelist defaults of DFT4He3d.f90:149-168 / modules.f90. */
+void he4g_default_config(he4g_config* cfg, int nx, int ny, int nz, double xmax, double ymax,
+                         double zmax);
+
+/* Host-side setup tables, the work of fforma.f90:11-61 (OT form factor of the
+ * cored LJ potential, p = 0 from bforce :256-280), initcg.f90:32-49 (coarse
+ * graining kernel), DFT4He3d.f90:592-596 (alpha_s Gaussian kalfs) and
+ * potenimpini.f90:11-27 + V_impur.f90 Select_Pot (radial impurity table).
+ * selec: "Xe_He" or "Ar_He". Output half-grid arrays hold (nx/2+1)*ny*nz
+ * doubles; potion holds cfg->npot doubles; kalfs may be NULL. */
+int he4g_build_tables(const he4g_config* cfg, const char* selec, double r_cutoff, double umax,
+                      double* fvlj4, double* wcgk, double* kalfs, double* potion);
+
+/* Allocates the run on the current CUDA device and uploads the tables
+ * (replaces dimen.f90, fftini fft.f90:5-76 and the table set-up calls of
+ * DFT4He3d.f90:518-596). kalfs is required for core OTC, else may be NULL. */
+int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
+                const double* kalfs, const double* potion, he4g_run** out);
+
+void he4g_destroy(he4g_run* run);
+const char* he4g_last_error(const he4g_run* run);
+
+/* Loads psi (complex, Fortran order), rimp[3] (A) and vimp[3] (A*K) and resets
+ * the integrator phase like a fresh start (readenc mode 0/2 then the zeroing
+ * of q, pc, qr, qv and the impurity history: dimen.f90:117-118,
+ * DFT4He3d.f90:796-800). den = |psi|^2 (:637). */
+int he4g_set_state(he4g_run* run, const double* psi, const double rimp[3], const double vimp[3]);
+
+/* ---------------------------------------------- reference-routine mirrors */
+
+/* potenimp(rimp): impurity potential on the grid by linear interpolation of
+ * the radial table (potenimp.f90:1-20, updatepoten :71-95). */
+int he4g_potenimp(he4g_run* run, const double rimp[3]);
+
+/* poten(): mean field pot4[den] (poten.f90:5-118, term_alfa.f90 for OTC),
+ * including derden (derden.f90:26-28). */
+int he4g_poten(he4g_run* run);
+
+/* forceimp(rimp, F): F = -sum(grad(den)*uimp)*dxyz with the uimp of the last
+ * he4g_potenimp call and the density gradient of the last he4g_poten call
+ * (potenimp.f90:24-55; the rimp argument is unused there too). */
+int he4g_forceimp(he4g_run* run, const double rimp[3], double F[3]);
+
+/* steprk(deltat): one Runge–Kutta–Gill step of psi and (rimp, vimp)
+ * (steprk.f90:21-150), including its three inner potential evaluations. */
+int he4g_steprk(he4g_run* run, double deltat);
+
+/* steppc(deltat, errHe, errimp): one Hamming predictor–modifier–corrector
+ * step (steppc.f90:1-178), including its inner potential evaluation. */
+int he4g_steppc(he4g_run* run, double deltat, double* errHe, double* errimp);
+
+/* energy(): energy components (energy.f90:12-144). Call after he4g_poten. */
+int he4g_energy(he4g_run* run, he4g_energies* e);
+
+/* r_cm(rho, npart, xcm, ycm, zcm) (r_cm.f90:23-58). */
+int he4g_r_cm(he4g_run* run, double npart, double cm[3]);
+
+/* The observables block of DFT4He3d.f90:869-943 (norm, centre of mass,
+ * angular momentum via complex first derivatives, <x^2>,<y^2>,<z^2>). */
+int he4g_observables(he4g_run* run, double npart, he4g_obs* o);
+
+/* The loop body DFT4He3d.f90:840-852 run nsteps times on the device:
+ * Runge–Kutta–Gill while fewer than 3 steps were taken since set_state (or
+ * always when lrk), else predictor–corrector; then potenimp(rimp), poten(),
+ * forceimp(rimp, aimp), aimp /= m. Per-step (r, v, a) go to a device ring.
+ * errHe/errimp (nullable) receive the last predictor–corrector errors. */
+int he4g_step(he4g_run* run, int nsteps, double* errHe, double* errimp);
+
+/* he4g_step with CUDA events recorded on the run's stream before its first
+ * and after its last launch; *device_ms receives the elapsed device time. */
+int he4g_step_timed(he4g_run* run, int nsteps, double* device_ms);
+
+/* Kernel launches issued by this run since it was created. */
+long long he4g_launch_count(const he4g_run* run);
+
+/* ------------------------------------------------------------- readback */
+
+/* Copies up to cap trajectory rows written since the last call; each row is
+ * 10 doubles: step index, r[3] (A), v[3] (A*K), a[3] (A*K^2). *n = rows. */
+int he4g_get_trajectory(he4g_run* run, double* rows, int cap, int* n);
+
+int he4g_get_psi(he4g_run* run, double* psi);  /* 2*nx*ny*nz doubles */
+int he4g_get_den(he4g_run* run, double* den);  /* nx*ny*nz doubles   */
+
+/* Field readback for checks: which = 0 pot4, 1 dencg, 2 delj4, 3 uimp,
+ * 4 dxden, 5 dyden, 6 dzden, 7 ualphas (OTC), 8 denalf (OTC). */
+int he4g_get_field(he4g_run* run, int which, double* out);
+
+/* Impurity state: r (A), v (A*K), a (A*K^2). */
+int he4g_get_impurity(he4g_run* run, double r[3], double v[3], double a[3]);
+
+/* Overwrites r (A), v (A*K) and a (A*K^2) of the impurity and keeps the
+ * integrator history; the Fortran wrappers call it with the driver's module
+ * variables rimp, vimp, aimp (set at DFT4He3d.f90:849-852) before a step. */
+int he4g_set_impurity(he4g_run* run, const double r[3], const double v[3], const double a[3]);
+
+/* Steps taken since the last set_state. */
+int he4g_steps_taken(const he4g_run* run);
+
+/* Average device time (ms) of the kernels of the last he4g_step call, per
+ * kernel family; used by the benchmark to compute the roofline figures.
+ * names/ms arrays of capacity cap; returns the number of families. */
+int he4g_kernel_times(he4g_run* run, const char** names, double* ms, int* launches, int cap);
+int he4g_enable_timing(he4g_run* run, int on);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HE4G_H */

@@ -1,0 +1,197 @@
+"""GPU parity: the sm_103a library, called through its C ABI, against the FP64
+CPU oracle on the same seeded states.
+
+Tolerances (FP64 build): fields after one potential evaluation agree to
+1e-12 of their maximum; after N steps the density, psi, every energy
+component, the norm and the impurity trajectory agree to 1e-10 relative.
+uimp is computed with the same rounding sequence on both sides and must agree
+bit for bit.
+"""
+import numpy as np
+import pytest
+
+from helpers import gpu_run, make_case, oracle_run, rel, rel_field
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-12
+STEP_TOL = 1e-10
+SMALL_CASES = ["he100_xe_32", "he300_ar_48", "he200_xe_40x48x64"]
+
+
+@pytest.fixture(scope="module", params=SMALL_CASES)
+def pair(request):
+    cfg, tk, psi, r, v, meta = make_case(request.param)
+    g = gpu_run(cfg, tk, psi, r, v)
+    o = oracle_run(cfg, tk, psi, r, v)
+    yield g, o, cfg, tk, psi, r, v, meta
+    g.close()
+    o.close()
+
+
+def test_uimp_bitwise(pair):
+    g, o, *_ = pair
+    assert np.array_equal(g.field("uimp"), o.field("uimp"))
+
+
+def test_initial_evaluation(pair):
+    g, o, *_ = pair
+    for name in ("dencg", "delj4", "pot4"):
+        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
+    for name in ("dxden", "dyden", "dzden"):
+        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
+    rg, vg, ag = g.impurity()
+    ro, vo, ao = o.impurity()
+    assert np.array_equal(rg, ro) and np.array_equal(vg, vo)
+    assert rel(ag, ao) < 1e-10
+
+
+def test_energy_and_observables(pair):
+    g, o, cfg, tk, psi, r, v, meta = pair
+    eg, eo = g.energy(), o.energy()
+    for k in eo:
+        assert abs(eg[k] - eo[k]) <= 1e-11 * max(abs(eo[k]), 1e-6), k
+    og, oo = g.observables(meta["n4"]), o.observables(meta["n4"])
+    assert rel(og["npart"], oo["npart"]) < 1e-12
+    assert np.allclose(og["cm"], oo["cm"], rtol=1e-11, atol=1e-12)
+    assert np.allclose(og["r2"], oo["r2"], rtol=1e-11)
+    assert np.allclose(og["ang"], oo["ang"], rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("case,nsteps", [("he100_xe_32", 12), ("he300_ar_48", 8), ("he200_xe_40x48x64", 7)])
+def test_steps_match_oracle(case, nsteps):
+    """3 RK-Gill + PC steps with the trailing re-evaluation (DFT4He3d.f90:840-852)."""
+    cfg, tk, psi, r, v, meta = make_case(case)
+    g = gpu_run(cfg, tk, psi, r, v)
+    o = oracle_run(cfg, tk, psi, r, v)
+    eg = g.step(nsteps)
+    eo = o.step(nsteps)
+    assert rel_field(g.den, o.den) < STEP_TOL
+    assert rel_field(g.psi, o.psi) < STEP_TOL
+    # errHe sums |P - C|, a difference of nearly equal states: compared loosely
+    assert abs(eg[0] - eo[0]) <= 1e-6 * eo[0]
+    rg, vg, ag = g.impurity()
+    ro, vo, ao = o.impurity()
+    assert rel(rg, ro) < STEP_TOL and rel(vg, vo) < STEP_TOL and rel(ag, ao) < 1e-8
+    enG, enO = g.energy(), o.energy()
+    for k in enO:
+        assert abs(enG[k] - enO[k]) <= STEP_TOL * max(abs(enO[k]), 1e-3), k
+    assert rel(g.den.sum(), o.den.sum()) < 1e-12
+    traj = g.trajectory()
+    assert traj.shape == (nsteps, 10)
+    assert np.array_equal(traj[:, 0], np.arange(1, nsteps + 1))
+    np.testing.assert_allclose(traj[-1, 1:4], ro, rtol=STEP_TOL)
+    g.close()
+    o.close()
+
+
+def test_reference_routines_compose_like_the_driver():
+    """steprk/steppc/potenimp/poten/forceimp called one by one, as the Fortran
+    driver calls them, give the same state as he4g_step."""
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    a = gpu_run(cfg, tk, psi, r, v)
+    b = gpu_run(cfg, tk, psi, r, v)
+    a.step(5)
+    dt = cfg.deltat
+    m = cfg.mimpur * 0.02061484
+    for it in range(1, 6):
+        if it <= 3:
+            b.steprk(dt)
+        else:
+            b.steppc(dt)
+        rb, vb, _ = b.impurity()
+        b.potenimp(rb)
+        b.poten()
+        F = b.forceimp(rb)
+        # aimp = F / mAg_u on the host (DFT4He3d.f90:852), handed back like the
+        # module variables a Fortran wrapper passes on its next call
+        b.set_impurity(rb, vb, F / m)
+    assert np.array_equal(b.psi, a.psi)
+    assert all(np.array_equal(x, y) for x, y in zip(a.impurity(), b.impurity()))
+
+
+def test_otc_alpha_s_matches_oracle():
+    """Core OTC (lsolid off): term_alfa and E_alpha (term_alfa.f90, energy.f90:99-105)."""
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", core=1, lsolid=0, hcg=2.190323)
+    g = gpu_run(cfg, tk, psi, r, v)
+    o = oracle_run(cfg, tk, psi, r, v)
+    for name in ("denalf", "ualphas", "pot4", "dencg"):
+        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
+    eg, eo = g.energy(), o.energy()
+    assert eo["ealphas"] != 0.0
+    assert abs(eg["ealphas"] - eo["ealphas"]) <= 1e-11 * abs(eo["ealphas"])
+    g.step(5)
+    o.step(5)
+    assert rel_field(g.den, o.den) < STEP_TOL
+    eg, eo = g.energy(), o.energy()
+    for k in eo:
+        assert abs(eg[k] - eo[k]) <= STEP_TOL * max(abs(eo[k]), 1e-3), k
+
+
+def test_lrk_runs_rk_every_step():
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", lrk=1)
+    g = gpu_run(cfg, tk, psi, r, v)
+    o = oracle_run(cfg, tk, psi, r, v)
+    g.step(5)
+    o.step(5)
+    assert rel_field(g.den, o.den) < STEP_TOL
+
+
+def test_step_before_state_is_an_error():
+    import he4gpu
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    run = he4gpu.Run(cfg, selec=tk["selec"], r_cutoff=tk["r_cutoff"], umax=tk["umax"])
+    with pytest.raises(he4gpu.He4gError) as e:
+        run.step(1)
+    assert e.value.code == he4gpu.abi.HE4G_ESTATE
+
+
+def test_zero_density_stops_like_steprk():
+    """A density that is not > 0 after an RK stage is an error (steprk.f90:89-92)."""
+    import he4gpu
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    psi = psi.copy()
+    # a slab of exact zeros deeper than the stencil half-width: its first plane
+    # has only zero neighbours, so H.psi = 0 there and den stays 0
+    psi[0:8, :, :] = 0.0
+    run = gpu_run(cfg, tk, psi, r, v)
+    with pytest.raises(he4gpu.He4gError) as e:
+        run.step(1)
+    assert e.value.code == he4gpu.abi.HE4G_EDENSITY
+
+
+def test_impurity_beyond_table_is_an_error():
+    import he4gpu
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    far = np.array([0.0, 0.0, -10.0 * meta["zmax"]])
+    with pytest.raises(he4gpu.He4gError) as e:
+        gpu_run(cfg, tk, psi, far, v)
+    assert e.value.code == he4gpu.abi.HE4G_ETABLE
+
+
+def test_runs_are_independent():
+    """Two runs on one device do not share state."""
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    a = gpu_run(cfg, tk, psi, r, v)
+    b = gpu_run(cfg, tk, psi * 1.01, r, v)
+    a.step(4)
+    c = gpu_run(cfg, tk, psi, r, v)
+    c.step(4)
+    assert np.array_equal(a.psi, c.psi)
+    assert not np.array_equal(a.psi, b.psi)
+
+
+def test_config1_short_run():
+    """The 128^3 He_1000 + Xe collision: 4 steps (3 RK + 1 PC) against the oracle."""
+    cfg, tk, psi, r, v, meta = make_case("he1000_xe_128")
+    g = gpu_run(cfg, tk, psi, r, v)
+    o = oracle_run(cfg, tk, psi, r, v)
+    g.step(4)
+    o.step(4)
+    assert rel_field(g.den, o.den) < STEP_TOL
+    rg, *_ = g.impurity()
+    ro, *_ = o.impurity()
+    assert rel(rg, ro) < STEP_TOL
+    eg, eo = g.energy(), o.energy()
+    for k in eo:
+        assert abs(eg[k] - eo[k]) <= STEP_TOL * max(abs(eo[k]), 1e-3), k
