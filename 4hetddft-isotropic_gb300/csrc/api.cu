@@ -184,7 +184,8 @@ void make_axis(he4g_run* r, FftAxis& ax, int n, std::vector<void*>& tw_hold) {
     tw[t] = make_double2(static_cast<double>(cosl(a)), static_cast<double>(-sinl(a)));
   }
   double2* d = dalloc<double2>(r, n, false);
-  cudaMemcpy(d, tw.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
+  cudaMemcpyAsync(d, tw.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, r->s);
+  cudaStreamSynchronize(r->s);  // tw is a local vector
   ax.tw = d;
   (void)tw_hold;
 }
@@ -586,10 +587,12 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
         sv = sv + tz[k];
         tc[((size_t)k * c.ny + j) * c.nx + i] = static_cast<float>(c.lambdah * sv);
       }
-  cudaMemcpy(r->xs, x.data(), sizeof(double) * c.nx, cudaMemcpyHostToDevice);
-  cudaMemcpy(r->ys, y.data(), sizeof(double) * c.ny, cudaMemcpyHostToDevice);
-  cudaMemcpy(r->zs, z.data(), sizeof(double) * c.nz, cudaMemcpyHostToDevice);
-  cudaMemcpy(r->timec, tc.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+  // every upload is ordered on the run's stream after the zeroing memsets
+  cudaMemcpyAsync(r->xs, x.data(), sizeof(double) * c.nx, cudaMemcpyHostToDevice, r->s);
+  cudaMemcpyAsync(r->ys, y.data(), sizeof(double) * c.ny, cudaMemcpyHostToDevice, r->s);
+  cudaMemcpyAsync(r->zs, z.data(), sizeof(double) * c.nz, cudaMemcpyHostToDevice, r->s);
+  cudaMemcpyAsync(r->timec, tc.data(), sizeof(float) * n, cudaMemcpyHostToDevice, r->s);
+  cudaStreamSynchronize(r->s);  // the host vectors go out of scope below
   std::vector<void*> hold;
   make_axis(r, r->plan.xh, c.nx / 2, hold);
   make_axis(r, r->plan.y, c.ny, hold);
@@ -605,7 +608,8 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
       he4g_destroy(r);
       return HE4G_ENOMEM;
     }
-    cudaMemcpy(d, twx.data(), sizeof(double2) * (c.nx / 2), cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(d, twx.data(), sizeof(double2) * (c.nx / 2), cudaMemcpyHostToDevice, r->s);
+    cudaStreamSynchronize(r->s);
     r->plan.twx = d;
   }
   cudaError_t e = cudaStreamSynchronize(r->s);
