@@ -35,6 +35,11 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
 
 
+def set_case(name):
+    global CASE
+    CASE = name
+
+
 def algorithmic_bytes_per_step(nx, ny, nz):
     """Compulsory HBM bytes of one predictor-corrector step per kernel family
     (reads + writes of each launch's inputs and outputs, stencil neighbours
@@ -332,7 +337,10 @@ def ours(args):
     line = None
     if rank == 0:
         e2e_steps = max(3, min(args.steps, 10))
-        e2e_val, h2d, d2h = e2e_measure(run, psi, r, v, e2e_steps)
+        if args.no_e2e:
+            e2e_val, h2d, d2h = None, 0, 0
+        else:
+            e2e_val, h2d, d2h = e2e_measure(run, psi, r, v, e2e_steps)
         cpu = None
         if ws == 1 and not args.no_cpu:
             try:
@@ -347,15 +355,16 @@ def ours(args):
             "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": warm, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Woods-Saxon droplet + Xe)",
-            "config": {"workload": CASE + " FP64 predictor-corrector step", "grid": [256, 256, 256], "h": 0.4,
-                       "n4": 5000, "impurity": "Xe", "v_A_per_ps": 3.0, "impact_parameter": "0.5 R",
+            "config": {"workload": CASE + " FP64 predictor-corrector step", "grid": [cfg.nx, cfg.ny, cfg.nz],
+                       "h": meta["h"], "n4": meta["n4"], "impurity": meta["imp"], "v_A_per_ps": meta["v"],
+                       "impact_parameter": f"{meta['b_frac']} R",
                        "l2": "inputs larger than L2 (psi 268 MB, history 1.9 GB); no flush",
                        "parallelism": f"replicas x{ws}"},
             "grid_point_updates_per_s": value * cfg.nx * cfg.ny * cfg.nz,
             "hbm_gbs": roofline["step_gbs"],
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_val * ws, "unit": "steps/s", "h2d_bytes_per_step": h2d,
+            "e2e": {"value": e2e_val * ws if e2e_val else None, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "gpu_launches_per_step": launches / args.steps,
@@ -382,7 +391,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
+    ap.add_argument("--case", default=CASE, help="workload (profiling runs use smaller ones)")
     args = ap.parse_args()
+    set_case(args.case)
     if args.impl == "reference":
         return reference_arm(args)
     return ours(args)
