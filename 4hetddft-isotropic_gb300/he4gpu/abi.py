@@ -97,6 +97,8 @@ SIGNATURES = {
     "he4g_get_impurity": (C.c_int, [_P, _D, _D, _D]),
     "he4g_set_impurity": (C.c_int, [_P, _D, _D, _D]),
     "he4g_step_timed": (C.c_int, [_P, C.c_int, _D]),
+    "he4g_forceimp_noalloc": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                        C.c_double, _P, _P]),
     "he4g_launch_count": (C.c_longlong, [_P]),
     "he4g_steps_taken": (C.c_int, [_P]),
     "he4g_kernel_times": (C.c_int, [_P, C.POINTER(C.c_char_p), _D, C.POINTER(C.c_int), C.c_int]),

@@ -167,6 +167,31 @@ int he4g_observables(he4g_run* run, double npart, he4g_obs* o);
  * errHe/errimp (nullable) receive the last predictor–corrector errors. */
 int he4g_step(he4g_run* run, int nsteps, double* errHe, double* errimp);
 
+/* The impurity force F = -sum(grad(den) * uimp) * dxyz of he4g_forceimp for
+ * callers that must not allocate device memory. This entry point has no
+ * counterpart in the reference; it serves hosts that keep the fields in
+ * device memory they manage themselves (a CUDA Fortran / OpenACC port of the
+ * driver, or a serving loop that packs runs into HBM by footprint) and call
+ * the force inside their time loop, where cudaMalloc would synchronise the
+ * whole device every step and can fail once co-resident runs fill the GPU.
+ *  - den, uimp: device arrays of nx*ny*nz doubles (Fortran order); F: device
+ *    array of 3 doubles that receives the force; the grid spacing is
+ *    2*xmax/nx etc. as in he4g_config; stream: a cudaStream_t (NULL = the
+ *    legacy default stream). The call is asynchronous on that stream.
+ *  - Nothing is allocated or freed: the per-block partial sums go to a
+ *    built-in device array of 3 MiB that every GPU which loads the library
+ *    holds until the process exits. It fits 131072 blocks of 64x4 points,
+ *    i.e. ceil(nx/64)*ceil(ny/4)*nz <= 131072 (every grid up to 320^3);
+ *    larger grids are rejected with HE4G_EINVAL and a message on stderr.
+ *  - The first call on a device looks up that array's device address with
+ *    the device current; make that first call before any stream capture.
+ *  - All calls share the array, which keeps the last call's partial sums;
+ *    no part of it needs zeroing (each call writes every slot it reads), but
+ *    calls that overlap on the GPU (e.g. on two streams at once) race on it.
+ * Returns HE4G_OK, HE4G_EINVAL or HE4G_ECUDA. */
+int he4g_forceimp_noalloc(const double* den, const double* uimp, int nx, int ny, int nz, double xmax,
+                          double ymax, double zmax, double* F, void* stream);
+
 /* he4g_step with CUDA events recorded on the run's stream before its first
  * and after its last launch; *device_ms receives the elapsed device time. */
 int he4g_step_timed(he4g_run* run, int nsteps, double* device_ms);
