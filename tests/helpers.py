@@ -32,6 +32,14 @@ def rel_field(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
+def rel_vec(a, b):
+    """max |a - b| / max |b| for small vectors (components that vanish by
+    symmetry, such as an impurity's y coordinate, are judged on the vector's
+    scale)."""
+    a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
 def rel(a, b):
     a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
