@@ -7,6 +7,16 @@
 // rotation), h[0..1] = hpsiold as f_{n-1}, f_{n-2}. The classical impurity
 // and its integrator scalars stay on the device (ImpState), so a step issues
 // no host synchronisation.
+//
+// Precision: HE4G_PREC_FP64 keeps every array in FP64. HE4G_PREC_MIXED keeps
+// psi, its history, pc and q in FP64 and everything else (fields, spectra,
+// tables, hpsiold) in FP32, plus an FP32 copy of psi for the stencils
+// (psi32[cur32], ping-ponged with psi32[1 - cur32]).
+//
+// The mean field sums the Lennard-Jones convolution and the correlation
+// convolution in k-space before one shared inverse transform, so delj4 is
+// not formed during a step; he4g_energy and he4g_get_field form it on demand
+// from the same density.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,36 +58,48 @@ struct he4g_run {
   he4g_config cfg{};
   Grid g{};
   Stencil st{};
+  StencilF stf{};
   Functional fn{};
   FftPlan plan{};
+  int prec = HE4G_PREC_FP64;
+  size_t rs = 8;  // bytes of a field element
   cudaStream_t s = nullptr;
   double mass = 0.0;
   std::string err;
   std::vector<void*> allocs;
 
+  // FP64 in both precisions
   double2* psi = nullptr;
   double2* scratch = nullptr;
   double2* old[3] = {nullptr, nullptr, nullptr};
-  double2* h[2] = {nullptr, nullptr};
   double2* q = nullptr;
   double2* pc = nullptr;
-  double *den = nullptr, *pot4 = nullptr, *dencg = nullptr, *delj4 = nullptr, *uimp = nullptr;
-  float* timec = nullptr;
   double *xs = nullptr, *ys = nullptr, *zs = nullptr;
-  double *fvlj4 = nullptr, *wcgk = nullptr, *kalfs = nullptr, *potion = nullptr;
-  double2 *spec0 = nullptr, *spec1 = nullptr, *spec2 = nullptr;
-  double *dx = nullptr, *dy = nullptr, *dz = nullptr;
-  double *denalf = nullptr, *falfs = nullptr, *ix = nullptr, *iy = nullptr, *iz = nullptr;
-  double *ualphas = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr,
-         *t6 = nullptr;
+  // precision-typed (double / double2 or float / float2)
+  void* h[2] = {nullptr, nullptr};
+  void *den = nullptr, *pot4 = nullptr, *dencg = nullptr, *delj4 = nullptr, *uimp = nullptr;
+  void *fvlj4 = nullptr, *wcgk = nullptr, *kalfs = nullptr, *potion = nullptr;
+  void *spec0 = nullptr, *spec1 = nullptr, *spec2 = nullptr;
+  void *dx = nullptr, *dy = nullptr, *dz = nullptr;
+  void *denalf = nullptr, *falfs = nullptr, *ix = nullptr, *iy = nullptr, *iz = nullptr;
+  void *ualphas = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr,
+       *t6 = nullptr;
+  float* timec = nullptr;
+  // mixed precision only
+  float2* psi32[2] = {nullptr, nullptr};
+  int cur32 = 0;
+  float *xsf = nullptr, *ysf = nullptr, *zsf = nullptr;
+
   double* partials = nullptr;
   double* small = nullptr;  // reduction outputs / cm
   ImpState* imp = nullptr;
   double* ring = nullptr;
   int pblocks = 0;
+  int fblocks = 0;
 
   int iter = 0;
   bool have_state = false;
+  bool delj4_valid = false;
   long long ring_read = 0;
 
   long long launches = 0;
@@ -91,6 +113,8 @@ struct he4g_run {
 
 namespace {
 
+bool mixed(const he4g_run* r) { return r->prec == HE4G_PREC_MIXED; }
+
 int fail(he4g_run* r, int code, const std::string& msg) {
   if (r) r->err = msg;
   return code;
@@ -99,13 +123,16 @@ int cuda_fail(he4g_run* r, cudaError_t e, const char* where) {
   return fail(r, HE4G_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+void* dalloc_bytes(he4g_run* r, size_t bytes, bool zero = true) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes + 16) != cudaSuccess) return nullptr;
+  r->allocs.push_back(p);
+  if (zero) cudaMemsetAsync(p, 0, bytes, r->s);
+  return p;
+}
 template <typename T>
 T* dalloc(he4g_run* r, size_t count, bool zero = true) {
-  void* p = nullptr;
-  if (cudaMalloc(&p, count * sizeof(T) + 16) != cudaSuccess) return nullptr;
-  r->allocs.push_back(p);
-  if (zero) cudaMemsetAsync(p, 0, count * sizeof(T), r->s);
-  return static_cast<T*>(p);
+  return static_cast<T*>(dalloc_bytes(r, count * sizeof(T), zero));
 }
 
 cudaEvent_t take_event(he4g_run* r) {
@@ -119,7 +146,8 @@ cudaEvent_t take_event(he4g_run* r) {
   return e;
 }
 
-// RAII bracket that records a start/stop event pair around a launch family
+// RAII bracket that counts the launches of a family and, when timing is on,
+// records a start/stop event pair around them
 struct Tick {
   he4g_run* r;
   int fam;
@@ -154,7 +182,34 @@ void collect_timing(he4g_run* r) {
   r->pending.clear();
 }
 
-void make_axis(he4g_run* r, FftAxis& ax, int n, std::vector<void*>& tw_hold) {
+// upload of a host double array into a precision-typed device array
+void upload_field(he4g_run* r, void* dst, const double* src, size_t n) {
+  if (!mixed(r)) {
+    cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, r->s);
+    cudaStreamSynchronize(r->s);
+    return;
+  }
+  std::vector<float> f(n);
+  for (size_t i = 0; i < n; ++i) f[i] = static_cast<float>(src[i]);
+  cudaMemcpyAsync(dst, f.data(), sizeof(float) * n, cudaMemcpyHostToDevice, r->s);
+  cudaStreamSynchronize(r->s);
+}
+
+int download_field(he4g_run* r, const void* src, double* dst, size_t n, const char* where) {
+  cudaError_t e;
+  if (!mixed(r)) {
+    e = cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, r->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
+  } else {
+    std::vector<float> f(n);
+    e = cudaMemcpyAsync(f.data(), src, sizeof(float) * n, cudaMemcpyDeviceToHost, r->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
+    for (size_t i = 0; i < n; ++i) dst[i] = f[i];
+  }
+  return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, where);
+}
+
+void make_axis(he4g_run* r, FftAxis& ax, int n) {
   ax.n = n;
   ax.nf = 0;
   int m = n;
@@ -179,15 +234,19 @@ void make_axis(he4g_run* r, FftAxis& ax, int n, std::vector<void*>& tw_hold) {
     m /= 5;
   }
   std::vector<double2> tw(n);
+  std::vector<float2> twf(n);
   for (int t = 0; t < n; ++t) {
     const long double a = 2.0L * 3.141592653589793238462643383279502884L * t / n;
     tw[t] = make_double2(static_cast<double>(cosl(a)), static_cast<double>(-sinl(a)));
+    twf[t] = make_float2(static_cast<float>(cosl(a)), static_cast<float>(-sinl(a)));
   }
   double2* d = dalloc<double2>(r, n, false);
+  float2* df = dalloc<float2>(r, n, false);
   cudaMemcpyAsync(d, tw.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, r->s);
-  cudaStreamSynchronize(r->s);  // tw is a local vector
+  cudaMemcpyAsync(df, twf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice, r->s);
+  cudaStreamSynchronize(r->s);  // the host vectors go out of scope
   ax.tw = d;
-  (void)tw_hold;
+  ax.twf = df;
 }
 
 bool radix_ok(int n) {
@@ -201,142 +260,201 @@ bool radix_ok(int n) {
 // ----------------------------------------------------------------- pieces
 void potenimp_dev(he4g_run* r, int sel) {
   Tick t(r, F_POTENIMP);
-  launch_potenimp(r->g, r->xs, r->ys, r->zs, r->potion, r->cfg.npot, r->cfg.delinter, r->imp, sel, r->uimp,
-                  r->s);
+  if (mixed(r))
+    launch_potenimp_mp(r->g, r->xsf, r->ysf, r->zsf, static_cast<const float*>(r->potion), r->cfg.npot,
+                       static_cast<float>(r->cfg.delinter), r->imp, sel, static_cast<float*>(r->uimp), r->s);
+  else
+    launch_potenimp(r->g, r->xs, r->ys, r->zs, static_cast<const double*>(r->potion), r->cfg.npot, r->cfg.delinter,
+                    r->imp, sel, static_cast<double*>(r->uimp), r->s);
 }
 
-// convolution of a real field with one radial table: out = IFFT(tab * FFT(a*b))
-void conv_dev(he4g_run* r, const double* a, const double* b, const double* tab, double* out) {
+// out = IFFT(tab * FFT(a*b)) (b nullable) through spec0
+void conv_dev(he4g_run* r, const void* a, const void* b, const void* tab, void* out) {
   const Grid& g = r->g;
   {
     Tick t(r, F_FFT_X_R2C);
     if (b)
-      fft_x_r2c_prod(g, r->plan, a, b, r->spec0, r->s);
+      fft_x_r2c_prod(g, r->plan, r->prec, a, b, r->spec0, r->s);
     else
-      fft_x_r2c(g, r->plan, a, r->spec0, r->s);
+      fft_x_r2c(g, r->plan, r->prec, a, r->spec0, r->s);
   }
-  double2* sp[1] = {r->spec0};
+  void* sp[1] = {r->spec0};
   {
     Tick t(r, F_FFT_Y);
-    fft_y(g, r->plan, sp, 1, -1, r->s);
+    fft_y(g, r->plan, r->prec, sp, 1, -1, r->s);
   }
   {
     Tick t(r, F_FFT_Z_CONV);
-    const double* f[1] = {tab};
-    fft_z_conv(g, r->plan, r->spec0, sp, f, 1, 0.5 * g.renor, r->s);
+    const void* f[1] = {tab};
+    fft_z_conv(g, r->plan, r->prec, r->spec0, sp, f, 1, 0.5 * g.renor, nullptr, r->s);
   }
   {
     Tick t(r, F_FFT_Y);
-    fft_y(g, r->plan, sp, 1, +1, r->s);
+    fft_y(g, r->plan, r->prec, sp, 1, +1, r->s);
   }
   {
     Tick t(r, F_FFT_X_C2R);
-    const double2* in[1] = {r->spec0};
-    double* o[1] = {out};
-    fft_x_c2r(g, r->plan, in, o, 1, r->s);
+    const void* in[1] = {r->spec0};
+    void* o[1] = {out};
+    fft_x_c2r(g, r->plan, r->prec, in, o, 1, r->s);
   }
+}
+
+void grad1_dev(he4g_run* r, int axis, const void* in, void* out) {
+  if (mixed(r))
+    launch_grad1_f(r->g, r->stf, axis, static_cast<const float*>(in), static_cast<float*>(out), r->s);
+  else
+    launch_grad1(r->g, r->st, axis, static_cast<const double*>(in), static_cast<double*>(out), r->s);
 }
 
 // term_alfa (term_alfa.f90:5-117) and pot4 += ualphas (poten.f90:96-107)
 void alpha_s_dev(he4g_run* r) {
   const Grid& g = r->g;
+  const bool mp = mixed(r);
   {
     Tick t(r, F_ALPHA_S);
-    launch_falfs(g, r->denalf, r->cfg.den0s, r->falfs, r->s);
+    if (mp)
+      launch_falfs_f(g, static_cast<const float*>(r->denalf), static_cast<float>(r->cfg.den0s),
+                     static_cast<float*>(r->falfs), r->s);
+    else
+      launch_falfs(g, static_cast<const double*>(r->denalf), r->cfg.den0s, static_cast<double*>(r->falfs), r->s);
   }
   conv_dev(r, r->falfs, r->dx, r->kalfs, r->ix);
   conv_dev(r, r->falfs, r->dy, r->kalfs, r->iy);
   conv_dev(r, r->falfs, r->dz, r->kalfs, r->iz);
   {
     Tick t(r, F_ALPHA_S);
-    launch_dot3(g, r->dx, r->dy, r->dz, r->ix, r->iy, r->iz, r->t1, r->s);
+    if (mp)
+      launch_dot3_f(g, static_cast<const float*>(r->dx), static_cast<const float*>(r->dy),
+                    static_cast<const float*>(r->dz), static_cast<const float*>(r->ix),
+                    static_cast<const float*>(r->iy), static_cast<const float*>(r->iz), static_cast<float*>(r->t1),
+                    r->s);
+    else
+      launch_dot3(g, static_cast<const double*>(r->dx), static_cast<const double*>(r->dy),
+                  static_cast<const double*>(r->dz), static_cast<const double*>(r->ix),
+                  static_cast<const double*>(r->iy), static_cast<const double*>(r->iz), static_cast<double*>(r->t1),
+                  r->s);
   }
   conv_dev(r, r->t1, nullptr, r->kalfs, r->ualphas);
   {
     Tick t(r, F_ALPHA_S, 5);
-    launch_ualphas_a(g, r->falfs, r->ix, r->iy, r->iz, r->ualphas, r->t1, r->t2, r->t3, r->cfg.den0s, r->s);
-    launch_grad1(g, r->st, 0, r->t1, r->t4, r->s);
-    launch_grad1(g, r->st, 1, r->t2, r->t5, r->s);
-    launch_grad1(g, r->st, 2, r->t3, r->t6, r->s);
-    launch_ualphas_b(g, r->ualphas, r->t4, r->t5, r->t6, r->cfg.h2o2m4, r->cfg.alphas, r->pot4, r->s);
+    if (mp) {
+      launch_ualphas_a_f(g, static_cast<const float*>(r->falfs), static_cast<const float*>(r->ix),
+                         static_cast<const float*>(r->iy), static_cast<const float*>(r->iz),
+                         static_cast<float*>(r->ualphas), static_cast<float*>(r->t1), static_cast<float*>(r->t2),
+                         static_cast<float*>(r->t3), static_cast<float>(r->cfg.den0s), r->s);
+    } else {
+      launch_ualphas_a(g, static_cast<const double*>(r->falfs), static_cast<const double*>(r->ix),
+                       static_cast<const double*>(r->iy), static_cast<const double*>(r->iz),
+                       static_cast<double*>(r->ualphas), static_cast<double*>(r->t1), static_cast<double*>(r->t2),
+                       static_cast<double*>(r->t3), r->cfg.den0s, r->s);
+    }
+    grad1_dev(r, 0, r->t1, r->t4);
+    grad1_dev(r, 1, r->t2, r->t5);
+    grad1_dev(r, 2, r->t3, r->t6);
+    if (mp)
+      launch_ualphas_b_f(g, static_cast<float*>(r->ualphas), static_cast<const float*>(r->t4),
+                         static_cast<const float*>(r->t5), static_cast<const float*>(r->t6),
+                         static_cast<float>(r->cfg.h2o2m4), static_cast<float>(r->cfg.alphas),
+                         static_cast<float*>(r->pot4), r->s);
+    else
+      launch_ualphas_b(g, static_cast<double*>(r->ualphas), static_cast<const double*>(r->t4),
+                       static_cast<const double*>(r->t5), static_cast<const double*>(r->t6), r->cfg.h2o2m4,
+                       r->cfg.alphas, static_cast<double*>(r->pot4), r->s);
   }
 }
 
-// poten (poten.f90:5-118)
+// poten (poten.f90:5-118). delj4 + the correlation convolution are summed in
+// the (kx, ky, z) space of the z pass and share one inverse y and x pass.
 void poten_dev(he4g_run* r) {
   const Grid& g = r->g;
   const bool otc = r->fn.otc;
+  const int prec = r->prec;
+  r->delj4_valid = false;
   {
     Tick t(r, F_FFT_X_R2C);
-    fft_x_r2c(g, r->plan, r->den, r->spec0, r->s);
+    fft_x_r2c(g, r->plan, prec, r->den, r->spec0, r->s);
   }
-  double2* sp[1] = {r->spec0};
+  void* sp0[1] = {r->spec0};
   {
     Tick t(r, F_FFT_Y);
-    fft_y(g, r->plan, sp, 1, -1, r->s);
+    fft_y(g, r->plan, prec, sp0, 1, -1, r->s);
   }
-  double2* outs[3] = {r->spec0, r->spec1, r->spec2};
-  const double* facs[3] = {r->wcgk, r->fvlj4, r->kalfs};
-  const int nout = otc ? 3 : 2;
   {
+    // rho-hat -> coarse-grained density (spec0), Lennard-Jones (spec1), alpha_s density (spec2)
     Tick t(r, F_FFT_Z_CONV);
-    fft_z_conv(g, r->plan, r->spec0, outs, facs, nout, 0.5 * g.renor, r->s);
+    void* outs[3] = {r->spec0, r->spec1, r->spec2};
+    const void* facs[3] = {r->wcgk, r->fvlj4, r->kalfs};
+    fft_z_conv(g, r->plan, prec, r->spec0, outs, facs, otc ? 3 : 2, 0.5 * g.renor, nullptr, r->s);
   }
   {
     Tick t(r, F_FFT_Y);
-    fft_y(g, r->plan, outs, nout, +1, r->s);
+    void* sp[2] = {r->spec0, r->spec2};
+    fft_y(g, r->plan, prec, sp, otc ? 2 : 1, +1, r->s);
   }
   {
-    Tick t(r, F_FFT_X_C2R, otc ? 2 : 1);
-    const double2* in[2] = {r->spec0, r->spec1};
-    double* o[2] = {r->dencg, r->delj4};
-    fft_x_c2r(g, r->plan, in, o, 2, r->s);
-    if (otc) {
-      const double2* in2[1] = {r->spec2};
-      double* o2[1] = {r->denalf};
-      fft_x_c2r(g, r->plan, in2, o2, 1, r->s);
-    }
+    Tick t(r, F_FFT_X_C2R);
+    const void* in[2] = {r->spec0, r->spec2};
+    void* o[2] = {r->dencg, r->denalf};
+    fft_x_c2r(g, r->plan, prec, in, o, otc ? 2 : 1, r->s);
   }
   {
     Tick t(r, F_FFT_X_R2C);
-    fft_x_r2c_corr(g, r->plan, r->den, r->dencg, r->cfg.cp4, r->cfg.cpp4, r->spec0, r->s);
+    fft_x_r2c_corr(g, r->plan, prec, r->den, r->dencg, r->cfg.cp4, r->cfg.cpp4, r->spec0, r->s);
   }
   {
     Tick t(r, F_FFT_Y);
-    fft_y(g, r->plan, sp, 1, -1, r->s);
+    fft_y(g, r->plan, prec, sp0, 1, -1, r->s);
   }
   {
+    // correlation convolution, plus the Lennard-Jones field already in spec1
     Tick t(r, F_FFT_Z_CONV);
-    const double* f1[1] = {r->wcgk};
-    fft_z_conv(g, r->plan, r->spec0, sp, f1, 1, 0.5 * g.renor, r->s);
+    const void* f1[1] = {r->wcgk};
+    fft_z_conv(g, r->plan, prec, r->spec0, sp0, f1, 1, 0.5 * g.renor, r->spec1, r->s);
   }
   {
     Tick t(r, F_FFT_Y);
-    fft_y(g, r->plan, sp, 1, +1, r->s);
+    fft_y(g, r->plan, prec, sp0, 1, +1, r->s);
   }
   {
     Tick t(r, F_FFT_X_C2R_POT4);
-    fft_x_c2r_pot4(g, r->plan, r->spec0, r->delj4, r->dencg, r->den, r->fn, r->pot4, r->s);
+    fft_x_c2r_pot4(g, r->plan, prec, r->spec0, r->dencg, r->den, r->fn, r->pot4, r->s);
   }
   if (otc) {
     {
       Tick t(r, F_ALPHA_S, 3);
-      launch_grad1(g, r->st, 0, r->den, r->dx, r->s);
-      launch_grad1(g, r->st, 1, r->den, r->dy, r->s);
-      launch_grad1(g, r->st, 2, r->den, r->dz, r->s);
+      grad1_dev(r, 0, r->den, r->dx);
+      grad1_dev(r, 1, r->den, r->dy);
+      grad1_dev(r, 2, r->den, r->dz);
     }
     alpha_s_dev(r);
   }
 }
 
+// delj4 = V_LJ * den (poten.f90:46-50), formed on demand for the energy
+void delj4_dev(he4g_run* r) {
+  if (r->delj4_valid) return;
+  conv_dev(r, r->den, nullptr, r->fvlj4, r->delj4);
+  r->delj4_valid = true;
+}
+
 // forceimp (potenimp.f90:24-55); store_accel: aimp = F / m on the device
 void force_dev(he4g_run* r, int store_accel) {
+  int nb;
   {
     Tick t(r, F_FORCE);
-    launch_force(r->g, r->st, r->den, r->uimp, nullptr, nullptr, nullptr, r->partials, r->s);
+    if (mixed(r)) {
+      launch_force_mp(r->g, r->stf, static_cast<const float*>(r->den), static_cast<const float*>(r->uimp),
+                      r->partials, r->s);
+      nb = r->fblocks;
+    } else {
+      launch_force(r->g, r->st, static_cast<const double*>(r->den), static_cast<const double*>(r->uimp), nullptr,
+                   nullptr, nullptr, r->partials, r->s);
+      nb = r->pblocks;
+    }
   }
   Tick t(r, F_SCALAR);
-  launch_imp_force(r->imp, r->partials, r->pblocks, r->g.dxyz, r->mass, store_accel, r->s);
+  launch_imp_force(r->imp, r->partials, nb, r->g.dxyz, r->mass, store_accel, r->s);
 }
 
 // potenimp(rimp); poten(); forceimp(rimp, aimp); aimp /= m
@@ -370,9 +488,18 @@ void steprk_dev(he4g_run* r, double dt) {
       Tick t(r, F_RK_STAGE);
       // stage 1 shifts the histories: hpsiold(2) = hpsiold(1), hpsiold(1) = H.psi,
       // psiold(3..1) = psiold(2..1), psi
-      double2* f_out = j == 0 ? r->h[1] : nullptr;
-      launch_rk_stage(r->g, r->st, r->fn, r->psi, r->scratch, r->q, f_out, r->pot4, r->uimp, r->timec, r->den,
-                      arun[j], brun[j], crun[j], dt, health, r->s);
+      void* f_out = j == 0 ? r->h[1] : nullptr;
+      if (mixed(r)) {
+        launch_rk_stage_mp(r->g, r->stf, r->fn, r->psi32[r->cur32], r->psi, r->scratch, r->psi32[1 - r->cur32],
+                           r->q, static_cast<float2*>(f_out), static_cast<const float*>(r->pot4),
+                           static_cast<const float*>(r->uimp), r->timec, static_cast<float*>(r->den), arun[j],
+                           brun[j], crun[j], dt, health, r->s);
+        r->cur32 = 1 - r->cur32;
+      } else {
+        launch_rk_stage(r->g, r->st, r->fn, r->psi, r->scratch, r->q, static_cast<double2*>(f_out),
+                        static_cast<const double*>(r->pot4), static_cast<const double*>(r->uimp), r->timec,
+                        static_cast<double*>(r->den), arun[j], brun[j], crun[j], dt, health, r->s);
+      }
     }
     if (j == 0) {
       double2* freed = r->old[2];
@@ -396,10 +523,21 @@ void steprk_dev(he4g_run* r, double dt) {
 // steppc (steppc.f90:1-178)
 void steppc_dev(he4g_run* r, double dt) {
   const double c112 = 112.0 / 121.0, c9 = 9.0 / 121.0, c4o3 = 4.0 / 3.0;
+  const bool mp = mixed(r);
   {
     Tick t(r, F_PC_PREDICT);
-    launch_pc_predict(r->g, r->st, r->fn, r->psi, r->old[2], r->h[0], r->h[1], r->pc, r->pot4, r->uimp,
-                      r->timec, r->den, c4o3 * dt, c112, r->s);
+    if (mp) {
+      launch_pc_predict_mp(r->g, r->stf, r->fn, r->psi32[r->cur32], r->old[2], r->psi32[1 - r->cur32],
+                           static_cast<const float2*>(r->h[0]), static_cast<float2*>(r->h[1]), r->pc,
+                           static_cast<const float*>(r->pot4), static_cast<const float*>(r->uimp), r->timec,
+                           static_cast<float*>(r->den), c4o3 * dt, c112, r->s);
+      r->cur32 = 1 - r->cur32;
+    } else {
+      launch_pc_predict(r->g, r->st, r->fn, r->psi, r->old[2], static_cast<double2*>(r->h[0]),
+                        static_cast<double2*>(r->h[1]), r->pc, static_cast<const double*>(r->pot4),
+                        static_cast<const double*>(r->uimp), r->timec, static_cast<double*>(r->den), c4o3 * dt, c112,
+                        r->s);
+    }
   }
   // old[2] now holds the modified prediction; psi_n becomes psiold(ioldp(3))
   double2* psit = r->old[2];
@@ -414,8 +552,19 @@ void steppc_dev(he4g_run* r, double dt) {
   force_dev(r, 1);
   {
     Tick t(r, F_PC_CORRECT);
-    launch_pc_correct(r->g, r->st, r->fn, psit, r->old[2], r->old[1], r->h[0], r->h[1], r->pc, r->pot4,
-                      r->uimp, r->timec, r->scratch, r->den, r->partials, 3.0 * dt, c9, &r->imp->health, r->s);
+    if (mp) {
+      launch_pc_correct_mp(r->g, r->stf, r->fn, r->psi32[r->cur32], r->old[2], r->old[1],
+                           static_cast<const float2*>(r->h[0]), static_cast<const float2*>(r->h[1]), r->pc,
+                           static_cast<const float*>(r->pot4), static_cast<const float*>(r->uimp), r->timec,
+                           r->scratch, r->psi32[1 - r->cur32], static_cast<float*>(r->den), r->partials, 3.0 * dt, c9,
+                           &r->imp->health, r->s);
+      r->cur32 = 1 - r->cur32;
+    } else {
+      launch_pc_correct(r->g, r->st, r->fn, psit, r->old[2], r->old[1], static_cast<const double2*>(r->h[0]),
+                        static_cast<const double2*>(r->h[1]), r->pc, static_cast<const double*>(r->pot4),
+                        static_cast<const double*>(r->uimp), r->timec, r->scratch, static_cast<double*>(r->den),
+                        r->partials, 3.0 * dt, c9, &r->imp->health, r->s);
+    }
   }
   r->psi = r->scratch;
   r->scratch = psit;
@@ -445,6 +594,28 @@ int sync_err(he4g_run* r, const char* where) {
   return HE4G_OK;
 }
 
+int step_impl(he4g_run* r, int nsteps, cudaEvent_t stop) {
+  if (nsteps < 0) return fail(r, HE4G_EINVAL, "nsteps < 0");
+  for (int s = 0; s < nsteps; ++s) {
+    const int iteraux = r->iter + 1;
+    if (iteraux <= 3 || r->cfg.lrk)
+      steprk_dev(r, r->cfg.deltat);
+    else
+      steppc_dev(r, r->cfg.deltat);
+    evaluate_dev(r);
+    r->iter += 1;
+    {
+      Tick t(r, F_SCALAR);
+      launch_imp_record(r->imp, r->ring, r->iter, r->s);
+    }
+    if (r->timing && (s % 16) == 15) collect_timing(r);
+  }
+  if (stop) cudaEventRecord(stop, r->s);
+  int rc = sync_err(r, "step");
+  if (rc) return rc;
+  return health_check(r);
+}
+
 }  // namespace
 
 // ======================================================================= ABI
@@ -461,10 +632,9 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   he4g_config& c = r->cfg;
   if (c.lsolid) c.core = HE4G_CORE_OT;  // DFT4He3d.f90:476
   auto bad = [&](const std::string& m) {
-    int rc = fail(r, HE4G_EINVAL, m);
     std::fprintf(stderr, "he4g_create: %s\n", m.c_str());
     delete r;
-    return rc;
+    return HE4G_EINVAL;
   };
   if (c.npd != 13 || c.icon != 13) return bad("only npd = 13 and icon = 13 are supported");
   if (c.nx < 16 || c.ny < 16 || c.nz < 16 || c.nx > kMaxN || c.ny > kMaxN || c.nz > kMaxN)
@@ -473,7 +643,9 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   if (!radix_ok(c.nx) || !radix_ok(c.ny) || !radix_ok(c.nz)) return bad("grid sizes must be 2^a 3^b 5^c");
   if (c.core == HE4G_CORE_OTC && !kalfs) return bad("core OTC needs the kalfs table");
   if (c.npot < 2 || !(c.delinter > 0)) return bad("bad potential table");
-  if (c.precision != HE4G_PREC_FP64) return bad("unsupported precision");
+  if (c.precision != HE4G_PREC_FP64 && c.precision != HE4G_PREC_MIXED) return bad("unsupported precision");
+  r->prec = c.precision;
+  r->rs = mixed(r) ? 4 : 8;
   if (cudaStreamCreateWithFlags(&r->s, cudaStreamNonBlocking) != cudaSuccess) return bad("no CUDA device");
 
   Grid& g = r->g;
@@ -504,9 +676,12 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
     for (int k = 0; k <= kStencilHalf; ++k) {
       r->st.d1[a][k] = r1[k] * s1;
       r->st.d2[a][k] = r2[k] * s2;
+      r->stf.d1[a][k] = static_cast<float>(r->st.d1[a][k]);
+      r->stf.d2[a][k] = static_cast<float>(r->st.d2[a][k]);
     }
     r->st.d2c += r->st.d2[a][0];
   }
+  r->stf.d2c = static_cast<float>(r->st.d2c);
   Functional& fn = r->fn;
   fn.h2o2m4 = c.h2o2m4;
   fn.cp4 = c.cp4;
@@ -521,40 +696,41 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   fn.lsolid = c.lsolid;
   fn.otc = c.core == HE4G_CORE_OTC;
 
-  const size_t n = g.n, nh = g.nh;
+  const size_t n = g.n, nh = g.nh, rs = r->rs;
   bool ok = true;
   auto chk = [&](const void* p) { ok = ok && p != nullptr; };
   chk(r->psi = dalloc<double2>(r, n));
   chk(r->scratch = dalloc<double2>(r, n));
   for (int i = 0; i < 3; ++i) chk(r->old[i] = dalloc<double2>(r, n));
-  for (int i = 0; i < 2; ++i) chk(r->h[i] = dalloc<double2>(r, n));
   chk(r->q = dalloc<double2>(r, n));
   chk(r->pc = dalloc<double2>(r, n));
-  chk(r->den = dalloc<double>(r, n));
-  chk(r->pot4 = dalloc<double>(r, n));
-  chk(r->dencg = dalloc<double>(r, n));
-  chk(r->delj4 = dalloc<double>(r, n));
-  chk(r->uimp = dalloc<double>(r, n));
+  for (int i = 0; i < 2; ++i) chk(r->h[i] = dalloc_bytes(r, 2 * rs * n));
+  for (void** p : {&r->den, &r->pot4, &r->dencg, &r->delj4, &r->uimp}) chk(*p = dalloc_bytes(r, rs * n));
   chk(r->timec = dalloc<float>(r, n));
-  chk(r->spec0 = dalloc<double2>(r, nh));
-  chk(r->spec1 = dalloc<double2>(r, nh));
-  chk(r->fvlj4 = dalloc<double>(r, nh, false));
-  chk(r->wcgk = dalloc<double>(r, nh, false));
-  chk(r->potion = dalloc<double>(r, c.npot, false));
+  chk(r->spec0 = dalloc_bytes(r, 2 * rs * nh));
+  chk(r->spec1 = dalloc_bytes(r, 2 * rs * nh));
+  chk(r->fvlj4 = dalloc_bytes(r, rs * nh, false));
+  chk(r->wcgk = dalloc_bytes(r, rs * nh, false));
+  chk(r->potion = dalloc_bytes(r, rs * c.npot, false));
   chk(r->xs = dalloc<double>(r, c.nx, false));
   chk(r->ys = dalloc<double>(r, c.ny, false));
   chk(r->zs = dalloc<double>(r, c.nz, false));
-  chk(r->dx = dalloc<double>(r, n));
-  chk(r->dy = dalloc<double>(r, n));
-  chk(r->dz = dalloc<double>(r, n));
+  for (void** p : {&r->dx, &r->dy, &r->dz}) chk(*p = dalloc_bytes(r, rs * n));
+  if (mixed(r)) {
+    for (int i = 0; i < 2; ++i) chk(r->psi32[i] = dalloc<float2>(r, n));
+    chk(r->xsf = dalloc<float>(r, c.nx, false));
+    chk(r->ysf = dalloc<float>(r, c.ny, false));
+    chk(r->zsf = dalloc<float>(r, c.nz, false));
+  }
   if (fn.otc) {
-    chk(r->spec2 = dalloc<double2>(r, nh));
-    chk(r->kalfs = dalloc<double>(r, nh, false));
-    for (double** p : {&r->denalf, &r->falfs, &r->ix, &r->iy, &r->iz, &r->ualphas, &r->t1, &r->t2, &r->t3,
-                       &r->t4, &r->t5, &r->t6})
-      chk(*p = dalloc<double>(r, n));
+    chk(r->spec2 = dalloc_bytes(r, 2 * rs * nh));
+    chk(r->kalfs = dalloc_bytes(r, rs * nh, false));
+    for (void** p : {&r->denalf, &r->falfs, &r->ix, &r->iy, &r->iz, &r->ualphas, &r->t1, &r->t2, &r->t3, &r->t4,
+                     &r->t5, &r->t6})
+      chk(*p = dalloc_bytes(r, rs * n));
   }
   r->pblocks = pc_blocks(g);
+  r->fblocks = force_blocks_mp(g);
   chk(r->partials = dalloc<double>(r, (size_t)r->pblocks * 12));
   chk(r->small = dalloc<double>(r, 64));
   chk(r->imp = dalloc<ImpState>(r, 1));
@@ -563,10 +739,10 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
     he4g_destroy(r);
     return HE4G_ENOMEM;
   }
-  cudaMemcpyAsync(r->fvlj4, fvlj4, sizeof(double) * nh, cudaMemcpyHostToDevice, r->s);
-  cudaMemcpyAsync(r->wcgk, wcgk, sizeof(double) * nh, cudaMemcpyHostToDevice, r->s);
-  if (fn.otc) cudaMemcpyAsync(r->kalfs, kalfs, sizeof(double) * nh, cudaMemcpyHostToDevice, r->s);
-  cudaMemcpyAsync(r->potion, potion, sizeof(double) * c.npot, cudaMemcpyHostToDevice, r->s);
+  upload_field(r, r->fvlj4, fvlj4, nh);
+  upload_field(r, r->wcgk, wcgk, nh);
+  if (fn.otc) upload_field(r, r->kalfs, kalfs, nh);
+  upload_field(r, r->potion, potion, c.npot);
   // grids (DFT4He3d.f90:303-313) and the absorber (:689-699), its real part
   // rounded to single precision as the reference's default-kind CMPLX does
   std::vector<double> x(c.nx), y(c.ny), z(c.nz), tx(c.nx), ty(c.ny), tz(c.nz);
@@ -592,25 +768,35 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   cudaMemcpyAsync(r->ys, y.data(), sizeof(double) * c.ny, cudaMemcpyHostToDevice, r->s);
   cudaMemcpyAsync(r->zs, z.data(), sizeof(double) * c.nz, cudaMemcpyHostToDevice, r->s);
   cudaMemcpyAsync(r->timec, tc.data(), sizeof(float) * n, cudaMemcpyHostToDevice, r->s);
+  std::vector<float> xf(x.begin(), x.end()), yf(y.begin(), y.end()), zf(z.begin(), z.end());
+  if (mixed(r)) {
+    cudaMemcpyAsync(r->xsf, xf.data(), sizeof(float) * c.nx, cudaMemcpyHostToDevice, r->s);
+    cudaMemcpyAsync(r->ysf, yf.data(), sizeof(float) * c.ny, cudaMemcpyHostToDevice, r->s);
+    cudaMemcpyAsync(r->zsf, zf.data(), sizeof(float) * c.nz, cudaMemcpyHostToDevice, r->s);
+  }
   cudaStreamSynchronize(r->s);  // the host vectors go out of scope below
-  std::vector<void*> hold;
-  make_axis(r, r->plan.xh, c.nx / 2, hold);
-  make_axis(r, r->plan.y, c.ny, hold);
-  make_axis(r, r->plan.z, c.nz, hold);
+  make_axis(r, r->plan.xh, c.nx / 2);
+  make_axis(r, r->plan.y, c.ny);
+  make_axis(r, r->plan.z, c.nz);
   {
     std::vector<double2> twx(c.nx / 2);
+    std::vector<float2> twxf(c.nx / 2);
     for (int k = 0; k < c.nx / 2; ++k) {
       const long double a = 2.0L * 3.141592653589793238462643383279502884L * k / c.nx;
       twx[k] = make_double2(static_cast<double>(cosl(a)), static_cast<double>(-sinl(a)));
+      twxf[k] = make_float2(static_cast<float>(cosl(a)), static_cast<float>(-sinl(a)));
     }
     double2* d = dalloc<double2>(r, c.nx / 2, false);
-    if (!d) {
+    float2* df = dalloc<float2>(r, c.nx / 2, false);
+    if (!d || !df) {
       he4g_destroy(r);
       return HE4G_ENOMEM;
     }
     cudaMemcpyAsync(d, twx.data(), sizeof(double2) * (c.nx / 2), cudaMemcpyHostToDevice, r->s);
+    cudaMemcpyAsync(df, twxf.data(), sizeof(float2) * (c.nx / 2), cudaMemcpyHostToDevice, r->s);
     cudaStreamSynchronize(r->s);
     r->plan.twx = d;
+    r->plan.twxf = df;
   }
   cudaError_t e = cudaStreamSynchronize(r->s);
   if (e == cudaSuccess) e = cudaGetLastError();
@@ -641,8 +827,6 @@ int he4g_set_state(he4g_run* r, const double* psi, const double rimp[3], const d
   const size_t n = r->g.n;
   cudaError_t e = cudaMemcpyAsync(r->psi, psi, sizeof(double2) * n, cudaMemcpyHostToDevice, r->s);
   if (e != cudaSuccess) return cuda_fail(r, e, "set_state");
-  // den = conjg(psi)*psi: any stage that has den as output runs |psi|^2;
-  // a zero-step RK stage would change psi, so compute den directly
   cudaMemsetAsync(r->q, 0, sizeof(double2) * n, r->s);
   cudaMemsetAsync(r->pc, 0, sizeof(double2) * n, r->s);
   ImpState h{};
@@ -654,7 +838,12 @@ int he4g_set_state(he4g_run* r, const double* psi, const double rimp[3], const d
   for (int a = 0; a < 3; ++a) h.ioldr[a] = h.ioldv[a] = a;
   for (int a = 0; a < 2; ++a) h.iolda[a] = a;
   cudaMemcpyAsync(r->imp, &h, sizeof h, cudaMemcpyHostToDevice, r->s);
-  launch_density(r->g, r->psi, r->den, r->s);
+  if (mixed(r)) {
+    r->cur32 = 0;
+    launch_split_mp(r->g, r->psi, r->psi32[0], static_cast<float*>(r->den), r->s);
+  } else {
+    launch_density(r->g, r->psi, static_cast<double*>(r->den), r->s);
+  }
   r->iter = 0;
   r->have_state = true;
   r->ring_read = 0;
@@ -733,38 +922,6 @@ int he4g_step(he4g_run* r, int nsteps, double* errHe, double* errimp) {
   return rc;
 }
 
-}  // extern "C"
-
-namespace {
-int step_impl(he4g_run* r, int nsteps, cudaEvent_t stop) {
-  if (nsteps < 0) return fail(r, HE4G_EINVAL, "nsteps < 0");
-  for (int s = 0; s < nsteps; ++s) {
-    const int iteraux = r->iter + 1;
-    if (iteraux <= 3 || r->cfg.lrk)
-      steprk_dev(r, r->cfg.deltat);
-    else
-      steppc_dev(r, r->cfg.deltat);
-    evaluate_dev(r);
-    r->iter += 1;
-    {
-      Tick t(r, F_SCALAR);
-      launch_imp_record(r->imp, r->ring, r->iter, r->s);
-    }
-    if (r->timing && (s % 16) == 15) collect_timing(r);
-  }
-  if (stop) cudaEventRecord(stop, r->s);
-  int rc = sync_err(r, "step");
-  if (rc) return rc;
-  return health_check(r);
-}
-}  // namespace
-
-extern "C" {
-
-int he4g_steps_taken(const he4g_run* r) { return r ? r->iter : -1; }
-
-long long he4g_launch_count(const he4g_run* r) { return r ? r->launches : -1; }
-
 int he4g_step_timed(he4g_run* r, int nsteps, double* device_ms) {
   int rc = check_ready(r);
   if (rc) return rc;
@@ -772,9 +929,7 @@ int he4g_step_timed(he4g_run* r, int nsteps, double* device_ms) {
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   cudaEventRecord(a, r->s);
-  const bool was = r->timing;
   rc = step_impl(r, nsteps, b);
-  r->timing = was;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, a, b);
   cudaEventDestroy(a);
@@ -782,6 +937,10 @@ int he4g_step_timed(he4g_run* r, int nsteps, double* device_ms) {
   if (device_ms) *device_ms = ms;
   return rc;
 }
+
+int he4g_steps_taken(const he4g_run* r) { return r ? r->iter : -1; }
+
+long long he4g_launch_count(const he4g_run* r) { return r ? r->launches : -1; }
 
 int he4g_get_trajectory(he4g_run* r, double* rows, int cap, int* n) {
   if (!r || !rows || !n || cap < 0) return HE4G_EINVAL;
@@ -815,33 +974,35 @@ int he4g_get_psi(he4g_run* r, double* psi) {
 
 int he4g_get_den(he4g_run* r, double* den) {
   if (!r || !den) return HE4G_EINVAL;
-  cudaError_t e = cudaMemcpyAsync(den, r->den, sizeof(double) * r->g.n, cudaMemcpyDeviceToHost, r->s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
-  return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "get_den");
+  return download_field(r, r->den, den, r->g.n, "get_den");
 }
 
 int he4g_get_field(he4g_run* r, int which, double* out) {
   if (!r || !out) return HE4G_EINVAL;
-  const double* src = nullptr;
+  const void* src = nullptr;
   switch (which) {
     case 0: src = r->pot4; break;
     case 1: src = r->dencg; break;
-    case 2: src = r->delj4; break;
+    case 2:
+      if (!r->have_state) return fail(r, HE4G_ESTATE, "set_state has not been called");
+      delj4_dev(r);
+      src = r->delj4;
+      break;
     case 3: src = r->uimp; break;
     case 4:
     case 5:
-    case 6:
-      launch_grad1(r->g, r->st, which - 4, r->den, which == 4 ? r->dx : which == 5 ? r->dy : r->dz, r->s);
-      src = which == 4 ? r->dx : which == 5 ? r->dy : r->dz;
+    case 6: {
+      void* d = which == 4 ? r->dx : which == 5 ? r->dy : r->dz;
+      grad1_dev(r, which - 4, r->den, d);
+      src = d;
       break;
+    }
     case 7: src = r->ualphas; break;
     case 8: src = r->denalf; break;
     default: return fail(r, HE4G_EINVAL, "unknown field");
   }
   if (!src) return fail(r, HE4G_EINVAL, "field not available for this core");
-  cudaError_t e = cudaMemcpyAsync(out, src, sizeof(double) * r->g.n, cudaMemcpyDeviceToHost, r->s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
-  return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "get_field");
+  return download_field(r, src, out, r->g.n, "get_field");
 }
 
 int he4g_get_impurity(he4g_run* r, double rr[3], double v[3], double a[3]) {
@@ -881,8 +1042,22 @@ int he4g_energy(he4g_run* r, he4g_energies* en) {
   if (!en) return HE4G_EINVAL;
   const Grid& g = r->g;
   const bool otc = r->fn.otc;
-  launch_energy_point(g, r->fn, r->den, r->dencg, r->delj4, r->uimp, otc ? r->falfs : nullptr, r->dx, r->dy,
-                      r->dz, r->ix, r->iy, r->iz, r->xs, r->ys, r->zs, r->partials, r->s);
+  delj4_dev(r);
+  if (mixed(r)) {
+    launch_energy_point_mp(g, r->fn, static_cast<const float*>(r->den), static_cast<const float*>(r->dencg),
+                           static_cast<const float*>(r->delj4), static_cast<const float*>(r->uimp),
+                           otc ? static_cast<const float*>(r->falfs) : nullptr, static_cast<const float*>(r->dx),
+                           static_cast<const float*>(r->dy), static_cast<const float*>(r->dz),
+                           static_cast<const float*>(r->ix), static_cast<const float*>(r->iy),
+                           static_cast<const float*>(r->iz), r->xs, r->ys, r->zs, r->partials, r->s);
+  } else {
+    launch_energy_point(g, r->fn, static_cast<const double*>(r->den), static_cast<const double*>(r->dencg),
+                        static_cast<const double*>(r->delj4), static_cast<const double*>(r->uimp),
+                        otc ? static_cast<const double*>(r->falfs) : nullptr, static_cast<const double*>(r->dx),
+                        static_cast<const double*>(r->dy), static_cast<const double*>(r->dz),
+                        static_cast<const double*>(r->ix), static_cast<const double*>(r->iy),
+                        static_cast<const double*>(r->iz), r->xs, r->ys, r->zs, r->partials, r->s);
+  }
   launch_reduce(r->partials, r->pblocks, 12, r->small, r->s);
   cudaMemsetAsync(r->small + 40, 0, sizeof(double) * 3, r->s);
   launch_energy_grad(g, r->st, r->psi, r->xs, r->ys, r->zs, r->small + 40, r->partials, r->s);
@@ -919,8 +1094,16 @@ int he4g_observables(he4g_run* r, double npart, he4g_obs* o) {
   if (rc) return rc;
   if (!o) return HE4G_EINVAL;
   const Grid& g = r->g;
-  launch_energy_point(g, r->fn, r->den, r->dencg, r->delj4, r->uimp, nullptr, r->dx, r->dy, r->dz, r->ix,
-                      r->iy, r->iz, r->xs, r->ys, r->zs, r->partials, r->s);
+  delj4_dev(r);
+  if (mixed(r)) {
+    launch_energy_point_mp(g, r->fn, static_cast<const float*>(r->den), static_cast<const float*>(r->dencg),
+                           static_cast<const float*>(r->delj4), static_cast<const float*>(r->uimp), nullptr, nullptr,
+                           nullptr, nullptr, nullptr, nullptr, nullptr, r->xs, r->ys, r->zs, r->partials, r->s);
+  } else {
+    launch_energy_point(g, r->fn, static_cast<const double*>(r->den), static_cast<const double*>(r->dencg),
+                        static_cast<const double*>(r->delj4), static_cast<const double*>(r->uimp), nullptr, nullptr,
+                        nullptr, nullptr, nullptr, nullptr, nullptr, r->xs, r->ys, r->zs, r->partials, r->s);
+  }
   launch_reduce(r->partials, r->pblocks, 12, r->small, r->s);
   double v[12];
   cudaMemcpyAsync(v, r->small, sizeof v, cudaMemcpyDeviceToHost, r->s);

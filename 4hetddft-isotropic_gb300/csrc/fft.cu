@@ -1,13 +1,17 @@
-// fft.cu — FP64 3D real FFT convolutions of the mean field on sm_103a.
+// fft.cu — 3D real FFT convolutions of the mean field on sm_103a, in FP64
+// (the reference's arithmetic) or FP32 (the mixed-precision form).
 //
 // Replaces the FFTW plans of fft.f90:5-153 and the k-space products of
 // poten.f90:27-74 / term_alfa.f90:41-80. A 3D transform is three batched
 // line passes (x, y, z); every pass stages whole lines in shared memory and
 // runs a mixed-radix (8, 4, 2, 3, 5) Stockham FFT there, so HBM is touched
 // once per pass. The z pass is fused with the k-space product and the inverse
-// z transform (forward -> x form factor(s) -> inverse with one read and one
-// write of the spectrum), and may emit several products of one spectrum (the
-// coarse-grained density and the Lennard-Jones field share rho-hat).
+// z transform (forward -> x form factor(s) -> inverse, one read and one write
+// of the spectrum), may emit several products of one spectrum (the
+// coarse-grained density and the Lennard-Jones field share rho-hat), and may
+// add a second, already z-inverted spectrum to its output (the Lennard-Jones
+// and correlation fields are summed there, before one shared inverse y/x
+// pass).
 //
 // Real transforms along x pack a length-nx real line into a length-nx/2
 // complex line and untangle the halves afterwards. Scale conventions: the
@@ -23,156 +27,196 @@ namespace he4g {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kTileCols = 8;  // kx columns per y/z block
 
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+template <typename R>
+struct Cx;
+template <>
+struct Cx<double> {
+  using T = double2;
+  static constexpr int kTile = 8;  // kx columns per y/z block: 128-byte rows
+};
+template <>
+struct Cx<float> {
+  using T = float2;
+  static constexpr int kTile = 16;
+};
+template <typename R>
+using C2 = typename Cx<R>::T;
+
+template <typename R>
+__device__ __forceinline__ C2<R> mk(R x, R y) {
+  C2<R> c;
+  c.x = x;
+  c.y = y;
+  return c;
+}
+template <typename R>
+__device__ __forceinline__ C2<R> cadd(C2<R> a, C2<R> b) { return mk<R>(a.x + b.x, a.y + b.y); }
+template <typename R>
+__device__ __forceinline__ C2<R> csub(C2<R> a, C2<R> b) { return mk<R>(a.x - b.x, a.y - b.y); }
+template <typename R>
+__device__ __forceinline__ C2<R> cconj(C2<R> a) { return mk<R>(a.x, -a.y); }
 
 // a * w (SIGN < 0) or a * conj(w) (SIGN > 0)
-template <int SIGN>
-__device__ __forceinline__ double2 mulw(double2 a, double2 w) {
-  if (SIGN < 0) return make_double2(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
-  return make_double2(fma(a.x, w.x, a.y * w.y), fma(a.y, w.x, -a.x * w.y));
+template <typename R, int SIGN>
+__device__ __forceinline__ C2<R> mulw(C2<R> a, C2<R> w) {
+  if (SIGN < 0) return mk<R>(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
+  return mk<R>(fma(a.x, w.x, a.y * w.y), fma(a.y, w.x, -a.x * w.y));
 }
 // a * (SIGN * i)
-template <int SIGN>
-__device__ __forceinline__ double2 jmul(double2 a) {
-  return SIGN < 0 ? make_double2(a.y, -a.x) : make_double2(-a.y, a.x);
+template <typename R, int SIGN>
+__device__ __forceinline__ C2<R> jmul(C2<R> a) {
+  return SIGN < 0 ? mk<R>(a.y, -a.x) : mk<R>(-a.y, a.x);
 }
 
-template <int SIGN>
-__device__ __forceinline__ void bf2(double2* v) {
-  double2 t = v[0];
-  v[0] = cadd(t, v[1]);
-  v[1] = csub(t, v[1]);
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf2(C2<R>* v) {
+  C2<R> t = v[0];
+  v[0] = cadd<R>(t, v[1]);
+  v[1] = csub<R>(t, v[1]);
 }
-template <int SIGN>
-__device__ __forceinline__ void bf4(double2& a0, double2& a1, double2& a2, double2& a3) {
-  double2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
-  double2 t2 = cadd(a1, a3), t3 = jmul<SIGN>(csub(a1, a3));
-  a0 = cadd(t0, t2);
-  a2 = csub(t0, t2);
-  a1 = cadd(t1, t3);
-  a3 = csub(t1, t3);
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf4(C2<R>& a0, C2<R>& a1, C2<R>& a2, C2<R>& a3) {
+  C2<R> t0 = cadd<R>(a0, a2), t1 = csub<R>(a0, a2);
+  C2<R> t2 = cadd<R>(a1, a3), t3 = jmul<R, SIGN>(csub<R>(a1, a3));
+  a0 = cadd<R>(t0, t2);
+  a2 = csub<R>(t0, t2);
+  a1 = cadd<R>(t1, t3);
+  a3 = csub<R>(t1, t3);
 }
-template <int SIGN>
-__device__ __forceinline__ void bf8(double2* v) {
-  const double r = 0.70710678118654752440;
-  double2 a0 = v[0], a1 = v[2], a2 = v[4], a3 = v[6];
-  double2 b0 = v[1], b1 = v[3], b2 = v[5], b3 = v[7];
-  bf4<SIGN>(a0, a1, a2, a3);
-  bf4<SIGN>(b0, b1, b2, b3);
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf8(C2<R>* v) {
+  const R r = (R)0.70710678118654752440;
+  C2<R> a0 = v[0], a1 = v[2], a2 = v[4], a3 = v[6];
+  C2<R> b0 = v[1], b1 = v[3], b2 = v[5], b3 = v[7];
+  bf4<R, SIGN>(a0, a1, a2, a3);
+  bf4<R, SIGN>(b0, b1, b2, b3);
   if (SIGN < 0) {
-    b1 = make_double2((b1.x + b1.y) * r, (b1.y - b1.x) * r);
-    b3 = make_double2((b3.y - b3.x) * r, -(b3.x + b3.y) * r);
+    b1 = mk<R>((b1.x + b1.y) * r, (b1.y - b1.x) * r);
+    b3 = mk<R>((b3.y - b3.x) * r, -(b3.x + b3.y) * r);
   } else {
-    b1 = make_double2((b1.x - b1.y) * r, (b1.y + b1.x) * r);
-    b3 = make_double2(-(b3.x + b3.y) * r, (b3.x - b3.y) * r);
+    b1 = mk<R>((b1.x - b1.y) * r, (b1.y + b1.x) * r);
+    b3 = mk<R>(-(b3.x + b3.y) * r, (b3.x - b3.y) * r);
   }
-  b2 = jmul<SIGN>(b2);
-  v[0] = cadd(a0, b0);
-  v[4] = csub(a0, b0);
-  v[1] = cadd(a1, b1);
-  v[5] = csub(a1, b1);
-  v[2] = cadd(a2, b2);
-  v[6] = csub(a2, b2);
-  v[3] = cadd(a3, b3);
-  v[7] = csub(a3, b3);
+  b2 = jmul<R, SIGN>(b2);
+  v[0] = cadd<R>(a0, b0);
+  v[4] = csub<R>(a0, b0);
+  v[1] = cadd<R>(a1, b1);
+  v[5] = csub<R>(a1, b1);
+  v[2] = cadd<R>(a2, b2);
+  v[6] = csub<R>(a2, b2);
+  v[3] = cadd<R>(a3, b3);
+  v[7] = csub<R>(a3, b3);
 }
-template <int SIGN>
-__device__ __forceinline__ void bf3(double2* v) {
-  const double s3 = 0.86602540378443864676;  // sin(2 pi / 3)
-  double2 b = cadd(v[1], v[2]);
-  double2 d = csub(v[1], v[2]);
-  double2 t = make_double2(fma(-0.5, b.x, v[0].x), fma(-0.5, b.y, v[0].y));
-  double2 s = jmul<SIGN>(make_double2(s3 * d.x, s3 * d.y));
-  v[0] = cadd(v[0], b);
-  v[1] = cadd(t, s);
-  v[2] = csub(t, s);
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf3(C2<R>* v) {
+  const R s3 = (R)0.86602540378443864676;  // sin(2 pi / 3)
+  C2<R> b = cadd<R>(v[1], v[2]);
+  C2<R> d = csub<R>(v[1], v[2]);
+  C2<R> t = mk<R>(fma((R)-0.5, b.x, v[0].x), fma((R)-0.5, b.y, v[0].y));
+  C2<R> s = jmul<R, SIGN>(mk<R>(s3 * d.x, s3 * d.y));
+  v[0] = cadd<R>(v[0], b);
+  v[1] = cadd<R>(t, s);
+  v[2] = csub<R>(t, s);
 }
-template <int SIGN>
-__device__ __forceinline__ void bf5(double2* v) {
-  const double c1 = 0.30901699437494742410, c2 = -0.80901699437494742410;  // cos(2pi/5), cos(4pi/5)
-  const double s1 = 0.95105651629515357212, s2 = 0.58778525229247312917;   // sin(2pi/5), sin(4pi/5)
-  double2 b1 = cadd(v[1], v[4]), b2 = cadd(v[2], v[3]);
-  double2 d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
-  double2 a0 = v[0];
-  double2 t1 = make_double2(fma(c2, b2.x, fma(c1, b1.x, a0.x)), fma(c2, b2.y, fma(c1, b1.y, a0.y)));
-  double2 t2 = make_double2(fma(c1, b2.x, fma(c2, b1.x, a0.x)), fma(c1, b2.y, fma(c2, b1.y, a0.y)));
-  double2 u1 = make_double2(fma(s2, d2.x, s1 * d1.x), fma(s2, d2.y, s1 * d1.y));
-  double2 u2 = make_double2(fma(-s1, d2.x, s2 * d1.x), fma(-s1, d2.y, s2 * d1.y));
-  u1 = jmul<SIGN>(u1);
-  u2 = jmul<SIGN>(u2);
-  v[0] = make_double2(a0.x + b1.x + b2.x, a0.y + b1.y + b2.y);
-  v[1] = cadd(t1, u1);
-  v[4] = csub(t1, u1);
-  v[2] = cadd(t2, u2);
-  v[3] = csub(t2, u2);
-}
-
-template <int R, int SIGN>
-__device__ __forceinline__ void butterfly(double2* v) {
-  if (R == 2) bf2<SIGN>(v);
-  if (R == 3) bf3<SIGN>(v);
-  if (R == 4) bf4<SIGN>(v[0], v[1], v[2], v[3]);
-  if (R == 5) bf5<SIGN>(v);
-  if (R == 8) bf8<SIGN>(v);
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf5(C2<R>* v) {
+  const R c1 = (R)0.30901699437494742410, c2 = (R)-0.80901699437494742410;  // cos(2pi/5), cos(4pi/5)
+  const R s1 = (R)0.95105651629515357212, s2 = (R)0.58778525229247312917;   // sin(2pi/5), sin(4pi/5)
+  C2<R> b1 = cadd<R>(v[1], v[4]), b2 = cadd<R>(v[2], v[3]);
+  C2<R> d1 = csub<R>(v[1], v[4]), d2 = csub<R>(v[2], v[3]);
+  C2<R> a0 = v[0];
+  C2<R> t1 = mk<R>(fma(c2, b2.x, fma(c1, b1.x, a0.x)), fma(c2, b2.y, fma(c1, b1.y, a0.y)));
+  C2<R> t2 = mk<R>(fma(c1, b2.x, fma(c2, b1.x, a0.x)), fma(c1, b2.y, fma(c2, b1.y, a0.y)));
+  C2<R> u1 = mk<R>(fma(s2, d2.x, s1 * d1.x), fma(s2, d2.y, s1 * d1.y));
+  C2<R> u2 = mk<R>(fma(-s1, d2.x, s2 * d1.x), fma(-s1, d2.y, s2 * d1.y));
+  u1 = jmul<R, SIGN>(u1);
+  u2 = jmul<R, SIGN>(u2);
+  v[0] = mk<R>(a0.x + b1.x + b2.x, a0.y + b1.y + b2.y);
+  v[1] = cadd<R>(t1, u1);
+  v[4] = csub<R>(t1, u1);
+  v[2] = cadd<R>(t2, u2);
+  v[3] = csub<R>(t2, u2);
 }
 
-// One Stockham pass of radix R over `nlines` lines of length n held in shared
-// memory at src + l*ld (natural order in, autosorted order out).
-template <int R, int SIGN>
-__device__ __forceinline__ void stockham_pass(const double2* __restrict__ src, double2* __restrict__ dst,
-                                              int n, int ns, int nlines, int ld,
-                                              const double2* __restrict__ tw) {
-  const int nr = n / R;
-  const int tstep = n / (ns * R);
+template <typename R, int RAD, int SIGN>
+__device__ __forceinline__ void butterfly(C2<R>* v) {
+  if (RAD == 2) bf2<R, SIGN>(v);
+  if (RAD == 3) bf3<R, SIGN>(v);
+  if (RAD == 4) bf4<R, SIGN>(v[0], v[1], v[2], v[3]);
+  if (RAD == 5) bf5<R, SIGN>(v);
+  if (RAD == 8) bf8<R, SIGN>(v);
+}
+
+template <typename R>
+__device__ __forceinline__ const C2<R>* twiddles(const FftAxis& ax);
+template <>
+__device__ __forceinline__ const double2* twiddles<double>(const FftAxis& ax) {
+  return ax.tw;
+}
+template <>
+__device__ __forceinline__ const float2* twiddles<float>(const FftAxis& ax) {
+  return ax.twf;
+}
+
+// One Stockham pass of radix RAD over `nlines` lines of length n held in
+// shared memory at src + l*ld (natural order in, autosorted order out).
+template <typename R, int RAD, int SIGN>
+__device__ __forceinline__ void stockham_pass(const C2<R>* __restrict__ src, C2<R>* __restrict__ dst, int n,
+                                              int ns, int nlines, int ld, const C2<R>* __restrict__ tw) {
+  const int nr = n / RAD;
+  const int tstep = n / (ns * RAD);
   const int total = nlines * nr;
   for (int w = threadIdx.x; w < total; w += blockDim.x) {
     const int l = w / nr;
     const int j = w - l * nr;
     const int k = j % ns;
-    const double2* s = src + l * ld;
-    double2 v[R];
+    const C2<R>* s = src + l * ld;
+    C2<R> v[RAD];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = s[j + r * nr];
+    for (int r = 0; r < RAD; ++r) v[r] = s[j + r * nr];
     if (k > 0) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = mulw<SIGN>(v[r], __ldg(&tw[r * k * tstep]));
+      for (int r = 1; r < RAD; ++r) v[r] = mulw<R, SIGN>(v[r], __ldg(&tw[r * k * tstep]));
     }
-    butterfly<R, SIGN>(v);
-    const int idx = (j / ns) * ns * R + k;
-    double2* d = dst + l * ld;
+    butterfly<R, RAD, SIGN>(v);
+    const int idx = (j / ns) * ns * RAD + k;
+    C2<R>* d = dst + l * ld;
 #pragma unroll
-    for (int r = 0; r < R; ++r) d[idx + r * ns] = v[r];
+    for (int r = 0; r < RAD; ++r) d[idx + r * ns] = v[r];
   }
 }
 
 // Full transform of nlines lines; a holds the input, b is scratch; returns
 // the buffer that holds the result. Ends with a barrier.
-template <int SIGN>
-__device__ double2* fft_smem(double2* a, double2* b, int nlines, int ld, const FftAxis& ax) {
+template <typename R, int SIGN>
+__device__ C2<R>* fft_smem(C2<R>* a, C2<R>* b, int nlines, int ld, const FftAxis& ax) {
+  const C2<R>* tw = twiddles<R>(ax);
   int ns = 1;
   for (int f = 0; f < ax.nf; ++f) {
-    const int R = ax.fac[f];
-    if (R == 8)
-      stockham_pass<8, SIGN>(a, b, ax.n, ns, nlines, ld, ax.tw);
-    else if (R == 4)
-      stockham_pass<4, SIGN>(a, b, ax.n, ns, nlines, ld, ax.tw);
-    else if (R == 2)
-      stockham_pass<2, SIGN>(a, b, ax.n, ns, nlines, ld, ax.tw);
-    else if (R == 3)
-      stockham_pass<3, SIGN>(a, b, ax.n, ns, nlines, ld, ax.tw);
+    const int rad = ax.fac[f];
+    if (rad == 8)
+      stockham_pass<R, 8, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
+    else if (rad == 4)
+      stockham_pass<R, 4, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
+    else if (rad == 2)
+      stockham_pass<R, 2, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
+    else if (rad == 3)
+      stockham_pass<R, 3, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
     else
-      stockham_pass<5, SIGN>(a, b, ax.n, ns, nlines, ld, ax.tw);
+      stockham_pass<R, 5, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
     __syncthreads();
-    double2* t = a;
+    C2<R>* t = a;
     a = b;
     b = t;
-    ns *= R;
+    ns *= rad;
   }
   return a;
+}
+
+template <typename R>
+__device__ __forceinline__ C2<R> ld_pair(const R* p) {
+  return __ldg(reinterpret_cast<const C2<R>*>(p));
 }
 
 // ------------------------------------------------------------------ x pass
@@ -180,81 +224,84 @@ enum { PRO_PLAIN = 0, PRO_CORR = 1, PRO_PROD = 2 };
 
 // Forward real transform along x of ny*nz lines. Output: 2*DFT_x in the half
 // spectrum (nxh, ny, nz).
-template <int PRO>
-__global__ void __launch_bounds__(kThreads) k_x_r2c(Grid g, FftAxis ax, const double2* __restrict__ twx,
-                                                    const double* __restrict__ in0,
-                                                    const double* __restrict__ in1, double c0, double c1,
-                                                    double2* __restrict__ out, int lpb) {
-  extern __shared__ double2 sm[];
+template <typename R, int PRO>
+__global__ void __launch_bounds__(kThreads) k_x_r2c(Grid g, FftAxis ax, const C2<R>* __restrict__ twx,
+                                                    const R* __restrict__ in0, const R* __restrict__ in1, R c0,
+                                                    R c1, C2<R>* __restrict__ out, int lpb) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
   const int m = ax.n;
   const int ld = m + 1;
-  double2* a = sm;
-  double2* b = sm + lpb * ld;
+  C2<R>* a = sm;
+  C2<R>* b = sm + lpb * ld;
   const long long nlines = (long long)g.ny * g.nz;
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
   for (int w = threadIdx.x; w < nl * m; w += blockDim.x) {
     const int l = w / m, j = w - l * m;
-    const long long e = (l0 + l) * g.nx + 2 * j;  // even: 16-byte aligned
-    double2 v;
+    const long long e = (l0 + l) * g.nx + 2 * j;  // even: aligned pair
+    C2<R> v;
     if (PRO == PRO_PLAIN) {
-      v = __ldg(reinterpret_cast<const double2*>(in0 + e));
+      v = ld_pair<R>(in0 + e);
     } else if (PRO == PRO_CORR) {
       // g = den*dencg*(cp4 + cpp4*dencg) (poten.f90:62-64)
-      double2 d = __ldg(reinterpret_cast<const double2*>(in0 + e));
-      double2 c = __ldg(reinterpret_cast<const double2*>(in1 + e));
-      v = make_double2(d.x * c.x * fma(c1, c.x, c0), d.y * c.y * fma(c1, c.y, c0));
+      const C2<R> d = ld_pair<R>(in0 + e);
+      const C2<R> c = ld_pair<R>(in1 + e);
+      v = mk<R>(d.x * c.x * fma(c1, c.x, c0), d.y * c.y * fma(c1, c.y, c0));
     } else {
-      double2 p = __ldg(reinterpret_cast<const double2*>(in0 + e));
-      double2 q = __ldg(reinterpret_cast<const double2*>(in1 + e));
-      v = make_double2(p.x * q.x, p.y * q.y);
+      const C2<R> p = ld_pair<R>(in0 + e);
+      const C2<R> q = ld_pair<R>(in1 + e);
+      v = mk<R>(p.x * q.x, p.y * q.y);
     }
     a[l * ld + j] = v;
   }
   __syncthreads();
-  double2* r = fft_smem<-1>(a, b, nl, ld, ax);
+  C2<R>* r = fft_smem<R, -1>(a, b, nl, ld, ax);
   // untangle: 2X[k] = Fe + W^k (-i) Fo, 2X[m-k] = conj(Fe - W^k (-i) Fo)
   const int half = m / 2;
   for (int w = threadIdx.x; w < nl * (half + 1); w += blockDim.x) {
     const int l = w / (half + 1), k = w - l * (half + 1);
-    const double2 zk = r[l * ld + k];
-    const double2 zm = r[l * ld + (k == 0 ? 0 : m - k)];
-    double2* o = out + (l0 + l) * g.nxh;
+    const C2<R> zk = r[l * ld + k];
+    const C2<R> zm = r[l * ld + (k == 0 ? 0 : m - k)];
+    C2<R>* o = out + (l0 + l) * g.nxh;
     if (k == 0) {
-      o[0] = make_double2(2.0 * (zk.x + zk.y), 0.0);
-      o[m] = make_double2(2.0 * (zk.x - zk.y), 0.0);
+      o[0] = mk<R>((R)2 * (zk.x + zk.y), (R)0);
+      o[m] = mk<R>((R)2 * (zk.x - zk.y), (R)0);
       continue;
     }
-    const double2 fe = cadd(zk, cconj(zm));
-    const double2 fo = jmul<-1>(csub(zk, cconj(zm)));
-    const double2 t = mulw<-1>(fo, __ldg(&twx[k]));
-    o[k] = cadd(fe, t);
-    o[m - k] = cconj(csub(fe, t));
+    const C2<R> fe = cadd<R>(zk, cconj<R>(zm));
+    const C2<R> fo = jmul<R, -1>(csub<R>(zk, cconj<R>(zm)));
+    const C2<R> t = mulw<R, -1>(fo, __ldg(&twx[k]));
+    o[k] = cadd<R>(fe, t);
+    o[m - k] = cconj<R>(csub<R>(fe, t));
   }
 }
 
 enum { EPI_STORE = 0, EPI_POT4 = 1 };
 
+template <typename R>
 struct Pot4Args {
-  const double* delj4;
-  const double* dencg;
-  const double* den;
+  const R* dencg;
+  const R* den;
   Functional fn;
 };
 
-// Inverse real transform along x (unnormalised c2r convention).
-template <int EPI>
-__global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const double2* __restrict__ twx,
-                                                    const double2* __restrict__ in0,
-                                                    const double2* __restrict__ in1, double* out0,
-                                                    double* out1, Pot4Args pa, int lpb) {
-  extern __shared__ double2 sm[];
+// Inverse real transform along x (unnormalised c2r convention). EPI_POT4:
+// the spectrum holds delj4 + the correlation convolution; the epilogue adds
+// the local correlation term and the solid penalty (poten.f90:80-94,110-114).
+template <typename R, int EPI>
+__global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2<R>* __restrict__ twx,
+                                                    const C2<R>* __restrict__ in0,
+                                                    const C2<R>* __restrict__ in1, R* out0, R* out1,
+                                                    Pot4Args<R> pa, int lpb) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
   const int m = ax.n;
   const int ld = m + 2;
-  double2* a = sm;
-  double2* b = sm + lpb * ld;
-  const double2* in = blockIdx.y == 0 ? in0 : in1;
-  double* out = blockIdx.y == 0 ? out0 : out1;
+  C2<R>* a = sm;
+  C2<R>* b = sm + lpb * ld;
+  const C2<R>* in = blockIdx.y == 0 ? in0 : in1;
+  R* out = blockIdx.y == 0 ? out0 : out1;
   const long long nlines = (long long)g.ny * g.nz;
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
@@ -267,115 +314,128 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const do
   const int half = m / 2;
   for (int w = threadIdx.x; w < nl * (half + 1); w += blockDim.x) {
     const int l = w / (half + 1), k = w - l * (half + 1);
-    const double2 xk = b[l * ld + k];
-    const double2 xm = b[l * ld + m - k];
+    const C2<R> xk = b[l * ld + k];
+    const C2<R> xm = b[l * ld + m - k];
     if (k == 0) {
       // the imaginary parts of the x-DC and Nyquist bins carry no real data
-      a[l * ld] = make_double2(xk.x + xm.x, xk.x - xm.x);
+      a[l * ld] = mk<R>(xk.x + xm.x, xk.x - xm.x);
       continue;
     }
-    const double2 fe = cadd(xk, cconj(xm));
-    const double2 fo = mulw<1>(csub(xk, cconj(xm)), __ldg(&twx[k]));
-    a[l * ld + k] = cadd(fe, jmul<1>(fo));
-    if (k != m - k) a[l * ld + m - k] = cadd(cconj(fe), jmul<1>(cconj(fo)));
+    const C2<R> fe = cadd<R>(xk, cconj<R>(xm));
+    const C2<R> fo = mulw<R, 1>(csub<R>(xk, cconj<R>(xm)), __ldg(&twx[k]));
+    a[l * ld + k] = cadd<R>(fe, jmul<R, 1>(fo));
+    if (k != m - k) a[l * ld + m - k] = cadd<R>(cconj<R>(fe), jmul<R, 1>(cconj<R>(fo)));
   }
   __syncthreads();
-  double2* r = fft_smem<1>(a, b, nl, ld, ax);
+  C2<R>* r = fft_smem<R, 1>(a, b, nl, ld, ax);
   for (int w = threadIdx.x; w < nl * m; w += blockDim.x) {
     const int l = w / m, j = w - l * m;
     const long long e = (l0 + l) * g.nx + 2 * j;
-    double2 v = r[l * ld + j];
+    C2<R> v = r[l * ld + j];
     if (EPI == EPI_POT4) {
-      // pot4 = delj4 + dencg^2 (a0 + a1 dencg) + conv [+ penalty] (poten.f90:80-94,110-114)
       const Functional& fn = pa.fn;
-      double2 dl = __ldg(reinterpret_cast<const double2*>(pa.delj4 + e));
-      double2 cg = __ldg(reinterpret_cast<const double2*>(pa.dencg + e));
-      double p0 = fma(cg.x * cg.x, fma(fn.a1, cg.x, fn.a0), dl.x) + v.x;
-      double p1 = fma(cg.y * cg.y, fma(fn.a1, cg.y, fn.a0), dl.y) + v.y;
+      const C2<R> cg = ld_pair<R>(pa.dencg + e);
+      const R a0 = (R)fn.a0, a1 = (R)fn.a1;
+      R p0 = fma(cg.x * cg.x, fma(a1, cg.x, a0), v.x);
+      R p1 = fma(cg.y * cg.y, fma(a1, cg.y, a0), v.y);
       if (fn.lsolid) {
-        double2 d = __ldg(reinterpret_cast<const double2*>(pa.den + e));
-        double t0 = tanh(fn.beta_solid * (d.x - fn.den_m));
-        double t1 = tanh(fn.beta_solid * (d.y - fn.den_m));
-        p0 += fn.c_solid * (1.0 + t0 + fn.beta_solid * d.x * (1.0 - t0 * t0));
-        p1 += fn.c_solid * (1.0 + t1 + fn.beta_solid * d.y * (1.0 - t1 * t1));
+        const C2<R> d = ld_pair<R>(pa.den + e);
+        const R beta = (R)fn.beta_solid, dm = (R)fn.den_m, cs = (R)fn.c_solid;
+        const R t0 = tanh(beta * (d.x - dm));
+        const R t1 = tanh(beta * (d.y - dm));
+        p0 += cs * ((R)1 + t0 + beta * d.x * ((R)1 - t0 * t0));
+        p1 += cs * ((R)1 + t1 + beta * d.y * ((R)1 - t1 * t1));
       }
-      v = make_double2(p0, p1);
+      v = mk<R>(p0, p1);
     }
-    *reinterpret_cast<double2*>(out + e) = v;
+    *reinterpret_cast<C2<R>*>(out + e) = v;
   }
 }
 
 // ------------------------------------------------------------- y / z passes
-// In-place transform along y of the spectra in `specs` (blockIdx.z picks one).
+template <typename R>
 struct SpecList {
-  double2* p[4];
+  C2<R>* p[4];
 };
 
-template <int SIGN>
-__global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList specs) {
-  extern __shared__ double2 sm[];
+// In-place transform along y of the spectra in `specs` (blockIdx.z picks one).
+template <typename R, int SIGN>
+__global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> specs) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
+  constexpr int TX = Cx<R>::kTile;
   const int n = ax.n;  // ny
   const int ld = n + 1;
-  double2* a = sm;
-  double2* b = sm + kTileCols * ld;
-  double2* sp = specs.p[blockIdx.z];
-  const int kx0 = blockIdx.x * kTileCols;
-  const int ncol = min(kTileCols, g.nxh - kx0);
+  C2<R>* a = sm;
+  C2<R>* b = sm + TX * ld;
+  C2<R>* sp = specs.p[blockIdx.z];
+  const int kx0 = blockIdx.x * TX;
+  const int ncol = min(TX, g.nxh - kx0);
   const long long base = (long long)blockIdx.y * g.ny * g.nxh + kx0;
-  for (int w = threadIdx.x; w < kTileCols * n; w += blockDim.x) {
-    const int c = w % kTileCols, j = w / kTileCols;
+  for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
+    const int c = w % TX, j = w / TX;
     if (c < ncol) a[c * ld + j] = sp[base + (long long)j * g.nxh + c];
   }
   __syncthreads();
-  double2* r = fft_smem<SIGN>(a, b, ncol, ld, ax);
-  for (int w = threadIdx.x; w < kTileCols * n; w += blockDim.x) {
-    const int c = w % kTileCols, j = w / kTileCols;
+  C2<R>* r = fft_smem<R, SIGN>(a, b, ncol, ld, ax);
+  for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
+    const int c = w % TX, j = w / TX;
     if (c < ncol) sp[base + (long long)j * g.nxh + c] = r[c * ld + j];
   }
 }
 
+template <typename R>
 struct FactorList {
-  const double* f[3];
-  double2* out[3];
+  const R* f[3];
+  C2<R>* out[3];
 };
 
 // Forward z transform, product with each factor table (times scale), inverse
-// z transform; output 0 may alias the input.
-__global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const double2* in, FactorList fl,
-                                                     int nout, double scale) {
-  extern __shared__ double2 sm[];
+// z transform; output 0 may alias the input. `add` (nullable) is a spectrum
+// in the same (kx, ky, z) space that is added to output 0.
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C2<R>* in, FactorList<R> fl,
+                                                     int nout, R scale, const C2<R>* __restrict__ add) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
+  constexpr int TX = Cx<R>::kTile;
   const int n = ax.n;  // nz
   const int ld = n + 1;
-  double2* a = sm;
-  double2* b = sm + kTileCols * ld;
-  double2* c = sm + 2 * kTileCols * ld;
-  const int kx0 = blockIdx.x * kTileCols;
-  const int ncol = min(kTileCols, g.nxh - kx0);
+  C2<R>* a = sm;
+  C2<R>* b = sm + TX * ld;
+  C2<R>* c = sm + 2 * TX * ld;
+  const int kx0 = blockIdx.x * TX;
+  const int ncol = min(TX, g.nxh - kx0);
   const long long plane = (long long)g.ny * g.nxh;
   const long long base = (long long)blockIdx.y * g.nxh + kx0;
-  for (int w = threadIdx.x; w < kTileCols * n; w += blockDim.x) {
-    const int cc = w % kTileCols, k = w / kTileCols;
+  for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
+    const int cc = w % TX, k = w / TX;
     if (cc < ncol) a[cc * ld + k] = in[base + (long long)k * plane + cc];
   }
   __syncthreads();
-  double2* fwd = fft_smem<-1>(a, b, ncol, ld, ax);
-  double2* s1 = fwd == a ? b : a;
+  C2<R>* fwd = fft_smem<R, -1>(a, b, ncol, ld, ax);
+  C2<R>* s1 = fwd == a ? b : a;
   for (int o = 0; o < nout; ++o) {
-    const double* fac = fl.f[o];
-    for (int w = threadIdx.x; w < kTileCols * n; w += blockDim.x) {
-      const int cc = w % kTileCols, k = w / kTileCols;
+    const R* fac = fl.f[o];
+    for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
+      const int cc = w % TX, k = w / TX;
       if (cc < ncol) {
-        const double f = __ldg(&fac[base + (long long)k * plane + cc]) * scale;
-        const double2 v = fwd[cc * ld + k];
-        s1[cc * ld + k] = make_double2(v.x * f, v.y * f);
+        const R f = __ldg(&fac[base + (long long)k * plane + cc]) * scale;
+        const C2<R> v = fwd[cc * ld + k];
+        s1[cc * ld + k] = mk<R>(v.x * f, v.y * f);
       }
     }
     __syncthreads();
-    double2* r = fft_smem<1>(s1, c, ncol, ld, ax);
-    double2* dst = fl.out[o];
-    for (int w = threadIdx.x; w < kTileCols * n; w += blockDim.x) {
-      const int cc = w % kTileCols, k = w / kTileCols;
-      if (cc < ncol) dst[base + (long long)k * plane + cc] = r[cc * ld + k];
+    C2<R>* r = fft_smem<R, 1>(s1, c, ncol, ld, ax);
+    C2<R>* dst = fl.out[o];
+    for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
+      const int cc = w % TX, k = w / TX;
+      if (cc < ncol) {
+        const long long e = base + (long long)k * plane + cc;
+        C2<R> v = r[cc * ld + k];
+        if (o == 0 && add) v = cadd<R>(v, add[e]);
+        dst[e] = v;
+      }
     }
     __syncthreads();  // fwd stays intact; s1 and c are free again
   }
@@ -393,83 +453,146 @@ void set_smem(K kernel, size_t bytes) {
   if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <int PRO>
-void launch_r2c(const Grid& g, const FftPlan& p, const double* a, const double* b, double c0, double c1,
-                double2* out, cudaStream_t s) {
+template <typename R>
+const C2<R>* twx_of(const FftPlan& p);
+template <>
+const double2* twx_of<double>(const FftPlan& p) {
+  return p.twx;
+}
+template <>
+const float2* twx_of<float>(const FftPlan& p) {
+  return p.twxf;
+}
+
+template <typename R, int PRO>
+void launch_r2c(const Grid& g, const FftPlan& p, const R* a, const R* b, R c0, R c1, C2<R>* out, cudaStream_t s) {
   const int m = p.xh.n;
   const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(double2) * 2 * lpb * (m + 1);
-  set_smem(k_x_r2c<PRO>, smem);
+  const size_t smem = sizeof(C2<R>) * 2 * lpb * (m + 1);
+  set_smem(k_x_r2c<R, PRO>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb));
-  k_x_r2c<PRO><<<grid, kThreads, smem, s>>>(g, p.xh, p.twx, a, b, c0, c1, out, lpb);
+  k_x_r2c<R, PRO><<<grid, kThreads, smem, s>>>(g, p.xh, twx_of<R>(p), a, b, c0, c1, out, lpb);
+}
+
+template <typename R>
+void y_impl(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int sign, cudaStream_t s) {
+  constexpr int TX = Cx<R>::kTile;
+  SpecList<R> sl{};
+  for (int i = 0; i < nspec; ++i) sl.p[i] = static_cast<C2<R>*>(specs[i]);
+  const size_t smem = sizeof(C2<R>) * 2 * TX * (p.y.n + 1);
+  dim3 grid((g.nxh + TX - 1) / TX, g.nz, nspec);
+  if (sign < 0) {
+    set_smem(k_y<R, -1>, smem);
+    k_y<R, -1><<<grid, kThreads, smem, s>>>(g, p.y, sl);
+  } else {
+    set_smem(k_y<R, 1>, smem);
+    k_y<R, 1><<<grid, kThreads, smem, s>>>(g, p.y, sl);
+  }
+}
+
+template <typename R>
+void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors,
+                int nout, double scale, const void* add, cudaStream_t s) {
+  constexpr int TX = Cx<R>::kTile;
+  FactorList<R> fl{};
+  for (int i = 0; i < nout; ++i) {
+    fl.f[i] = static_cast<const R*>(factors[i]);
+    fl.out[i] = static_cast<C2<R>*>(outs[i]);
+  }
+  const size_t smem = sizeof(C2<R>) * 3 * TX * (p.z.n + 1);
+  set_smem(k_z_conv<R>, smem);
+  dim3 grid((g.nxh + TX - 1) / TX, g.ny);
+  k_z_conv<R><<<grid, kThreads, smem, s>>>(g, p.z, static_cast<const C2<R>*>(in), fl, nout, (R)scale,
+                                           static_cast<const C2<R>*>(add));
+}
+
+template <typename R>
+void c2r_impl(const Grid& g, const FftPlan& p, const void* const* ins, void* const* outs, int nspec, cudaStream_t s) {
+  const int m = p.xh.n;
+  const int lpb = x_lines_per_block(m);
+  const size_t smem = sizeof(C2<R>) * 2 * lpb * (m + 2);
+  set_smem(k_x_c2r<R, EPI_STORE>, smem);
+  const long long nlines = (long long)g.ny * g.nz;
+  dim3 grid((unsigned)((nlines + lpb - 1) / lpb), nspec);
+  Pot4Args<R> pa{};
+  const C2<R>* i0 = static_cast<const C2<R>*>(ins[0]);
+  const C2<R>* i1 = nspec > 1 ? static_cast<const C2<R>*>(ins[1]) : i0;
+  R* o0 = static_cast<R*>(outs[0]);
+  R* o1 = nspec > 1 ? static_cast<R*>(outs[1]) : o0;
+  k_x_c2r<R, EPI_STORE><<<grid, kThreads, smem, s>>>(g, p.xh, twx_of<R>(p), i0, i1, o0, o1, pa, lpb);
+}
+
+template <typename R>
+void pot4_impl(const Grid& g, const FftPlan& p, const void* conv, const void* dencg, const void* den,
+               const Functional& fn, void* pot4, cudaStream_t s) {
+  const int m = p.xh.n;
+  const int lpb = x_lines_per_block(m);
+  const size_t smem = sizeof(C2<R>) * 2 * lpb * (m + 2);
+  set_smem(k_x_c2r<R, EPI_POT4>, smem);
+  const long long nlines = (long long)g.ny * g.nz;
+  dim3 grid((unsigned)((nlines + lpb - 1) / lpb), 1);
+  Pot4Args<R> pa{static_cast<const R*>(dencg), static_cast<const R*>(den), fn};
+  const C2<R>* c = static_cast<const C2<R>*>(conv);
+  k_x_c2r<R, EPI_POT4><<<grid, kThreads, smem, s>>>(g, p.xh, twx_of<R>(p), c, c, static_cast<R*>(pot4),
+                                                    static_cast<R*>(pot4), pa, lpb);
 }
 
 }  // namespace
 
-void fft_x_r2c(const Grid& g, const FftPlan& p, const double* in, double2* out, cudaStream_t s) {
-  launch_r2c<PRO_PLAIN>(g, p, in, nullptr, 0.0, 0.0, out, s);
+// -------------------------------------------------------------- launchers
+void fft_x_r2c(const Grid& g, const FftPlan& p, int prec, const void* in, void* out, cudaStream_t s) {
+  if (prec == HE4G_PREC_FP64)
+    launch_r2c<double, PRO_PLAIN>(g, p, static_cast<const double*>(in), nullptr, 0.0, 0.0,
+                                  static_cast<double2*>(out), s);
+  else
+    launch_r2c<float, PRO_PLAIN>(g, p, static_cast<const float*>(in), nullptr, 0.f, 0.f,
+                                 static_cast<float2*>(out), s);
 }
-void fft_x_r2c_corr(const Grid& g, const FftPlan& p, const double* den, const double* dencg, double cp4,
-                    double cpp4, double2* out, cudaStream_t s) {
-  launch_r2c<PRO_CORR>(g, p, den, dencg, cp4, cpp4, out, s);
+void fft_x_r2c_corr(const Grid& g, const FftPlan& p, int prec, const void* den, const void* dencg, double cp4,
+                    double cpp4, void* out, cudaStream_t s) {
+  if (prec == HE4G_PREC_FP64)
+    launch_r2c<double, PRO_CORR>(g, p, static_cast<const double*>(den), static_cast<const double*>(dencg), cp4,
+                                 cpp4, static_cast<double2*>(out), s);
+  else
+    launch_r2c<float, PRO_CORR>(g, p, static_cast<const float*>(den), static_cast<const float*>(dencg),
+                                (float)cp4, (float)cpp4, static_cast<float2*>(out), s);
 }
-void fft_x_r2c_prod(const Grid& g, const FftPlan& p, const double* a, const double* b, double2* out,
+void fft_x_r2c_prod(const Grid& g, const FftPlan& p, int prec, const void* a, const void* b, void* out,
                     cudaStream_t s) {
-  launch_r2c<PRO_PROD>(g, p, a, b, 0.0, 0.0, out, s);
+  if (prec == HE4G_PREC_FP64)
+    launch_r2c<double, PRO_PROD>(g, p, static_cast<const double*>(a), static_cast<const double*>(b), 0.0, 0.0,
+                                 static_cast<double2*>(out), s);
+  else
+    launch_r2c<float, PRO_PROD>(g, p, static_cast<const float*>(a), static_cast<const float*>(b), 0.f, 0.f,
+                                static_cast<float2*>(out), s);
 }
-
-void fft_y(const Grid& g, const FftPlan& p, double2* const* specs, int nspec, int sign, cudaStream_t s) {
-  SpecList sl{};
-  for (int i = 0; i < nspec; ++i) sl.p[i] = specs[i];
-  const size_t smem = sizeof(double2) * 2 * kTileCols * (p.y.n + 1);
-  dim3 grid((g.nxh + kTileCols - 1) / kTileCols, g.nz, nspec);
-  if (sign < 0) {
-    set_smem(k_y<-1>, smem);
-    k_y<-1><<<grid, kThreads, smem, s>>>(g, p.y, sl);
-  } else {
-    set_smem(k_y<1>, smem);
-    k_y<1><<<grid, kThreads, smem, s>>>(g, p.y, sl);
-  }
+void fft_y(const Grid& g, const FftPlan& p, int prec, void* const* specs, int nspec, int sign, cudaStream_t s) {
+  if (prec == HE4G_PREC_FP64)
+    y_impl<double>(g, p, specs, nspec, sign, s);
+  else
+    y_impl<float>(g, p, specs, nspec, sign, s);
 }
-
-void fft_z_conv(const Grid& g, const FftPlan& p, const double2* in, double2* const* outs,
-                const double* const* factors, int nout, double scale, cudaStream_t s) {
-  FactorList fl{};
-  for (int i = 0; i < nout; ++i) {
-    fl.f[i] = factors[i];
-    fl.out[i] = outs[i];
-  }
-  const size_t smem = sizeof(double2) * 3 * kTileCols * (p.z.n + 1);
-  set_smem(k_z_conv, smem);
-  dim3 grid((g.nxh + kTileCols - 1) / kTileCols, g.ny);
-  k_z_conv<<<grid, kThreads, smem, s>>>(g, p.z, in, fl, nout, scale);
+void fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* const* outs,
+                const void* const* factors, int nout, double scale, const void* add, cudaStream_t s) {
+  if (prec == HE4G_PREC_FP64)
+    zconv_impl<double>(g, p, in, outs, factors, nout, scale, add, s);
+  else
+    zconv_impl<float>(g, p, in, outs, factors, nout, scale, add, s);
 }
-
-void fft_x_c2r(const Grid& g, const FftPlan& p, const double2* const* ins, double* const* outs, int nspec,
+void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins, void* const* outs, int nspec,
                cudaStream_t s) {
-  const int m = p.xh.n;
-  const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(double2) * 2 * lpb * (m + 2);
-  set_smem(k_x_c2r<EPI_STORE>, smem);
-  const long long nlines = (long long)g.ny * g.nz;
-  dim3 grid((unsigned)((nlines + lpb - 1) / lpb), nspec);
-  Pot4Args pa{};
-  k_x_c2r<EPI_STORE><<<grid, kThreads, smem, s>>>(g, p.xh, p.twx, ins[0], nspec > 1 ? ins[1] : ins[0],
-                                                  outs[0], nspec > 1 ? outs[1] : outs[0], pa, lpb);
+  if (prec == HE4G_PREC_FP64)
+    c2r_impl<double>(g, p, ins, outs, nspec, s);
+  else
+    c2r_impl<float>(g, p, ins, outs, nspec, s);
 }
-
-void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, const double2* conv, const double* delj4,
-                    const double* dencg, const double* den, const Functional& fn, double* pot4,
-                    cudaStream_t s) {
-  const int m = p.xh.n;
-  const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(double2) * 2 * lpb * (m + 2);
-  set_smem(k_x_c2r<EPI_POT4>, smem);
-  const long long nlines = (long long)g.ny * g.nz;
-  dim3 grid((unsigned)((nlines + lpb - 1) / lpb), 1);
-  Pot4Args pa{delj4, dencg, den, fn};
-  k_x_c2r<EPI_POT4><<<grid, kThreads, smem, s>>>(g, p.xh, p.twx, conv, conv, pot4, pot4, pa, lpb);
+void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv, const void* dencg,
+                    const void* den, const Functional& fn, void* pot4, cudaStream_t s) {
+  if (prec == HE4G_PREC_FP64)
+    pot4_impl<double>(g, p, conv, dencg, den, fn, pot4, s);
+  else
+    pot4_impl<float>(g, p, conv, dencg, den, fn, pot4, s);
 }
 
 }  // namespace he4g

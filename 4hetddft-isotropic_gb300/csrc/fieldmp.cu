@@ -1,0 +1,453 @@
+// fieldmp.cu — kernels of the mixed-precision form of the time step.
+//
+// The stencils, H.psi and the pointwise functional run in FP32 on FP32
+// fields; FP64 is kept where error accumulates over steps: the psi
+// accumulator of the predictor-corrector / Runge–Kutta–Gill updates (psi,
+// its history, pc and q are FP64), the norm and energy sums, the impurity
+// force sum and the impurity trajectory. Every update kernel also writes an
+// FP32 copy of the new psi, which the next stencil reads: converting the 37
+// neighbours of each point from FP64 would cost as much as FP64 arithmetic
+// on this GPU, whose FP64 rate is 1/61 of its FP32 rate.
+//
+// Formulas and their reference lines are those of field.cu.
+#include "he4g_internal.cuh"
+
+namespace he4g {
+
+namespace {
+
+constexpr int kBX = 64, kBY = 4;  // 256-thread point blocks
+constexpr int kZ = 8;             // z-planes per thread in the force sums
+
+struct Pt {
+  int i, j, k;
+  long long p;
+  bool ok;
+};
+__device__ __forceinline__ Pt point(const Grid& g) {
+  Pt t;
+  t.i = blockIdx.x * kBX + threadIdx.x;
+  t.j = blockIdx.y * kBY + threadIdx.y;
+  t.k = blockIdx.z;
+  t.ok = t.i < g.nx && t.j < g.ny;
+  t.p = ((long long)t.k * g.ny + t.j) * g.nx + t.i;
+  return t;
+}
+dim3 point_grid(const Grid& g) { return dim3((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, g.nz); }
+__device__ __forceinline__ int block_linear() {
+  return (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+}
+
+__device__ __forceinline__ float2 ld2f(const float2* p) { return __ldg(p); }
+
+// (d2x + d2y + d2z) psi in FP32, zero padded
+__device__ __forceinline__ float2 lap13f(const float2* __restrict__ f, const Pt& t, const Grid& g,
+                                         const StencilF& st) {
+  const float2 c = ld2f(f + t.p);
+  float ar = st.d2c * c.x, ai = st.d2c * c.y;
+  const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+  const float2 zero = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int o = 1; o <= kStencilHalf; ++o) {
+    float2 a = t.i - o >= 0 ? ld2f(f + t.p - o) : zero;
+    float2 b = t.i + o < g.nx ? ld2f(f + t.p + o) : zero;
+    ar = fmaf(st.d2[0][o], a.x + b.x, ar);
+    ai = fmaf(st.d2[0][o], a.y + b.y, ai);
+    a = t.j - o >= 0 ? ld2f(f + t.p - o * sy) : zero;
+    b = t.j + o < g.ny ? ld2f(f + t.p + o * sy) : zero;
+    ar = fmaf(st.d2[1][o], a.x + b.x, ar);
+    ai = fmaf(st.d2[1][o], a.y + b.y, ai);
+    a = t.k - o >= 0 ? ld2f(f + t.p - o * sz) : zero;
+    b = t.k + o < g.nz ? ld2f(f + t.p + o * sz) : zero;
+    ar = fmaf(st.d2[2][o], a.x + b.x, ar);
+    ai = fmaf(st.d2[2][o], a.y + b.y, ai);
+  }
+  return make_float2(ar, ai);
+}
+
+// timec*(lap*h2o2m4 - pot4*psi) - i*uimp*psi in FP32
+__device__ __forceinline__ float2 hpsif(float2 lap, float2 ps, float pot, float u, float T, float h2) {
+  const float ar = fmaf(lap.x, h2, -pot * ps.x);
+  const float ai = fmaf(lap.y, h2, -pot * ps.y);
+  const float br = fmaf(T, ar, -ai);
+  const float bi = fmaf(T, ai, ar);
+  return make_float2(fmaf(u, ps.y, br), fmaf(-u, ps.x, bi));
+}
+
+__device__ __forceinline__ int den_health(float d) {
+  const int b = __float_as_int(d);
+  if (b > 0 && b < 0x7F800000) return 0;
+  if ((b & 0x7F800000) == 0x7F800000) return 3;
+  return 1;
+}
+
+// FP32 warp sums converted once per warp, FP64 across warps and blocks
+template <int NV>
+__device__ __forceinline__ void block_sum_f(float (&v)[NV], double* partials) {
+  __shared__ double sh[NV][8];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int a = 0; a < NV; ++a) {
+    float x = v[a];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[a][wid] = (double)x;
+  }
+  __syncthreads();
+  if (tid < NV) {
+    double s = 0.0;
+    for (int w = 0; w < 8; ++w) s += sh[tid][w];
+    partials[(long long)block_linear() * NV + tid] = s;
+  }
+}
+
+template <int NV>
+__device__ __forceinline__ void block_sum_d(double (&v)[NV], double* partials) {
+  __shared__ double sh[NV][8];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int a = 0; a < NV; ++a) {
+    double x = v[a];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[a][wid] = x;
+  }
+  __syncthreads();
+  if (tid < NV) {
+    double s = 0.0;
+    for (int w = 0; w < 8; ++w) s += sh[tid][w];
+    partials[(long long)block_linear() * NV + tid] = s;
+  }
+}
+
+// Predictor + modifier (steppc.f90:45-65): H.psi from the FP32 copy of
+// psi_n, FP64 accumulation into the psi_{n-3} slot.
+__global__ void __launch_bounds__(256) k_pc_predict_mp(Grid g, StencilF st, Functional fn,
+                                                        const float2* __restrict__ psi32, double2* p3,
+                                                        float2* __restrict__ psi32_out,
+                                                        const float2* __restrict__ h1, float2* h2, double2* pc,
+                                                        const float* __restrict__ pot4,
+                                                        const float* __restrict__ uimp,
+                                                        const float* __restrict__ timec, float* den,
+                                                        double c4o3dt, double c112) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const float2 lap = lap13f(psi32, t, g, st);
+  const float2 ps = ld2f(psi32 + t.p);
+  const float2 f = hpsif(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), (float)fn.h2o2m4);
+  const float2 a1 = h1[t.p], a2 = h2[t.p];
+  const float tr = fmaf(2.f, a2.x, fmaf(2.f, f.x, -a1.x));
+  const float ti = fmaf(2.f, a2.y, fmaf(2.f, f.y, -a1.y));
+  const double2 o3 = p3[t.p], q = pc[t.p];
+  const double2 s1 = make_double2(fma(c4o3dt, (double)tr, o3.x), fma(c4o3dt, (double)ti, o3.y));
+  const double2 pn = make_double2(fma(-c112, q.x, s1.x), fma(-c112, q.y, s1.y));
+  p3[t.p] = pn;
+  pc[t.p] = s1;
+  h2[t.p] = f;
+  const float2 p32 = make_float2((float)pn.x, (float)pn.y);
+  psi32_out[t.p] = p32;
+  den[t.p] = fmaf(p32.x, p32.x, p32.y * p32.y);
+}
+
+// Corrector (steppc.f90:119-134)
+__global__ void __launch_bounds__(256) k_pc_correct_mp(Grid g, StencilF st, Functional fn,
+                                                        const float2* __restrict__ psit32,
+                                                        const double2* __restrict__ p3,
+                                                        const double2* __restrict__ p2,
+                                                        const float2* __restrict__ h1,
+                                                        const float2* __restrict__ h2, double2* pc,
+                                                        const float* __restrict__ pot4,
+                                                        const float* __restrict__ uimp,
+                                                        const float* __restrict__ timec, double2* psi_out,
+                                                        float2* __restrict__ psi32_out, float* den,
+                                                        double* partials, double f3, double c9, int* health) {
+  const Pt t = point(g);
+  float v[1] = {0.f};
+  if (t.ok) {
+    const float2 lap = lap13f(psit32, t, g, st);
+    const float2 ps = ld2f(psit32 + t.p);
+    const float2 f = hpsif(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), (float)fn.h2o2m4);
+    const float2 a1 = ld2f(h1 + t.p), a2 = ld2f(h2 + t.p);
+    const float tr = fmaf(2.f, a1.x, f.x) - a2.x;
+    const float ti = fmaf(2.f, a1.y, f.y) - a2.y;
+    const double2 o3 = __ldg(p3 + t.p), o2 = __ldg(p2 + t.p);
+    const double2 s5 = make_double2(0.125 * fma(f3, (double)tr, fma(9.0, o3.x, -o2.x)),
+                                    0.125 * fma(f3, (double)ti, fma(9.0, o3.y, -o2.y)));
+    double2 q = pc[t.p];
+    q = make_double2(q.x - s5.x, q.y - s5.y);
+    pc[t.p] = q;
+    const double2 pn = make_double2(fma(c9, q.x, s5.x), fma(c9, q.y, s5.y));
+    psi_out[t.p] = pn;
+    const float2 p32 = make_float2((float)pn.x, (float)pn.y);
+    psi32_out[t.p] = p32;
+    const float d = fmaf(p32.x, p32.x, p32.y * p32.y);
+    den[t.p] = d;
+    const float qx = (float)q.x, qy = (float)q.y;
+    v[0] = sqrtf(fmaf(qx, qx, qy * qy));
+    const int h = den_health(d) & 2;
+    if (h) atomicOr(health, h);
+  }
+  block_sum_f<1>(v, partials);
+}
+
+// Runge–Kutta–Gill stage (steprk.f90:57-92) with FP64 psi and q
+__global__ void __launch_bounds__(256) k_rk_stage_mp(Grid g, StencilF st, Functional fn,
+                                                      const float2* __restrict__ psi32,
+                                                      const double2* __restrict__ psi, double2* psi_out,
+                                                      float2* __restrict__ psi32_out, double2* q, float2* f_out,
+                                                      const float* __restrict__ pot4,
+                                                      const float* __restrict__ uimp,
+                                                      const float* __restrict__ timec, float* den, double ar,
+                                                      double br, double cr, double dt, int* health) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const float2 lap = lap13f(psi32, t, g, st);
+  const float2 ps = ld2f(psi32 + t.p);
+  const float2 f = hpsif(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), (float)fn.h2o2m4);
+  const double fx = (double)f.x, fy = (double)f.y;
+  double2 qq = q[t.p];
+  const double2 s1 = make_double2(ar * fma(-br, qq.x, fx), ar * fma(-br, qq.y, fy));
+  qq = make_double2(fma(-cr, fx, fma(3.0, s1.x, qq.x)), fma(-cr, fy, fma(3.0, s1.y, qq.y)));
+  q[t.p] = qq;
+  if (f_out) f_out[t.p] = f;
+  const double2 p0 = __ldg(psi + t.p);
+  const double2 pn = make_double2(fma(dt, s1.x, p0.x), fma(dt, s1.y, p0.y));
+  psi_out[t.p] = pn;
+  const float2 p32 = make_float2((float)pn.x, (float)pn.y);
+  psi32_out[t.p] = p32;
+  const float d = fmaf(p32.x, p32.x, p32.y * p32.y);
+  den[t.p] = d;
+  const int h = den_health(d);
+  if (h) atomicOr(health, h);
+}
+
+// FP32 copy of psi and den = |psi|^2 after a state upload
+__global__ void k_split_mp(Grid g, const double2* __restrict__ psi, float2* psi32, float* den) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const double2 p = psi[t.p];
+  const float2 p32 = make_float2((float)p.x, (float)p.y);
+  psi32[t.p] = p32;
+  den[t.p] = fmaf(p32.x, p32.x, p32.y * p32.y);
+}
+
+// updatepoten (potenimp.f90:71-95) in FP32
+__global__ void __launch_bounds__(256) k_potenimp_mp(Grid g, const float* __restrict__ xs,
+                                                      const float* __restrict__ ys, const float* __restrict__ zs,
+                                                      const float* __restrict__ potion, int npot, float delinter,
+                                                      ImpState* imp, int center_sel, float* uimp) {
+  const Pt t = point(g);
+  const double* c = center_sel == 0 ? imp->rimp : imp->center;
+  const double c0 = c[0], c1 = c[1], c2 = c[2];
+  if (center_sel == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 &&
+      threadIdx.y == 0) {
+    imp->center[0] = c0;
+    imp->center[1] = c1;
+    imp->center[2] = c2;
+  }
+  if (!t.ok) return;
+  const float dz = __ldg(zs + t.k) - (float)c2;
+  const float dy = __ldg(ys + t.j) - (float)c1;
+  const float dx = __ldg(xs + t.i) - (float)c0;
+  const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+  const int ir = (int)(r / delinter);
+  const float w = fmodf(r, delinter) / delinter;
+  float u = 0.f;
+  if (ir >= 0 && ir + 1 < npot) {
+    u = fmaf(__ldg(potion + ir), 1.f - w, __ldg(potion + ir + 1) * w);
+  } else {
+    atomicOr(&imp->health, 4);
+  }
+  uimp[t.p] = u;
+}
+
+// grad(den) . uimp summed per block: each thread walks kZ z-planes and
+// accumulates its FP32 products in FP64
+__global__ void __launch_bounds__(256) k_force_mp(Grid g, StencilF st, const float* __restrict__ den,
+                                                   const float* __restrict__ uimp, double* partials) {
+  const int i = blockIdx.x * kBX + threadIdx.x;
+  const int j = blockIdx.y * kBY + threadIdx.y;
+  const int k0 = blockIdx.z * kZ;
+  double v[3] = {0.0, 0.0, 0.0};
+  if (i < g.nx && j < g.ny) {
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    for (int k = k0; k < min(k0 + kZ, g.nz); ++k) {
+      const long long p = ((long long)k * g.ny + j) * g.nx + i;
+      float gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+      for (int o = 1; o <= kStencilHalf; ++o) {
+        float a = i - o >= 0 ? __ldg(den + p - o) : 0.f;
+        float b = i + o < g.nx ? __ldg(den + p + o) : 0.f;
+        gx = fmaf(st.d1[0][o], b - a, gx);
+        a = j - o >= 0 ? __ldg(den + p - o * sy) : 0.f;
+        b = j + o < g.ny ? __ldg(den + p + o * sy) : 0.f;
+        gy = fmaf(st.d1[1][o], b - a, gy);
+        a = k - o >= 0 ? __ldg(den + p - o * sz) : 0.f;
+        b = k + o < g.nz ? __ldg(den + p + o * sz) : 0.f;
+        gz = fmaf(st.d1[2][o], b - a, gz);
+      }
+      const float u = __ldg(uimp + p);
+      v[0] += (double)(gx * u);
+      v[1] += (double)(gy * u);
+      v[2] += (double)(gz * u);
+    }
+  }
+  block_sum_d<3>(v, partials);
+}
+
+__global__ void __launch_bounds__(256) k_grad1_f(Grid g, StencilF st, int axis, const float* __restrict__ in,
+                                                  float* out) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const long long s = axis == 0 ? 1 : axis == 1 ? (long long)g.nx : (long long)g.nx * g.ny;
+  const int c = axis == 0 ? t.i : axis == 1 ? t.j : t.k;
+  const int nl = axis == 0 ? g.nx : axis == 1 ? g.ny : g.nz;
+  float acc = 0.f;
+#pragma unroll
+  for (int o = 1; o <= kStencilHalf; ++o) {
+    const float a = c - o >= 0 ? __ldg(in + t.p - o * s) : 0.f;
+    const float b = c + o < nl ? __ldg(in + t.p + o * s) : 0.f;
+    acc = fmaf(st.d1[axis][o], b - a, acc);
+  }
+  out[t.p] = acc;
+}
+
+__global__ void k_falfs_f(Grid g, const float* denalf, float den0s, float* falfs) {
+  const Pt t = point(g);
+  if (t.ok) falfs[t.p] = 1.f - denalf[t.p] / den0s;
+}
+__global__ void k_dot3_f(Grid g, const float* ax, const float* ay, const float* az, const float* bx,
+                         const float* by, const float* bz, float* out) {
+  const Pt t = point(g);
+  if (t.ok) out[t.p] = (ax[t.p] * bx[t.p]) + (ay[t.p] * by[t.p]) + (az[t.p] * bz[t.p]);
+}
+__global__ void k_ualphas_a_f(Grid g, const float* falfs, const float* ix, const float* iy, const float* iz,
+                              float* u, float* s1, float* s2, float* s3, float den0s) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  u[t.p] = u[t.p] / den0s;
+  s1[t.p] = falfs[t.p] * ix[t.p];
+  s2[t.p] = falfs[t.p] * iy[t.p];
+  s3[t.p] = falfs[t.p] * iz[t.p];
+}
+__global__ void k_ualphas_b_f(Grid g, float* u, const float* s4, const float* s5, const float* s6, float h2o2m4,
+                              float alphas, float* pot4) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const float v = (u[t.p] + s4[t.p] + s5[t.p] + s6[t.p]) * h2o2m4 * alphas;
+  u[t.p] = v;
+  pot4[t.p] = pot4[t.p] + v;
+}
+
+// energy / observable sums from FP32 fields and FP64 psi, summed in FP64
+// (same value slots as the FP64 kernels of field.cu)
+constexpr int kEP = 12;
+__global__ void __launch_bounds__(256) k_energy_point_mp(Grid g, Functional fn, double aux1, double aux2,
+                                                          const float* __restrict__ den,
+                                                          const float* __restrict__ dencg,
+                                                          const float* __restrict__ delj4,
+                                                          const float* __restrict__ uimp,
+                                                          const float* __restrict__ falfs,
+                                                          const float* __restrict__ dx, const float* __restrict__ dy,
+                                                          const float* __restrict__ dz, const float* __restrict__ ix,
+                                                          const float* __restrict__ iy, const float* __restrict__ iz,
+                                                          const double* __restrict__ xs,
+                                                          const double* __restrict__ ys,
+                                                          const double* __restrict__ zs, double* partials) {
+  const Pt t = point(g);
+  double v[kEP];
+#pragma unroll
+  for (int a = 0; a < kEP; ++a) v[a] = 0.0;
+  if (t.ok) {
+    const double d = den[t.p], cg = dencg[t.p];
+    const double x = xs[t.i], y = ys[t.j], z = zs[t.k];
+    v[0] = d;
+    v[1] = d * x;
+    v[2] = d * y;
+    v[3] = d * z;
+    v[4] = d * x * x;
+    v[5] = d * y * y;
+    v[6] = d * z * z;
+    v[7] = (double)delj4[t.p] * d;
+    v[8] = d * cg * cg * (aux1 + aux2 * cg);
+    if (fn.lsolid) v[9] = d * (1.0 + tanh(fn.beta_solid * (d - fn.den_m)));
+    v[10] = (double)uimp[t.p] * d;
+    if (falfs)
+      v[11] = (double)falfs[t.p] * ((double)dx[t.p] * ix[t.p] + (double)dy[t.p] * iy[t.p] + (double)dz[t.p] * iz[t.p]);
+  }
+  block_sum_d<kEP>(v, partials);
+}
+
+}  // namespace
+
+int force_blocks_mp(const Grid& g) {
+  return ((g.nx + kBX - 1) / kBX) * ((g.ny + kBY - 1) / kBY) * ((g.nz + kZ - 1) / kZ);
+}
+
+void launch_pc_predict_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
+                          double2* p3, float2* psi32_out, const float2* h1, float2* h2, double2* pc,
+                          const float* pot4, const float* uimp, const float* timec, float* den, double c4o3dt,
+                          double c112, cudaStream_t s) {
+  k_pc_predict_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, fn, psi32, p3, psi32_out, h1, h2, pc, pot4, uimp,
+                                                           timec, den, c4o3dt, c112);
+}
+void launch_pc_correct_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psit32,
+                          const double2* p3, const double2* p2, const float2* h1, const float2* h2, double2* pc,
+                          const float* pot4, const float* uimp, const float* timec, double2* psi_out,
+                          float2* psi32_out, float* den, double* partials, double f3, double c9, int* health,
+                          cudaStream_t s) {
+  k_pc_correct_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, fn, psit32, p3, p2, h1, h2, pc, pot4, uimp,
+                                                           timec, psi_out, psi32_out, den, partials, f3, c9,
+                                                           health);
+}
+void launch_rk_stage_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
+                        const double2* psi, double2* psi_out, float2* psi32_out, double2* q, float2* f_out,
+                        const float* pot4, const float* uimp, const float* timec, float* den, double ar, double br,
+                        double cr, double dt, int* health, cudaStream_t s) {
+  k_rk_stage_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, fn, psi32, psi, psi_out, psi32_out, q, f_out, pot4,
+                                                         uimp, timec, den, ar, br, cr, dt, health);
+}
+void launch_split_mp(const Grid& g, const double2* psi, float2* psi32, float* den, cudaStream_t s) {
+  k_split_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, psi, psi32, den);
+}
+void launch_potenimp_mp(const Grid& g, const float* x, const float* y, const float* z, const float* potion,
+                        int npot, float delinter, ImpState* imp, int center_sel, float* uimp, cudaStream_t s) {
+  k_potenimp_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, x, y, z, potion, npot, delinter, imp, center_sel,
+                                                         uimp);
+}
+void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const float* uimp, double* partials,
+                     cudaStream_t s) {
+  dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZ - 1) / kZ);
+  k_force_mp<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, uimp, partials);
+}
+void launch_grad1_f(const Grid& g, const StencilF& st, int axis, const float* in, float* out, cudaStream_t s) {
+  k_grad1_f<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, axis, in, out);
+}
+void launch_falfs_f(const Grid& g, const float* denalf, float den0s, float* falfs, cudaStream_t s) {
+  k_falfs_f<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, denalf, den0s, falfs);
+}
+void launch_dot3_f(const Grid& g, const float* ax, const float* ay, const float* az, const float* bx,
+                   const float* by, const float* bz, float* out, cudaStream_t s) {
+  k_dot3_f<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, ax, ay, az, bx, by, bz, out);
+}
+void launch_ualphas_a_f(const Grid& g, const float* falfs, const float* ix, const float* iy, const float* iz,
+                        float* u, float* s1, float* s2, float* s3, float den0s, cudaStream_t s) {
+  k_ualphas_a_f<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, falfs, ix, iy, iz, u, s1, s2, s3, den0s);
+}
+void launch_ualphas_b_f(const Grid& g, float* u, const float* s4, const float* s5, const float* s6, float h2o2m4,
+                        float alphas, float* pot4, cudaStream_t s) {
+  k_ualphas_b_f<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, u, s4, s5, s6, h2o2m4, alphas, pot4);
+}
+void launch_energy_point_mp(const Grid& g, const Functional& fn, const float* den, const float* dencg,
+                            const float* delj4, const float* uimp, const float* falfs, const float* dx,
+                            const float* dy, const float* dz, const float* ix, const float* iy, const float* iz,
+                            const double* xs, const double* ys, const double* zs, double* partials,
+                            cudaStream_t s) {
+  const double aux1 = 0.5 * fn.cp4, aux2 = (1.0 / 3.0) * fn.cpp4;  // energy.f90:55-56
+  k_energy_point_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, fn, aux1, aux2, den, dencg, delj4, uimp, falfs,
+                                                             dx, dy, dz, ix, iy, iz, xs, ys, zs, partials);
+}
+
+}  // namespace he4g

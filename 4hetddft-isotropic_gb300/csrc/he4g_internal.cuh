@@ -19,12 +19,13 @@ constexpr int kStencilHalf = 6;   // 13-point stencils
 constexpr int kRedBlock = 256;    // threads of the reduction blocks
 
 // One 1D transform length with its mixed-radix factorisation and its
-// forward twiddles tw[t] = exp(-2 pi i t / n), t < n (device memory).
+// forward twiddles tw[t] = exp(-2 pi i t / n), t < n, in FP64 and FP32.
 struct FftAxis {
   int n;
   int nf;
   int fac[kMaxFactors];
   const double2* tw;
+  const float2* twf;
 };
 
 // Geometry of one run.
@@ -42,6 +43,11 @@ struct Stencil {
   double d1[3][kStencilHalf + 1];
   double d2[3][kStencilHalf + 1];
   double d2c;  // sum over axes of the centre coefficient of d2
+};
+struct StencilF {
+  float d1[3][kStencilHalf + 1];
+  float d2[3][kStencilHalf + 1];
+  float d2c;
 };
 
 // Constants of the H.psi / functional evaluation.
@@ -71,34 +77,36 @@ struct ImpState {
 constexpr int kRingRows = 8192;
 constexpr int kRingCols = 10;
 
-// kernel launch helpers (fft.cu)
 struct FftPlan {
-  FftAxis xh;   // packed half-length nx/2 along x
+  FftAxis xh;  // packed half-length nx/2 along x
   FftAxis y, z;
   const double2* twx;  // exp(-2 pi i k / nx), k < nx/2 (r2c/c2r packing)
+  const float2* twxf;
 };
 
-void fft_x_r2c(const Grid& g, const FftPlan& p, const double* in, double2* out, cudaStream_t s);
+// ------------------------------------------------- FFT passes (fft.cu)
+// prec: HE4G_PREC_FP64 (double fields, double2 spectra) or HE4G_PREC_MIXED
+// (float fields, float2 spectra); pointers are typed accordingly.
+void fft_x_r2c(const Grid& g, const FftPlan& p, int prec, const void* in, void* out, cudaStream_t s);
 // r2c of g = den*dencg*(cp4 + cpp4*dencg) (poten.f90:62-64), fused prologue
-void fft_x_r2c_corr(const Grid& g, const FftPlan& p, const double* den, const double* dencg,
-                    double cp4, double cpp4, double2* out, cudaStream_t s);
+void fft_x_r2c_corr(const Grid& g, const FftPlan& p, int prec, const void* den, const void* dencg, double cp4,
+                    double cpp4, void* out, cudaStream_t s);
 // r2c of a*b (term_alfa.f90:32-36)
-void fft_x_r2c_prod(const Grid& g, const FftPlan& p, const double* a, const double* b, double2* out,
+void fft_x_r2c_prod(const Grid& g, const FftPlan& p, int prec, const void* a, const void* b, void* out,
                     cudaStream_t s);
-void fft_y(const Grid& g, const FftPlan& p, double2* const* specs, int nspec, int sign, cudaStream_t s);
-// forward z, multiply by nout tables (each scaled by `scale`), inverse z
-void fft_z_conv(const Grid& g, const FftPlan& p, const double2* in, double2* const* outs,
-                const double* const* factors, int nout, double scale, cudaStream_t s);
-void fft_x_c2r(const Grid& g, const FftPlan& p, const double2* const* ins, double* const* outs,
-               int nspec, cudaStream_t s);
-// c2r of the correlation convolution fused with the pot4 assembly
+void fft_y(const Grid& g, const FftPlan& p, int prec, void* const* specs, int nspec, int sign, cudaStream_t s);
+// forward z, multiply by nout tables (each scaled by `scale`), inverse z;
+// `add` (nullable) is added to output 0
+void fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* const* outs,
+                const void* const* factors, int nout, double scale, const void* add, cudaStream_t s);
+void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins, void* const* outs, int nspec,
+               cudaStream_t s);
+// c2r of delj4 + correlation convolution fused with the rest of pot4
 // (poten.f90:80-94,110-114)
-void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, const double2* conv, const double* delj4,
-                    const double* dencg, const double* den, const Functional& fn, double* pot4,
-                    cudaStream_t s);
+void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv, const void* dencg,
+                    const void* den, const Functional& fn, void* pot4, cudaStream_t s);
 
-// stencil / pointwise kernels (field.cu)
-struct Slots;
+// ---------------------------------------- FP64 field kernels (field.cu)
 void launch_pc_predict(const Grid& g, const Stencil& st, const Functional& fn, const double2* psi,
                        double2* p3_out, double2* h1, double2* h2_out, double2* pc, const double* pot4,
                        const double* uimp, const float* timec, double* den, double c4o3dt, double c112,
@@ -131,7 +139,6 @@ void launch_energy_grad(const Grid& g, const Stencil& st, const double2* psi, co
                         cudaStream_t s);
 void launch_reduce(const double* partials, int nblocks, int nvals, double* out, cudaStream_t s);
 int pc_blocks(const Grid& g);
-
 void launch_density(const Grid& g, const double2* psi, double* den, cudaStream_t s);
 
 // OTC pointwise pieces (term_alfa.f90)
@@ -152,5 +159,39 @@ void launch_imp_pc_correct(ImpState* imp, const double* err_partials, int nblock
 void launch_imp_force(ImpState* imp, const double* partials, int nblocks, double dxyz, double mass,
                       int store_accel, cudaStream_t s);
 void launch_imp_record(ImpState* imp, double* ring, long long step, cudaStream_t s);
+
+// ------------------------- mixed-precision field kernels (fieldmp.cu)
+void launch_pc_predict_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
+                          double2* p3, float2* psi32_out, const float2* h1, float2* h2, double2* pc,
+                          const float* pot4, const float* uimp, const float* timec, float* den, double c4o3dt,
+                          double c112, cudaStream_t s);
+void launch_pc_correct_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psit32,
+                          const double2* p3, const double2* p2, const float2* h1, const float2* h2, double2* pc,
+                          const float* pot4, const float* uimp, const float* timec, double2* psi_out,
+                          float2* psi32_out, float* den, double* partials, double f3, double c9, int* health,
+                          cudaStream_t s);
+void launch_rk_stage_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
+                        const double2* psi, double2* psi_out, float2* psi32_out, double2* q, float2* f_out,
+                        const float* pot4, const float* uimp, const float* timec, float* den, double ar, double br,
+                        double cr, double dt, int* health, cudaStream_t s);
+void launch_split_mp(const Grid& g, const double2* psi, float2* psi32, float* den, cudaStream_t s);
+void launch_potenimp_mp(const Grid& g, const float* x, const float* y, const float* z, const float* potion,
+                        int npot, float delinter, ImpState* imp, int center_sel, float* uimp, cudaStream_t s);
+int force_blocks_mp(const Grid& g);
+void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const float* uimp, double* partials,
+                     cudaStream_t s);
+void launch_grad1_f(const Grid& g, const StencilF& st, int axis, const float* in, float* out, cudaStream_t s);
+void launch_falfs_f(const Grid& g, const float* denalf, float den0s, float* falfs, cudaStream_t s);
+void launch_dot3_f(const Grid& g, const float* ax, const float* ay, const float* az, const float* bx,
+                   const float* by, const float* bz, float* out, cudaStream_t s);
+void launch_ualphas_a_f(const Grid& g, const float* falfs, const float* ix, const float* iy, const float* iz,
+                        float* u, float* s1, float* s2, float* s3, float den0s, cudaStream_t s);
+void launch_ualphas_b_f(const Grid& g, float* u, const float* s4, const float* s5, const float* s6, float h2o2m4,
+                        float alphas, float* pot4, cudaStream_t s);
+void launch_energy_point_mp(const Grid& g, const Functional& fn, const float* den, const float* dencg,
+                            const float* delj4, const float* uimp, const float* falfs, const float* dx,
+                            const float* dy, const float* dz, const float* ix, const float* iy, const float* iz,
+                            const double* xs, const double* ys, const double* zs, double* partials,
+                            cudaStream_t s);
 
 }  // namespace he4g

@@ -1,5 +1,5 @@
 #!/usr/bin/env python3
-"""Throughput of the FP64 time step of the 256^3 He_5000 + Xe collision.
+"""Throughput of the time step of the 256^3 He_5000 + Xe collision.
 
 A step is one Hamming predictor–corrector step of psi and the impurity
 (steppc.f90) plus the driver's trailing re-evaluation of the impurity
@@ -8,6 +8,11 @@ sweeps, 2 mean-field evaluations (10 3D FFTs), 2 force reductions. The first
 three steps after set_state are Runge–Kutta–Gill steps and fall in the
 warm-up. Inputs (psi: 268 MB, history: 1.9 GB) are larger than L2, so no
 flush is needed between steps.
+
+The headline line is the FP64 form (the reference's arithmetic). The same
+line carries a `mixed` block: the mixed-precision form (FP32 fields, FP64
+accumulators and reductions) on the same workload, with its deviation from
+the FP64 form after the same steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -33,6 +38,8 @@ CASE = "he5000_xe_256"
 METRIC = "steps/s at 256^3 (FP64 predictor-corrector step, He_5000 + Xe)"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
+FP64 = 0
+MIXED = 1
 
 
 def set_case(name):
@@ -40,38 +47,43 @@ def set_case(name):
     CASE = name
 
 
-def algorithmic_bytes_per_step(nx, ny, nz):
-    """Compulsory HBM bytes of one predictor-corrector step per kernel family
-    (reads + writes of each launch's inputs and outputs, stencil neighbours
-    counted once, spectra as (nx/2+1)*ny*nz complex). Returns {family: bytes}."""
+def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64):
+    """Compulsory HBM bytes of one predictor-corrector step per kernel family:
+    reads + writes of each launch's inputs and outputs, stencil neighbours
+    counted once, spectra as (nx/2+1)*ny*nz complex. Returns {family: bytes}."""
     n = nx * ny * nz
     nh = (nx // 2 + 1) * ny * nz
     ev = 2  # potential evaluations per step
-    return {
+    if prec == FP64:
+        r, c = 8, 16  # real / complex element
         # R psi 16 pot4 8 uimp 8 timec 4 p3 16 h1 16 h2 16 pc 16 | W p3 16 pc 16 h2 16 den 8
-        "pc_predict": 156 * n,
+        pred = 156 * n
         # R psit 16 pot4 8 uimp 8 timec 4 p3 16 p2 16 h1 16 h2 16 pc 16 | W pc 16 psi 16 den 8
-        "pc_correct": 156 * n,
-        "potenimp": ev * 8 * n,
-        # den -> spec (8 + 16 nh/n), den,dencg -> spec (16 + 16 nh/n)
-        "fft_x_r2c": ev * (8 * n + 16 * nh + 16 * n + 16 * nh),
-        # 4 launches: fwd 1 spectrum, inv 2 spectra, fwd 1, inv 1 (read + write each)
-        "fft_y": ev * (32 * nh + 64 * nh + 32 * nh + 32 * nh),
-        # conv 1: R 16 + 2 tables x 8 | W 2 x 16 ; conv 2: R 16 + 8 | W 16
-        "fft_z_conv": ev * (64 * nh + 40 * nh),
-        # 2 spectra -> dencg, delj4
-        "fft_x_c2r": ev * (32 * nh + 16 * n),
-        # conv spectrum + delj4, dencg, den -> pot4
-        "fft_x_c2r_pot4": ev * (16 * nh + 32 * n),
-        # R den 8 + uimp 8
-        "force": ev * 16 * n,
+        corr = 156 * n
+    else:
+        r, c = 4, 8
+        # R psi32 8 pot4 4 uimp 4 timec 4 p3 16 h1 8 h2 8 pc 16 | W p3 16 psi32 8 pc 16 h2 8 den 4
+        pred = 120 * n
+        # R psit32 8 pot4 4 uimp 4 timec 4 p3 16 p2 16 h1 8 h2 8 pc 16 | W pc 16 psi 16 psi32 8 den 4
+        corr = 128 * n
+    return {
+        "pc_predict": pred,
+        "pc_correct": corr,
+        "potenimp": ev * r * n,
+        # den -> spectrum; den, dencg -> spectrum (correlation prologue)
+        "fft_x_r2c": ev * ((r * n + c * nh) + (2 * r * n + c * nh)),
+        # fwd 1, inv 1, fwd 1, inv 1 spectrum: read + write each
+        "fft_y": ev * 4 * 2 * c * nh,
+        # product 1: R spectrum + 2 tables | W 2 spectra; product 2: R spectrum + table + added spectrum | W
+        "fft_z_conv": ev * ((c + 2 * r + 2 * c) * nh + (c + r + c + c) * nh),
+        # spectrum -> dencg
+        "fft_x_c2r": ev * (c * nh + r * n),
+        # spectrum + dencg + den -> pot4
+        "fft_x_c2r_pot4": ev * (c * nh + 3 * r * n),
+        # R den + uimp
+        "force": ev * 2 * r * n,
         "impurity_scalar": 0,
     }
-
-
-def launches_per_step():
-    # per evaluation: potenimp 1, r2c 2, y 4, zconv 2, c2r 1, pot4 1, force 1, scalar 1 = 13
-    return 2 + 2 + 2 * 13
 
 
 def read_peaks():
@@ -141,16 +153,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_run():
+def make_run(prec=FP64):
     import he4gpu
     psi, r, v, meta = he4gpu.collision_case(CASE)
     kw, tk = he4gpu.config_for_case(meta)
-    cfg = he4gpu.default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], **kw)
+    cfg = he4gpu.default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], precision=prec, **kw)
     run = he4gpu.Run(cfg, selec=tk["selec"], r_cutoff=tk["r_cutoff"], umax=tk["umax"])
     return run, cfg, psi, r, v, meta
 
 
-def e2e_measure(run, psi, r, v, steps):
+def e2e_measure(run, psi, steps):
     """Steps through the public API with host buffers: per step the impurity
     state goes host->device (he4g_set_impurity, the driver's module variables),
     he4g_step runs one step, and psi plus the impurity state come back to
@@ -168,21 +180,16 @@ def e2e_measure(run, psi, r, v, steps):
     for _ in range(steps):
         run.set_impurity(rr, vv, aa)
         run.step(1)
-        rc = lib.he4g_get_psi(h, abi.dptr(host))
-        if rc:
+        if lib.he4g_get_psi(h, abi.dptr(host)):
             raise RuntimeError("get_psi failed")
         rr, vv, aa = run.impurity()
     dt = time.perf_counter() - t0
-    h2d = 72
-    d2h = psi.size * 16 + 72
-    return steps / dt, h2d, d2h
+    return steps / dt, 72, psi.size * 16 + 72
 
 
 def cpu_sample(kind_steps):
     """Times predictor-corrector steps of the FP64 CPU oracle at 256^3 (child
     process, all host cores). Prints one JSON line."""
-    import numpy as np
-
     import he4gpu
     from oracle import oracle
     psi, r, v, meta = he4gpu.collision_case(CASE)
@@ -192,8 +199,8 @@ def cpu_sample(kind_steps):
     o = oracle.OracleRun(cfg, tabs)
     o.set_state(psi, r, v)
     warm, steps = kind_steps
-    # the predictor-corrector step costs the same on any state; the sample
-    # skips the Runge–Kutta start and times PC steps directly
+    # a predictor-corrector step costs the same on any state; the sample skips
+    # the Runge–Kutta start and times PC steps plus the trailing evaluation
     for _ in range(warm):
         o.steppc(cfg.deltat)
         o.potenimp(o.impurity()[0])
@@ -207,7 +214,6 @@ def cpu_sample(kind_steps):
         o.poten()
         o.forceimp()
         ts.append(time.perf_counter() - t0)
-    del np
     print(json.dumps({"sec_per_step": statistics.median(ts), "steps": steps, "cores": os.cpu_count()}))
 
 
@@ -222,10 +228,8 @@ def run_cpu_sample(warm, steps):
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 def reference_arm(args):
@@ -254,93 +258,87 @@ def reference_arm(args):
     return 0
 
 
-def ours(args):
-    import numpy as np
-    ws, rank, local = dist_env()
-    dist = None
-    if ws > 1:
-        import torch
-        import torch.distributed as dist_mod
-        torch.cuda.set_device(local)
-        dist_mod.init_process_group("nccl")
-        dist = dist_mod
-    else:
-        try:
-            import torch
-            torch.cuda.set_device(0)
-        except Exception:
-            pass
-    import he4gpu
-    he4gpu.abi.load()
-    run, cfg, psi, r, v, meta = make_run()
-    run.set_state(psi, r, v)
-    warm = max(args.warmup, 3)
-    run.step(warm)
-
-    def barrier():
-        if dist:
-            dist.barrier()
-        try:
-            import torch
-            torch.cuda.synchronize()
-        except Exception:
-            pass
-
-    # timed region: K predictor-corrector steps, device-timed on the run's stream
+def timed_steps(run, cfg, prec, steps, barrier, clock_gpu):
+    """Device-timed steps with per-family CUDA-event times and the roofline of
+    the dominant family."""
     run.enable_timing(True)
     l0 = run.launch_count
     barrier()
-    with ClockSampler(local) as clk:
+    with ClockSampler(clock_gpu) as clk:
         t_wall = time.perf_counter()
-        dev_ms = run.step_timed(args.steps)
+        dev_ms = run.step_timed(steps)
         t_wall = time.perf_counter() - t_wall
     barrier()
     launches = run.launch_count - l0
     fam = run.kernel_times()
     run.enable_timing(False)
-    # an untimed-instrumentation repeat gives the step time without event overhead
+    # a repeat without per-launch events gives the step time without their overhead
     barrier()
-    dev_ms_clean = run.step_timed(args.steps)
+    dev_ms_clean = run.step_timed(steps)
     barrier()
     ms = min(dev_ms, dev_ms_clean)
+    bytes_fam = algorithmic_bytes_per_step(cfg.nx, cfg.ny, cfg.nz, prec)
+    tot = sum(v[0] for v in fam.values()) or 1.0
+    rows = []
+    for name, (fms, nl) in sorted(fam.items(), key=lambda x: -x[1][0]):
+        if nl == 0:
+            continue
+        b = bytes_fam.get(name, 0) * steps
+        rows.append({"family": name, "ms_total": round(fms, 4), "launches": nl, "share": round(fms / tot, 4),
+                     "gbs": round(b / (fms * 1e-3) / 1e9, 1) if fms > 0 and b else None})
+    top = rows[0]
+    peak, peak_kind = read_peaks()
+    per_launch = bytes_fam[top["family"]] * steps / top["launches"]
+    achieved = per_launch / (top["ms_total"] / top["launches"] * 1e-3) / 1e9
+    step_bytes = sum(bytes_fam.values())
+    step_gbs = step_bytes / (ms / steps * 1e-3) / 1e9
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "peak_source": peak_kind, "kernel": top["family"], "traffic": None,
+        "step_algorithmic_bytes": step_bytes, "step_gbs": step_gbs, "step_frac": step_gbs / peak,
+        "families": rows,
+    }
+    return {"ms": ms, "launches": launches, "clocks": clk.summary(), "wall_s": t_wall, "roofline": roofline}
+
+
+def ours(args):
+    ws, rank, local = dist_env()
+    dist = None
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("nccl")
+        dist = dist_mod
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    import he4gpu
+    he4gpu.abi.load()
+    prec = MIXED if args.precision == "mixed" else FP64
+    run, cfg, psi, r, v, meta = make_run(prec)
+    run.set_state(psi, r, v)
+    warm = max(args.warmup, 3)
+    run.step(warm)
+    res = timed_steps(run, cfg, prec, args.steps, barrier, local)
+    ms = res["ms"]
     if dist:
-        import torch
         t = torch.tensor([ms], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = ws * args.steps / (ms * 1e-3)
-
-    # roofline of the dominant kernel family (largest share of device time)
-    bytes_fam = algorithmic_bytes_per_step(cfg.nx, cfg.ny, cfg.nz)
-    tot = sum(v[0] for v in fam.values()) or 1.0
-    fam_rows = []
-    for name, (fms, nl) in sorted(fam.items(), key=lambda x: -x[1][0]):
-        if nl == 0:
-            continue
-        b = bytes_fam.get(name, 0) * args.steps
-        fam_rows.append({"family": name, "ms_total": fms, "launches": nl, "share": fms / tot,
-                         "gbs": (b / (fms * 1e-3) / 1e9) if fms > 0 and b else None})
-    top = fam_rows[0]
-    peak, peak_kind = read_peaks()
-    per_launch_bytes = bytes_fam[top["family"]] * args.steps / top["launches"]
-    achieved = per_launch_bytes / (top["ms_total"] / top["launches"] * 1e-3) / 1e9
-    step_bytes = sum(bytes_fam.values())
-    roofline = {
-        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-        "peak_source": peak_kind, "kernel": top["family"], "traffic": None,
-        "step_algorithmic_bytes": step_bytes,
-        "step_gbs": step_bytes / (ms / args.steps * 1e-3) / 1e9,
-        "step_frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak,
-        "families": fam_rows,
-        "note": "FP64 issue rate (1.2 TFLOP/s measured on this GPU) bounds this path, not HBM",
-    }
     line = None
     if rank == 0:
-        e2e_steps = max(3, min(args.steps, 10))
         if args.no_e2e:
             e2e_val, h2d, d2h = None, 0, 0
         else:
-            e2e_val, h2d, d2h = e2e_measure(run, psi, r, v, e2e_steps)
+            e2e_val, h2d, d2h = e2e_measure(run, psi, max(3, min(args.steps, 10)))
+        mixed_block = None
+        if prec == FP64 and ws == 1 and not args.no_mixed:
+            mixed_block = mixed_measure(args, run, barrier, local)
         cpu = None
         if ws == 1 and not args.no_cpu:
             try:
@@ -351,25 +349,31 @@ def ours(args):
             except Exception as e:  # reported, not fatal
                 cpu = {"value": None, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
                        "sample": f"failed: {e}"[:300]}
+        rf = res["roofline"]
         line = {
-            "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": warm, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Woods-Saxon droplet + Xe)",
-            "config": {"workload": CASE + " FP64 predictor-corrector step", "grid": [cfg.nx, cfg.ny, cfg.nz],
-                       "h": meta["h"], "n4": meta["n4"], "impurity": meta["imp"], "v_A_per_ps": meta["v"],
-                       "impact_parameter": f"{meta['b_frac']} R",
+            "metric": METRIC if prec == FP64 else METRIC.replace("FP64", "mixed-precision"),
+            "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps, "warmup": warm,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == FP64 else "mixed (f32 fields, f64 accumulators)",
+            "data": "synthetic (seeded Woods-Saxon droplet + Xe)",
+            "config": {"workload": CASE + (" FP64" if prec == FP64 else " mixed") + " predictor-corrector step",
+                       "grid": [cfg.nx, cfg.ny, cfg.nz], "h": meta["h"], "n4": meta["n4"], "impurity": meta["imp"],
+                       "v_A_per_ps": meta["v"], "impact_parameter": f"{meta['b_frac']} R",
                        "l2": "inputs larger than L2 (psi 268 MB, history 1.9 GB); no flush",
                        "parallelism": f"replicas x{ws}"},
             "grid_point_updates_per_s": value * cfg.nx * cfg.ny * cfg.nz,
-            "hbm_gbs": roofline["step_gbs"],
-            "roofline": roofline,
+            "hbm_gbs": rf["step_gbs"],
+            "roofline": rf,
+            "fp64_note": ("FP64 issue bounds the FP64 form (GB300: 1.2 TFLOP/s FP64, 1/61 of FP32); ncu shows "
+                          "77-88% FP64-pipe activity in every kernel" if prec == FP64 else None),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val * ws if e2e_val else None, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches,
-            "gpu_launches_per_step": launches / args.steps,
-            "clocks": clk.summary(),
-            "wall_s_timed": t_wall,
+            "gpu_launches": res["launches"],
+            "gpu_launches_per_step": res["launches"] / args.steps,
+            "clocks": res["clocks"],
+            "wall_s_timed": res["wall_s"],
+            "mixed": mixed_block,
         }
     if dist:
         dist.barrier()
@@ -377,8 +381,41 @@ def ours(args):
     run.close()
     if line:
         print(json.dumps(line), flush=True)
-    del np
     return 0
+
+
+def mixed_measure(args, run64, barrier, gpu):
+    """The mixed-precision form on the same workload, and its deviation from
+    the FP64 run after the same number of steps."""
+    import numpy as np
+    run, cfg, psi, r, v, meta = make_run(MIXED)
+    run.set_state(psi, r, v)
+    steps64 = run64.steps_taken
+    warm = max(args.warmup, 3)
+    run.step(warm)
+    res = timed_steps(run, cfg, MIXED, args.steps, barrier, gpu)
+    # bring both runs to the same step count, then compare
+    run.step(max(0, steps64 - run.steps_taken))
+    extra = run.steps_taken - run64.steps_taken
+    if extra > 0:
+        run64.step(extra)
+    d64, dmx = run64.den, run.den
+    e64, emx = run64.energy(), run.energy()
+    r64, rmx = run64.impurity()[0], run.impurity()[0]
+    dev = {
+        "steps": run.steps_taken,
+        "den_max_rel": float(np.max(np.abs(dmx - d64)) / np.max(np.abs(d64))),
+        "norm_rel": float(abs(dmx.sum() - d64.sum()) / d64.sum()),
+        "etot_rel": float(abs(emx["etot"] - e64["etot"]) / abs(e64["etot"])),
+        "rimp_abs_A": float(np.max(np.abs(rmx - r64))),
+    }
+    ms = res["ms"]
+    run.close()
+    rf = res["roofline"]
+    return {"value": args.steps / (ms * 1e-3), "unit": "steps/s", "ms_per_step": ms / args.steps,
+            "dtype": "f32 fields/stencils/FFTs; f64 psi accumulator, reductions, force sum, trajectory",
+            "hbm_gbs": rf["step_gbs"], "roofline": rf, "gpu_launches": res["launches"],
+            "clocks": res["clocks"], "vs_fp64": dev}
 
 
 def main():
@@ -390,8 +427,10 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision block")
     ap.add_argument("--case", default=CASE, help="workload (profiling runs use smaller ones)")
     args = ap.parse_args()
     set_case(args.case)

@@ -48,7 +48,13 @@ extern "C" {
 #define HE4G_CORE_OTC 1 /* 'OTC': full Orsay–Trento with the alpha_s term     */
 
 /* arithmetic of the per-step fields */
-#define HE4G_PREC_FP64 0 /* every field and transform in FP64 (reference)   */
+/* HE4G_PREC_FP64: every field and transform in FP64 (the reference).
+ * HE4G_PREC_MIXED: FFT convolutions, stencils, H.psi and the pointwise
+ * functional in FP32; psi, its history, pc and q (the update accumulator),
+ * the norm and energy sums, the force sum and the impurity trajectory in
+ * FP64. */
+#define HE4G_PREC_FP64 0
+#define HE4G_PREC_MIXED 1
 
 /*
  * Run configuration. Defaults (he4g_default_config) are the reference's module
