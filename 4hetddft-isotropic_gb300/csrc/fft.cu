@@ -30,18 +30,33 @@ constexpr int kThreads = 256;
 
 template <typename R>
 struct Cx;
+// kTile: kx columns per y/z block (128-byte rows). kPad: shared-memory lines
+// get one padding element per 128 bytes (element i sits at i + (i >> kPad)),
+// which spreads the strided writes of the Stockham passes over all banks.
 template <>
 struct Cx<double> {
   using T = double2;
-  static constexpr int kTile = 8;  // kx columns per y/z block: 128-byte rows
+  static constexpr int kTile = 8;
+  static constexpr int kPad = 3;
 };
 template <>
 struct Cx<float> {
   using T = float2;
   static constexpr int kTile = 16;
+  static constexpr int kPad = 4;
 };
 template <typename R>
 using C2 = typename Cx<R>::T;
+
+template <typename R>
+__device__ __forceinline__ int pidx(int i) {
+  return i + (i >> Cx<R>::kPad);
+}
+// shared-memory stride of a line holding n elements
+template <typename R>
+__host__ __device__ constexpr int padded_len(int n) {
+  return n + (n >> Cx<R>::kPad) + 1;
+}
 
 template <typename R>
 __device__ __forceinline__ C2<R> mk(R x, R y) {
@@ -174,7 +189,7 @@ __device__ __forceinline__ void stockham_pass(const C2<R>* __restrict__ src, C2<
     const C2<R>* s = src + l * ld;
     C2<R> v[RAD];
 #pragma unroll
-    for (int r = 0; r < RAD; ++r) v[r] = s[j + r * nr];
+    for (int r = 0; r < RAD; ++r) v[r] = s[pidx<R>(j + r * nr)];
     if (k > 0) {
 #pragma unroll
       for (int r = 1; r < RAD; ++r) v[r] = mulw<R, SIGN>(v[r], __ldg(&tw[r * k * tstep]));
@@ -183,7 +198,7 @@ __device__ __forceinline__ void stockham_pass(const C2<R>* __restrict__ src, C2<
     const int idx = (j / ns) * ns * RAD + k;
     C2<R>* d = dst + l * ld;
 #pragma unroll
-    for (int r = 0; r < RAD; ++r) d[idx + r * ns] = v[r];
+    for (int r = 0; r < RAD; ++r) d[pidx<R>(idx + r * ns)] = v[r];
   }
 }
 
@@ -231,7 +246,7 @@ __global__ void __launch_bounds__(kThreads) k_x_r2c(Grid g, FftAxis ax, const C2
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
   const int m = ax.n;
-  const int ld = m + 1;
+  const int ld = padded_len<R>(m);
   C2<R>* a = sm;
   C2<R>* b = sm + lpb * ld;
   const long long nlines = (long long)g.ny * g.nz;
@@ -253,7 +268,7 @@ __global__ void __launch_bounds__(kThreads) k_x_r2c(Grid g, FftAxis ax, const C2
       const C2<R> q = ld_pair<R>(in1 + e);
       v = mk<R>(p.x * q.x, p.y * q.y);
     }
-    a[l * ld + j] = v;
+    a[l * ld + pidx<R>(j)] = v;
   }
   __syncthreads();
   C2<R>* r = fft_smem<R, -1>(a, b, nl, ld, ax);
@@ -261,8 +276,8 @@ __global__ void __launch_bounds__(kThreads) k_x_r2c(Grid g, FftAxis ax, const C2
   const int half = m / 2;
   for (int w = threadIdx.x; w < nl * (half + 1); w += blockDim.x) {
     const int l = w / (half + 1), k = w - l * (half + 1);
-    const C2<R> zk = r[l * ld + k];
-    const C2<R> zm = r[l * ld + (k == 0 ? 0 : m - k)];
+    const C2<R> zk = r[l * ld + pidx<R>(k)];
+    const C2<R> zm = r[l * ld + pidx<R>(k == 0 ? 0 : m - k)];
     C2<R>* o = out + (l0 + l) * g.nxh;
     if (k == 0) {
       o[0] = mk<R>((R)2 * (zk.x + zk.y), (R)0);
@@ -297,7 +312,7 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
   const int m = ax.n;
-  const int ld = m + 2;
+  const int ld = padded_len<R>(m + 1);
   C2<R>* a = sm;
   C2<R>* b = sm + lpb * ld;
   const C2<R>* in = blockIdx.y == 0 ? in0 : in1;
@@ -307,15 +322,15 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
   const int nl = (int)min((long long)lpb, nlines - l0);
   for (int w = threadIdx.x; w < nl * (m + 1); w += blockDim.x) {
     const int l = w / (m + 1), k = w - l * (m + 1);
-    b[l * ld + k] = __ldg(&in[(l0 + l) * g.nxh + k]);
+    b[l * ld + pidx<R>(k)] = __ldg(&in[(l0 + l) * g.nxh + k]);
   }
   __syncthreads();
   // tangle: Z[k] = Fe + i Fo, Fe = X[k] + conj(X[m-k]), Fo = (X[k] - conj(X[m-k])) conj(W^k)
   const int half = m / 2;
   for (int w = threadIdx.x; w < nl * (half + 1); w += blockDim.x) {
     const int l = w / (half + 1), k = w - l * (half + 1);
-    const C2<R> xk = b[l * ld + k];
-    const C2<R> xm = b[l * ld + m - k];
+    const C2<R> xk = b[l * ld + pidx<R>(k)];
+    const C2<R> xm = b[l * ld + pidx<R>(m - k)];
     if (k == 0) {
       // the imaginary parts of the x-DC and Nyquist bins carry no real data
       a[l * ld] = mk<R>(xk.x + xm.x, xk.x - xm.x);
@@ -323,15 +338,15 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
     }
     const C2<R> fe = cadd<R>(xk, cconj<R>(xm));
     const C2<R> fo = mulw<R, 1>(csub<R>(xk, cconj<R>(xm)), __ldg(&twx[k]));
-    a[l * ld + k] = cadd<R>(fe, jmul<R, 1>(fo));
-    if (k != m - k) a[l * ld + m - k] = cadd<R>(cconj<R>(fe), jmul<R, 1>(cconj<R>(fo)));
+    a[l * ld + pidx<R>(k)] = cadd<R>(fe, jmul<R, 1>(fo));
+    if (k != m - k) a[l * ld + pidx<R>(m - k)] = cadd<R>(cconj<R>(fe), jmul<R, 1>(cconj<R>(fo)));
   }
   __syncthreads();
   C2<R>* r = fft_smem<R, 1>(a, b, nl, ld, ax);
   for (int w = threadIdx.x; w < nl * m; w += blockDim.x) {
     const int l = w / m, j = w - l * m;
     const long long e = (l0 + l) * g.nx + 2 * j;
-    C2<R> v = r[l * ld + j];
+    C2<R> v = r[l * ld + pidx<R>(j)];
     if (EPI == EPI_POT4) {
       const Functional& fn = pa.fn;
       const C2<R> cg = ld_pair<R>(pa.dencg + e);
@@ -365,7 +380,7 @@ __global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> 
   C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
   constexpr int TX = Cx<R>::kTile;
   const int n = ax.n;  // ny
-  const int ld = n + 1;
+  const int ld = padded_len<R>(n);
   C2<R>* a = sm;
   C2<R>* b = sm + TX * ld;
   C2<R>* sp = specs.p[blockIdx.z];
@@ -374,13 +389,13 @@ __global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> 
   const long long base = (long long)blockIdx.y * g.ny * g.nxh + kx0;
   for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
     const int c = w % TX, j = w / TX;
-    if (c < ncol) a[c * ld + j] = sp[base + (long long)j * g.nxh + c];
+    if (c < ncol) a[c * ld + pidx<R>(j)] = sp[base + (long long)j * g.nxh + c];
   }
   __syncthreads();
   C2<R>* r = fft_smem<R, SIGN>(a, b, ncol, ld, ax);
   for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
     const int c = w % TX, j = w / TX;
-    if (c < ncol) sp[base + (long long)j * g.nxh + c] = r[c * ld + j];
+    if (c < ncol) sp[base + (long long)j * g.nxh + c] = r[c * ld + pidx<R>(j)];
   }
 }
 
@@ -400,7 +415,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
   constexpr int TX = Cx<R>::kTile;
   const int n = ax.n;  // nz
-  const int ld = n + 1;
+  const int ld = padded_len<R>(n);
   C2<R>* a = sm;
   C2<R>* b = sm + TX * ld;
   C2<R>* c = sm + 2 * TX * ld;
@@ -410,7 +425,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   const long long base = (long long)blockIdx.y * g.nxh + kx0;
   for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
     const int cc = w % TX, k = w / TX;
-    if (cc < ncol) a[cc * ld + k] = in[base + (long long)k * plane + cc];
+    if (cc < ncol) a[cc * ld + pidx<R>(k)] = in[base + (long long)k * plane + cc];
   }
   __syncthreads();
   C2<R>* fwd = fft_smem<R, -1>(a, b, ncol, ld, ax);
@@ -421,8 +436,8 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
       const int cc = w % TX, k = w / TX;
       if (cc < ncol) {
         const R f = __ldg(&fac[base + (long long)k * plane + cc]) * scale;
-        const C2<R> v = fwd[cc * ld + k];
-        s1[cc * ld + k] = mk<R>(v.x * f, v.y * f);
+        const C2<R> v = fwd[cc * ld + pidx<R>(k)];
+        s1[cc * ld + pidx<R>(k)] = mk<R>(v.x * f, v.y * f);
       }
     }
     __syncthreads();
@@ -432,7 +447,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
       const int cc = w % TX, k = w / TX;
       if (cc < ncol) {
         const long long e = base + (long long)k * plane + cc;
-        C2<R> v = r[cc * ld + k];
+        C2<R> v = r[cc * ld + pidx<R>(k)];
         if (o == 0 && add) v = cadd<R>(v, add[e]);
         dst[e] = v;
       }
@@ -468,7 +483,7 @@ template <typename R, int PRO>
 void launch_r2c(const Grid& g, const FftPlan& p, const R* a, const R* b, R c0, R c1, C2<R>* out, cudaStream_t s) {
   const int m = p.xh.n;
   const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(C2<R>) * 2 * lpb * (m + 1);
+  const size_t smem = sizeof(C2<R>) * 2 * lpb * padded_len<R>(m);
   set_smem(k_x_r2c<R, PRO>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb));
@@ -480,7 +495,7 @@ void y_impl(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int 
   constexpr int TX = Cx<R>::kTile;
   SpecList<R> sl{};
   for (int i = 0; i < nspec; ++i) sl.p[i] = static_cast<C2<R>*>(specs[i]);
-  const size_t smem = sizeof(C2<R>) * 2 * TX * (p.y.n + 1);
+  const size_t smem = sizeof(C2<R>) * 2 * TX * padded_len<R>(p.y.n);
   dim3 grid((g.nxh + TX - 1) / TX, g.nz, nspec);
   if (sign < 0) {
     set_smem(k_y<R, -1>, smem);
@@ -500,7 +515,7 @@ void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* ou
     fl.f[i] = static_cast<const R*>(factors[i]);
     fl.out[i] = static_cast<C2<R>*>(outs[i]);
   }
-  const size_t smem = sizeof(C2<R>) * 3 * TX * (p.z.n + 1);
+  const size_t smem = sizeof(C2<R>) * 3 * TX * padded_len<R>(p.z.n);
   set_smem(k_z_conv<R>, smem);
   dim3 grid((g.nxh + TX - 1) / TX, g.ny);
   k_z_conv<R><<<grid, kThreads, smem, s>>>(g, p.z, static_cast<const C2<R>*>(in), fl, nout, (R)scale,
@@ -511,7 +526,7 @@ template <typename R>
 void c2r_impl(const Grid& g, const FftPlan& p, const void* const* ins, void* const* outs, int nspec, cudaStream_t s) {
   const int m = p.xh.n;
   const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(C2<R>) * 2 * lpb * (m + 2);
+  const size_t smem = sizeof(C2<R>) * 2 * lpb * padded_len<R>(m + 1);
   set_smem(k_x_c2r<R, EPI_STORE>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb), nspec);
@@ -528,7 +543,7 @@ void pot4_impl(const Grid& g, const FftPlan& p, const void* conv, const void* de
                const Functional& fn, void* pot4, cudaStream_t s) {
   const int m = p.xh.n;
   const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(C2<R>) * 2 * lpb * (m + 2);
+  const size_t smem = sizeof(C2<R>) * 2 * lpb * padded_len<R>(m + 1);
   set_smem(k_x_c2r<R, EPI_POT4>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb), 1);

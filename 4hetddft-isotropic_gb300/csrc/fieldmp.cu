@@ -252,8 +252,12 @@ __global__ void __launch_bounds__(256) k_potenimp_mp(Grid g, const float* __rest
   const float dy = __ldg(ys + t.j) - (float)c1;
   const float dx = __ldg(xs + t.i) - (float)c0;
   const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-  const int ir = (int)(r / delinter);
-  const float w = fmodf(r, delinter) / delinter;
+  // node and weight from one quotient: the reference's int(r/d), mod(r,d)/d
+  // pair disagrees at table nodes whenever r/d rounds up, and in FP32 that
+  // happens often enough to put a full table step into uimp
+  const float qd = r / delinter;
+  const int ir = (int)qd;
+  const float w = qd - (float)ir;
   float u = 0.f;
   if (ir >= 0 && ir + 1 < npot) {
     u = fmaf(__ldg(potion + ir), 1.f - w, __ldg(potion + ir + 1) * w);
@@ -263,14 +267,23 @@ __global__ void __launch_bounds__(256) k_potenimp_mp(Grid g, const float* __rest
   uimp[t.p] = u;
 }
 
-// grad(den) . uimp summed per block: each thread walks kZ z-planes and
-// accumulates its FP32 products in FP64
+// grad(den) . uimp summed per block: each thread walks kZ z-planes with a
+// compensated (Kahan) FP32 sum of its products, then the block and the grid
+// sum in FP64
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = x - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
 __global__ void __launch_bounds__(256) k_force_mp(Grid g, StencilF st, const float* __restrict__ den,
                                                    const float* __restrict__ uimp, double* partials) {
   const int i = blockIdx.x * kBX + threadIdx.x;
   const int j = blockIdx.y * kBY + threadIdx.y;
   const int k0 = blockIdx.z * kZ;
   double v[3] = {0.0, 0.0, 0.0};
+  float s[3] = {0.f, 0.f, 0.f}, cc[3] = {0.f, 0.f, 0.f};
   if (i < g.nx && j < g.ny) {
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
     for (int k = k0; k < min(k0 + kZ, g.nz); ++k) {
@@ -289,10 +302,12 @@ __global__ void __launch_bounds__(256) k_force_mp(Grid g, StencilF st, const flo
         gz = fmaf(st.d1[2][o], b - a, gz);
       }
       const float u = __ldg(uimp + p);
-      v[0] += (double)(gx * u);
-      v[1] += (double)(gy * u);
-      v[2] += (double)(gz * u);
+      kahan_add(s[0], cc[0], gx * u);
+      kahan_add(s[1], cc[1], gy * u);
+      kahan_add(s[2], cc[2], gz * u);
     }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) v[a] = (double)s[a] - (double)cc[a];
   }
   block_sum_d<3>(v, partials);
 }
