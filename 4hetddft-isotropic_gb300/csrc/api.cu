@@ -233,6 +233,16 @@ void make_axis(he4g_run* r, FftAxis& ax, int n) {
     ax.fac[ax.nf++] = 5;
     m /= 5;
   }
+  // exact multiply-high division for the pass indices (w < 2^16, d <= 320:
+  // the rounding excess w/2^32 stays below 1/d)
+  int ns = 1;
+  for (int f = 0; f < ax.nf; ++f) {
+    const unsigned long long two32 = 1ull << 32;
+    const unsigned long long nr = (unsigned long long)(n / ax.fac[f]);
+    ax.mag_nr[f] = nr == 1 ? 0u : (unsigned)((two32 + nr - 1) / nr);  // 0: divisor 1
+    ax.mag_ns[f] = ns == 1 ? 0u : (unsigned)((two32 + ns - 1) / ns);
+    ns *= ax.fac[f];
+  }
   std::vector<double2> tw(n);
   std::vector<float2> twf(n);
   for (int t = 0; t < n; ++t) {

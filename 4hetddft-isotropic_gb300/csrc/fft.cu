@@ -42,7 +42,7 @@ struct Cx<double> {
 template <>
 struct Cx<float> {
   using T = float2;
-  static constexpr int kTile = 16;
+  static constexpr int kTile = 8;
   static constexpr int kPad = 4;
 };
 template <typename R>
@@ -176,50 +176,64 @@ __device__ __forceinline__ const float2* twiddles<float>(const FftAxis& ax) {
 
 // One Stockham pass of radix RAD over `nlines` lines of length n held in
 // shared memory at src + l*ld (natural order in, autosorted order out).
+// w / d by multiply-high (mag = ceil(2^32/d); mag == 0 marks d == 1)
+__device__ __forceinline__ int mdiv(int w, unsigned mag) { return mag ? (int)__umulhi((unsigned)w, mag) : w; }
+
+// tw points to the n twiddles of the axis staged in shared memory.
 template <typename R, int RAD, int SIGN>
 __device__ __forceinline__ void stockham_pass(const C2<R>* __restrict__ src, C2<R>* __restrict__ dst, int n,
-                                              int ns, int nlines, int ld, const C2<R>* __restrict__ tw) {
+                                              int ns, int nlines, int ld, const C2<R>* __restrict__ tw,
+                                              unsigned mag_nr, unsigned mag_ns) {
   const int nr = n / RAD;
   const int tstep = n / (ns * RAD);
   const int total = nlines * nr;
   for (int w = threadIdx.x; w < total; w += blockDim.x) {
-    const int l = w / nr;
+    const int l = mdiv(w, mag_nr);
     const int j = w - l * nr;
-    const int k = j % ns;
+    const int q = mdiv(j, mag_ns);
+    const int k = j - q * ns;
     const C2<R>* s = src + l * ld;
     C2<R> v[RAD];
 #pragma unroll
     for (int r = 0; r < RAD; ++r) v[r] = s[pidx<R>(j + r * nr)];
     if (k > 0) {
 #pragma unroll
-      for (int r = 1; r < RAD; ++r) v[r] = mulw<R, SIGN>(v[r], __ldg(&tw[r * k * tstep]));
+      for (int r = 1; r < RAD; ++r) v[r] = mulw<R, SIGN>(v[r], tw[r * k * tstep]);
     }
     butterfly<R, RAD, SIGN>(v);
-    const int idx = (j / ns) * ns * RAD + k;
+    const int idx = q * ns * RAD + k;
     C2<R>* d = dst + l * ld;
 #pragma unroll
     for (int r = 0; r < RAD; ++r) d[pidx<R>(idx + r * ns)] = v[r];
   }
 }
 
-// Full transform of nlines lines; a holds the input, b is scratch; returns
-// the buffer that holds the result. Ends with a barrier.
-template <typename R, int SIGN>
-__device__ C2<R>* fft_smem(C2<R>* a, C2<R>* b, int nlines, int ld, const FftAxis& ax) {
+// Copies the axis' n twiddles into shared memory (caller syncs).
+template <typename R>
+__device__ __forceinline__ void stage_twiddles(C2<R>* tws, const FftAxis& ax) {
   const C2<R>* tw = twiddles<R>(ax);
+  for (int t = threadIdx.x; t < ax.n; t += blockDim.x) tws[t] = __ldg(&tw[t]);
+}
+
+// Full transform of nlines lines; a holds the input, b is scratch, tws the
+// staged twiddles; returns the buffer that holds the result. Ends with a
+// barrier.
+template <typename R, int SIGN>
+__device__ C2<R>* fft_smem(C2<R>* a, C2<R>* b, int nlines, int ld, const FftAxis& ax, const C2<R>* tws) {
   int ns = 1;
   for (int f = 0; f < ax.nf; ++f) {
     const int rad = ax.fac[f];
+    const unsigned mnr = ax.mag_nr[f], mns = ax.mag_ns[f];
     if (rad == 8)
-      stockham_pass<R, 8, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
+      stockham_pass<R, 8, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
     else if (rad == 4)
-      stockham_pass<R, 4, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
+      stockham_pass<R, 4, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
     else if (rad == 2)
-      stockham_pass<R, 2, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
+      stockham_pass<R, 2, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
     else if (rad == 3)
-      stockham_pass<R, 3, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
+      stockham_pass<R, 3, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
     else
-      stockham_pass<R, 5, SIGN>(a, b, ax.n, ns, nlines, ld, tw);
+      stockham_pass<R, 5, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
     __syncthreads();
     C2<R>* t = a;
     a = b;
@@ -270,8 +284,10 @@ __global__ void __launch_bounds__(kThreads) k_x_r2c(Grid g, FftAxis ax, const C2
     }
     a[l * ld + pidx<R>(j)] = v;
   }
+  C2<R>* tws = sm + 2 * lpb * ld;
+  stage_twiddles<R>(tws, ax);
   __syncthreads();
-  C2<R>* r = fft_smem<R, -1>(a, b, nl, ld, ax);
+  C2<R>* r = fft_smem<R, -1>(a, b, nl, ld, ax, tws);
   // untangle: 2X[k] = Fe + W^k (-i) Fo, 2X[m-k] = conj(Fe - W^k (-i) Fo)
   const int half = m / 2;
   for (int w = threadIdx.x; w < nl * (half + 1); w += blockDim.x) {
@@ -324,6 +340,8 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
     const int l = w / (m + 1), k = w - l * (m + 1);
     b[l * ld + pidx<R>(k)] = __ldg(&in[(l0 + l) * g.nxh + k]);
   }
+  C2<R>* tws = sm + 2 * lpb * ld;
+  stage_twiddles<R>(tws, ax);
   __syncthreads();
   // tangle: Z[k] = Fe + i Fo, Fe = X[k] + conj(X[m-k]), Fo = (X[k] - conj(X[m-k])) conj(W^k)
   const int half = m / 2;
@@ -342,7 +360,7 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
     if (k != m - k) a[l * ld + pidx<R>(m - k)] = cadd<R>(cconj<R>(fe), jmul<R, 1>(cconj<R>(fo)));
   }
   __syncthreads();
-  C2<R>* r = fft_smem<R, 1>(a, b, nl, ld, ax);
+  C2<R>* r = fft_smem<R, 1>(a, b, nl, ld, ax, tws);
   for (int w = threadIdx.x; w < nl * m; w += blockDim.x) {
     const int l = w / m, j = w - l * m;
     const long long e = (l0 + l) * g.nx + 2 * j;
@@ -391,8 +409,10 @@ __global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> 
     const int c = w % TX, j = w / TX;
     if (c < ncol) a[c * ld + pidx<R>(j)] = sp[base + (long long)j * g.nxh + c];
   }
+  C2<R>* tws = sm + 2 * TX * ld;
+  stage_twiddles<R>(tws, ax);
   __syncthreads();
-  C2<R>* r = fft_smem<R, SIGN>(a, b, ncol, ld, ax);
+  C2<R>* r = fft_smem<R, SIGN>(a, b, ncol, ld, ax, tws);
   for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
     const int c = w % TX, j = w / TX;
     if (c < ncol) sp[base + (long long)j * g.nxh + c] = r[c * ld + pidx<R>(j)];
@@ -427,8 +447,10 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
     const int cc = w % TX, k = w / TX;
     if (cc < ncol) a[cc * ld + pidx<R>(k)] = in[base + (long long)k * plane + cc];
   }
+  C2<R>* tws = sm + 3 * TX * ld;
+  stage_twiddles<R>(tws, ax);
   __syncthreads();
-  C2<R>* fwd = fft_smem<R, -1>(a, b, ncol, ld, ax);
+  C2<R>* fwd = fft_smem<R, -1>(a, b, ncol, ld, ax, tws);
   C2<R>* s1 = fwd == a ? b : a;
   for (int o = 0; o < nout; ++o) {
     const R* fac = fl.f[o];
@@ -441,7 +463,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
       }
     }
     __syncthreads();
-    C2<R>* r = fft_smem<R, 1>(s1, c, ncol, ld, ax);
+    C2<R>* r = fft_smem<R, 1>(s1, c, ncol, ld, ax, tws);
     C2<R>* dst = fl.out[o];
     for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
       const int cc = w % TX, k = w / TX;
@@ -483,7 +505,7 @@ template <typename R, int PRO>
 void launch_r2c(const Grid& g, const FftPlan& p, const R* a, const R* b, R c0, R c1, C2<R>* out, cudaStream_t s) {
   const int m = p.xh.n;
   const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(C2<R>) * 2 * lpb * padded_len<R>(m);
+  const size_t smem = sizeof(C2<R>) * (2 * lpb * padded_len<R>(m) + m);
   set_smem(k_x_r2c<R, PRO>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb));
@@ -495,7 +517,7 @@ void y_impl(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int 
   constexpr int TX = Cx<R>::kTile;
   SpecList<R> sl{};
   for (int i = 0; i < nspec; ++i) sl.p[i] = static_cast<C2<R>*>(specs[i]);
-  const size_t smem = sizeof(C2<R>) * 2 * TX * padded_len<R>(p.y.n);
+  const size_t smem = sizeof(C2<R>) * (2 * TX * padded_len<R>(p.y.n) + p.y.n);
   dim3 grid((g.nxh + TX - 1) / TX, g.nz, nspec);
   if (sign < 0) {
     set_smem(k_y<R, -1>, smem);
@@ -515,7 +537,7 @@ void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* ou
     fl.f[i] = static_cast<const R*>(factors[i]);
     fl.out[i] = static_cast<C2<R>*>(outs[i]);
   }
-  const size_t smem = sizeof(C2<R>) * 3 * TX * padded_len<R>(p.z.n);
+  const size_t smem = sizeof(C2<R>) * (3 * TX * padded_len<R>(p.z.n) + p.z.n);
   set_smem(k_z_conv<R>, smem);
   dim3 grid((g.nxh + TX - 1) / TX, g.ny);
   k_z_conv<R><<<grid, kThreads, smem, s>>>(g, p.z, static_cast<const C2<R>*>(in), fl, nout, (R)scale,
@@ -526,7 +548,7 @@ template <typename R>
 void c2r_impl(const Grid& g, const FftPlan& p, const void* const* ins, void* const* outs, int nspec, cudaStream_t s) {
   const int m = p.xh.n;
   const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(C2<R>) * 2 * lpb * padded_len<R>(m + 1);
+  const size_t smem = sizeof(C2<R>) * (2 * lpb * padded_len<R>(m + 1) + m);
   set_smem(k_x_c2r<R, EPI_STORE>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb), nspec);
@@ -543,7 +565,7 @@ void pot4_impl(const Grid& g, const FftPlan& p, const void* conv, const void* de
                const Functional& fn, void* pot4, cudaStream_t s) {
   const int m = p.xh.n;
   const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(C2<R>) * 2 * lpb * padded_len<R>(m + 1);
+  const size_t smem = sizeof(C2<R>) * (2 * lpb * padded_len<R>(m + 1) + m);
   set_smem(k_x_c2r<R, EPI_POT4>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb), 1);

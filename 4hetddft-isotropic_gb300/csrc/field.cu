@@ -21,6 +21,7 @@ namespace he4g {
 namespace {
 
 constexpr int kBX = 64, kBY = 4;  // point-kernel blocks (256 threads)
+constexpr int kFinalThreads = 1024;  // single-block sums of the block partials
 
 __device__ __forceinline__ double2 ld2(const double2* p) { return __ldg(p); }
 
@@ -398,7 +399,7 @@ __global__ void __launch_bounds__(256) k_energy_grad(Grid g, Stencil st, const d
 
 // sums nvals columns of partials[nblocks][nvals] in a fixed order
 __device__ void reduce_cols(const double* partials, int nblocks, int nvals, double* out) {
-  __shared__ double sh[kRedBlock];
+  __shared__ double sh[kFinalThreads];
   for (int a = 0; a < nvals; ++a) {
     double x = 0.0;
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x) x += partials[(long long)b * nvals + a];
@@ -413,7 +414,7 @@ __device__ void reduce_cols(const double* partials, int nblocks, int nvals, doub
   }
 }
 
-__global__ void __launch_bounds__(kRedBlock) k_reduce(const double* partials, int nblocks, int nvals,
+__global__ void __launch_bounds__(kFinalThreads) k_reduce(const double* partials, int nblocks, int nvals,
                                                        double* out) {
   reduce_cols(partials, nblocks, nvals, out);
 }
@@ -481,7 +482,7 @@ __global__ void k_imp_pc_predict(ImpState* s, double f, double c112) {
 }
 
 // errHe reduction + corrector of (r, v) (steppc.f90:131-174)
-__global__ void __launch_bounds__(kRedBlock) k_imp_pc_correct(ImpState* s, const double* partials, int nblocks,
+__global__ void __launch_bounds__(kFinalThreads) k_imp_pc_correct(ImpState* s, const double* partials, int nblocks,
                                                                double dt, double c9, double nxyz) {
   __shared__ double tot[1];
   reduce_cols(partials, nblocks, 1, tot);
@@ -522,7 +523,7 @@ __global__ void __launch_bounds__(kRedBlock) k_imp_pc_correct(ImpState* s, const
 }
 
 // F = -sum(grad den * uimp) * dxyz; aimp = F / m when store_accel
-__global__ void __launch_bounds__(kRedBlock) k_imp_force(ImpState* s, const double* partials, int nblocks,
+__global__ void __launch_bounds__(kFinalThreads) k_imp_force(ImpState* s, const double* partials, int nblocks,
                                                           double dxyz, double mass, int store_accel) {
   __shared__ double tot[3];
   reduce_cols(partials, nblocks, 3, tot);
@@ -639,7 +640,7 @@ void launch_energy_grad(const Grid& g, const Stencil& st, const double2* psi, co
   k_energy_grad<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, psi, xs, ys, zs, cm, partials);
 }
 void launch_reduce(const double* partials, int nblocks, int nvals, double* out, cudaStream_t s) {
-  k_reduce<<<1, kRedBlock, 0, s>>>(partials, nblocks, nvals, out);
+  k_reduce<<<1, kFinalThreads, 0, s>>>(partials, nblocks, nvals, out);
 }
 void launch_density(const Grid& g, const double2* psi, double* den, cudaStream_t s) {
   k_density<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, psi, den);
@@ -667,11 +668,11 @@ void launch_imp_pc_predict(ImpState* imp, double c4o3dt, double c112, cudaStream
 }
 void launch_imp_pc_correct(ImpState* imp, const double* err_partials, int nblocks, double dt, double c9,
                            double nxyz, cudaStream_t s) {
-  k_imp_pc_correct<<<1, kRedBlock, 0, s>>>(imp, err_partials, nblocks, dt, c9, nxyz);
+  k_imp_pc_correct<<<1, kFinalThreads, 0, s>>>(imp, err_partials, nblocks, dt, c9, nxyz);
 }
 void launch_imp_force(ImpState* imp, const double* partials, int nblocks, double dxyz, double mass,
                       int store_accel, cudaStream_t s) {
-  k_imp_force<<<1, kRedBlock, 0, s>>>(imp, partials, nblocks, dxyz, mass, store_accel);
+  k_imp_force<<<1, kFinalThreads, 0, s>>>(imp, partials, nblocks, dxyz, mass, store_accel);
 }
 void launch_imp_record(ImpState* imp, double* ring, long long step, cudaStream_t s) {
   k_imp_record<<<1, 32, 0, s>>>(imp, ring, step);

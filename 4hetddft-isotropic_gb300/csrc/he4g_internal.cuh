@@ -20,10 +20,15 @@ constexpr int kRedBlock = 256;    // threads of the reduction blocks
 
 // One 1D transform length with its mixed-radix factorisation and its
 // forward twiddles tw[t] = exp(-2 pi i t / n), t < n, in FP64 and FP32.
+// mag_nr/mag_ns: ceil(2^32 / d) for the per-pass divisors d = n/R and
+// d = (product of the earlier radices), so that w / d = umulhi(w, mag) for
+// every index that occurs (w < 2^16, d <= 320).
 struct FftAxis {
   int n;
   int nf;
   int fac[kMaxFactors];
+  unsigned mag_nr[kMaxFactors];
+  unsigned mag_ns[kMaxFactors];
   const double2* tw;
   const float2* twf;
 };
