@@ -52,6 +52,22 @@ const char* kFamName[F_COUNT] = {"pc_predict", "pc_correct", "rk_stage",        
                                  "fft_x_r2c",  "fft_y",      "fft_z_conv",      "fft_x_c2r",
                                  "fft_x_c2r_pot4", "force",  "impurity_scalar", "alpha_s_pointwise"};
 
+// history roles a captured step graph was recorded with
+struct GraphKey {
+  const void* p[7];
+  int cur32;
+  bool operator==(const GraphKey& o) const {
+    for (int i = 0; i < 7; ++i)
+      if (p[i] != o.p[i]) return false;
+    return cur32 == o.cur32;
+  }
+};
+struct GraphEntry {
+  GraphKey key;
+  cudaGraphExec_t exec;
+  long long nlaunch;
+};
+
 }  // namespace
 
 struct he4g_run {
@@ -103,6 +119,8 @@ struct he4g_run {
   long long ring_read = 0;
 
   long long launches = 0;
+  bool use_graphs = false;
+  std::vector<GraphEntry> graphs;
   // timing
   bool timing = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -530,6 +548,32 @@ void steprk_dev(he4g_run* r, double dt) {
   }
 }
 
+// History roles of the predictor-corrector step. After the predictor the
+// old[2] slot holds the modified prediction and psi_n becomes psiold(ioldp(3));
+// h[0] = f_n, h[1] = f_{n-1}. After the corrector psi is the new state and the
+// slots rotate like ioldp (steppc.f90:69-71,139-142). The FP32 copy of psi
+// flips once per kernel that writes a new psi.
+double2* roles_after_predict(he4g_run* r) {
+  double2* psit = r->old[2];
+  r->old[2] = r->psi;
+  std::swap(r->h[0], r->h[1]);
+  if (mixed(r)) r->cur32 = 1 - r->cur32;
+  return psit;
+}
+void roles_after_correct(he4g_run* r, double2* psit) {
+  r->psi = r->scratch;
+  r->scratch = psit;
+  double2* n0 = r->old[2];  // psi_n
+  double2* n1 = r->old[0];  // psi_{n-1}
+  double2* n2 = r->old[1];  // psi_{n-2}
+  r->old[0] = n0;
+  r->old[1] = n1;
+  r->old[2] = n2;
+  if (mixed(r)) r->cur32 = 1 - r->cur32;
+}
+// the role change of one predictor-corrector step, without launching it
+void advance_pc_roles(he4g_run* r) { roles_after_correct(r, roles_after_predict(r)); }
+
 // steppc (steppc.f90:1-178)
 void steppc_dev(he4g_run* r, double dt) {
   const double c112 = 112.0 / 121.0, c9 = 9.0 / 121.0, c4o3 = 4.0 / 3.0;
@@ -541,7 +585,6 @@ void steppc_dev(he4g_run* r, double dt) {
                            static_cast<const float2*>(r->h[0]), static_cast<float2*>(r->h[1]), r->pc,
                            static_cast<const float*>(r->pot4), static_cast<const float*>(r->uimp), r->timec,
                            static_cast<float*>(r->den), c4o3 * dt, c112, r->s);
-      r->cur32 = 1 - r->cur32;
     } else {
       launch_pc_predict(r->g, r->st, r->fn, r->psi, r->old[2], static_cast<double2*>(r->h[0]),
                         static_cast<double2*>(r->h[1]), r->pc, static_cast<const double*>(r->pot4),
@@ -549,10 +592,7 @@ void steppc_dev(he4g_run* r, double dt) {
                         r->s);
     }
   }
-  // old[2] now holds the modified prediction; psi_n becomes psiold(ioldp(3))
-  double2* psit = r->old[2];
-  r->old[2] = r->psi;
-  std::swap(r->h[0], r->h[1]);  // h[0] = f_n, h[1] = f_{n-1}
+  double2* psit = roles_after_predict(r);
   {
     Tick t(r, F_SCALAR);
     launch_imp_pc_predict(r->imp, c4o3 * dt, c112, r->s);
@@ -568,7 +608,6 @@ void steppc_dev(he4g_run* r, double dt) {
                            static_cast<const float*>(r->pot4), static_cast<const float*>(r->uimp), r->timec,
                            r->scratch, r->psi32[1 - r->cur32], static_cast<float*>(r->den), r->partials, 3.0 * dt, c9,
                            &r->imp->health, r->s);
-      r->cur32 = 1 - r->cur32;
     } else {
       launch_pc_correct(r->g, r->st, r->fn, psit, r->old[2], r->old[1], static_cast<const double2*>(r->h[0]),
                         static_cast<const double2*>(r->h[1]), r->pc, static_cast<const double*>(r->pot4),
@@ -576,14 +615,7 @@ void steppc_dev(he4g_run* r, double dt) {
                         r->partials, 3.0 * dt, c9, &r->imp->health, r->s);
     }
   }
-  r->psi = r->scratch;
-  r->scratch = psit;
-  double2* n0 = r->old[2];  // psi_n
-  double2* n1 = r->old[0];  // psi_{n-1}
-  double2* n2 = r->old[1];  // psi_{n-2}
-  r->old[0] = n0;
-  r->old[1] = n1;
-  r->old[2] = n2;
+  roles_after_correct(r, psit);
   {
     Tick t(r, F_SCALAR);
     launch_imp_pc_correct(r->imp, r->partials, r->pblocks, dt, c9, static_cast<double>(r->g.n), r->s);
@@ -604,20 +636,85 @@ int sync_err(he4g_run* r, const char* where) {
   return HE4G_OK;
 }
 
+// the launches of one predictor-corrector step and the trailing evaluation
+void pc_step_launches(he4g_run* r) {
+  steppc_dev(r, r->cfg.deltat);
+  evaluate_dev(r);
+  Tick t(r, F_SCALAR);
+  launch_imp_record(r->imp, r->ring, r->s);
+}
+
+GraphKey current_key(const he4g_run* r) {
+  GraphKey k{};
+  k.p[0] = r->psi;
+  k.p[1] = r->scratch;
+  k.p[2] = r->old[0];
+  k.p[3] = r->old[1];
+  k.p[4] = r->old[2];
+  k.p[5] = r->h[0];
+  k.p[6] = r->h[1];
+  k.cur32 = r->cur32;
+  return k;
+}
+
+// One predictor-corrector step from a CUDA graph of its launches. The graph
+// for the current history roles is captured on first use (the roles repeat
+// every 10 steps) and replayed afterwards. Returns false when capture failed;
+// the roles are then unchanged and the caller launches the step directly.
+bool pc_step_graph(he4g_run* r) {
+  const GraphKey k = current_key(r);
+  for (auto& e : r->graphs) {
+    if (e.key == k) {
+      if (cudaGraphLaunch(e.exec, r->s) != cudaSuccess) return false;
+      advance_pc_roles(r);
+      r->launches += e.nlaunch;
+      return true;
+    }
+  }
+  const long long l0 = r->launches;
+  if (cudaStreamBeginCapture(r->s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+  pc_step_launches(r);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(r->s, &graph);
+  cudaGraphExec_t exec = nullptr;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess || cudaGraphLaunch(exec, r->s) != cudaSuccess) {
+    cudaGetLastError();
+    if (exec) cudaGraphExecDestroy(exec);
+    // capture recorded the launches without running them: undo the role change
+    r->psi = static_cast<double2*>(const_cast<void*>(k.p[0]));
+    r->scratch = static_cast<double2*>(const_cast<void*>(k.p[1]));
+    for (int i = 0; i < 3; ++i) r->old[i] = static_cast<double2*>(const_cast<void*>(k.p[2 + i]));
+    r->h[0] = const_cast<void*>(k.p[5]);
+    r->h[1] = const_cast<void*>(k.p[6]);
+    r->cur32 = k.cur32;
+    r->launches = l0;
+    r->use_graphs = false;
+    return false;
+  }
+  r->graphs.push_back({k, exec, r->launches - l0});
+  return true;
+}
+
+int one_step(he4g_run* r) {
+  const int iteraux = r->iter + 1;
+  if (iteraux <= 3 || r->cfg.lrk) {
+    steprk_dev(r, r->cfg.deltat);
+    evaluate_dev(r);
+    Tick t(r, F_SCALAR);
+    launch_imp_record(r->imp, r->ring, r->s);
+  } else if (!(r->use_graphs && !r->timing && pc_step_graph(r))) {
+    pc_step_launches(r);
+  }
+  r->iter += 1;
+  return HE4G_OK;
+}
+
 int step_impl(he4g_run* r, int nsteps, cudaEvent_t stop) {
   if (nsteps < 0) return fail(r, HE4G_EINVAL, "nsteps < 0");
   for (int s = 0; s < nsteps; ++s) {
-    const int iteraux = r->iter + 1;
-    if (iteraux <= 3 || r->cfg.lrk)
-      steprk_dev(r, r->cfg.deltat);
-    else
-      steppc_dev(r, r->cfg.deltat);
-    evaluate_dev(r);
-    r->iter += 1;
-    {
-      Tick t(r, F_SCALAR);
-      launch_imp_record(r->imp, r->ring, r->iter, r->s);
-    }
+    one_step(r);
     if (r->timing && (s % 16) == 15) collect_timing(r);
   }
   if (stop) cudaEventRecord(stop, r->s);
@@ -632,6 +729,47 @@ int step_impl(he4g_run* r, int nsteps, cudaEvent_t stop) {
 extern "C" {
 
 const char* he4g_last_error(const he4g_run* r) { return r ? r->err.c_str() : "null run"; }
+
+int he4g_footprint(const he4g_config* c, uint64_t* bytes) {
+  if (!c || !bytes || c->nx <= 0 || c->ny <= 0 || c->nz <= 0) return HE4G_EINVAL;
+  const uint64_t n = (uint64_t)c->nx * c->ny * c->nz;
+  const uint64_t nh = (uint64_t)(c->nx / 2 + 1) * c->ny * c->nz;
+  const bool mp = c->precision == HE4G_PREC_MIXED;
+  const bool otc = c->core == HE4G_CORE_OTC && !c->lsolid;
+  const uint64_t rs = mp ? 4 : 8;
+  uint64_t b = 0, nalloc = 0;
+  auto add = [&](uint64_t x, uint64_t count = 1) {
+    b += x * count;
+    nalloc += count;
+  };
+  add(16 * n, 7);                                   // psi, scratch, psiold x3, q, pc
+  add(2 * rs * n, 2);                               // hpsiold x2
+  add(rs * n, 5);                                   // den, pot4, dencg, delj4, uimp
+  add(4 * n);                                       // timec
+  add(2 * rs * nh, 2);                              // spectra
+  add(rs * nh, 2);                                  // form factors
+  add(rs * (uint64_t)c->npot);                      // radial table
+  add(8 * (uint64_t)(c->nx + c->ny + c->nz), 3);    // grids
+  add(rs * n, 3);                                   // density gradient
+  if (mp) {
+    add(8 * n, 2);                                  // FP32 copies of psi
+    add(4 * (uint64_t)(c->nx + c->ny + c->nz), 3);  // FP32 grids
+  }
+  if (otc) {
+    add(2 * rs * nh);
+    add(rs * nh);
+    add(rs * n, 12);
+  }
+  const uint64_t pblocks = (uint64_t)((c->nx + 63) / 64) * ((c->ny + 3) / 4) * c->nz;
+  add(pblocks * 12 * 8);
+  add(64 * 8);
+  add(sizeof(ImpState));
+  add((uint64_t)kRingRows * kRingCols * 8);
+  add(24 * (uint64_t)(c->nx / 2 + c->ny + c->nz + c->nx / 2), 4);  // twiddle tables
+  // allocation granularity (2 MiB pages) bounds the rounding of each buffer
+  *bytes = b + nalloc * (2ull << 20);
+  return HE4G_OK;
+}
 
 int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk, const double* kalfs,
                 const double* potion, he4g_run** out) {
@@ -827,6 +965,7 @@ void he4g_destroy(he4g_run* r) {
     cudaEventDestroy(p.second.second);
   }
   for (auto e : r->pool) cudaEventDestroy(e);
+  for (auto& g : r->graphs) cudaGraphExecDestroy(g.exec);
   for (void* p : r->allocs) cudaFree(p);
   if (r->s) cudaStreamDestroy(r->s);
   delete r;
@@ -946,6 +1085,31 @@ int he4g_step_timed(he4g_run* r, int nsteps, double* device_ms) {
   cudaEventDestroy(b);
   if (device_ms) *device_ms = ms;
   return rc;
+}
+
+int he4g_enable_graphs(he4g_run* r, int on) {
+  if (!r) return HE4G_EINVAL;
+  r->use_graphs = on != 0;
+  return HE4G_OK;
+}
+
+int he4g_step_many(he4g_run** runs, int n, int nsteps) {
+  if (!runs || n < 0 || nsteps < 0) return HE4G_EINVAL;
+  for (int i = 0; i < n; ++i) {
+    int rc = check_ready(runs[i]);
+    if (rc) return rc;
+  }
+  // step by step, run by run: each run's launches go to its own stream, so
+  // the kernels of different runs overlap on the device
+  for (int s = 0; s < nsteps; ++s)
+    for (int i = 0; i < n; ++i) one_step(runs[i]);
+  int first = HE4G_OK;
+  for (int i = 0; i < n; ++i) {
+    int rc = sync_err(runs[i], "step_many");
+    if (!rc) rc = health_check(runs[i]);
+    if (rc && first == HE4G_OK) first = rc;
+  }
+  return first;
 }
 
 int he4g_steps_taken(const he4g_run* r) { return r ? r->iter : -1; }

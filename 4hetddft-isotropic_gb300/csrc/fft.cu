@@ -19,6 +19,9 @@
 // c2r convention (n*x for the DFT of x); the z pass folds the remaining 1/2
 // and the 1/(nx*ny*nz) of fft.f90's renor into its product.
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "he4g_internal.cuh"
 
@@ -485,9 +488,22 @@ int x_lines_per_block(int m) {
   return lpb;
 }
 
+// Raises a kernel's dynamic shared-memory limit once per (kernel, device) to
+// the largest size requested so far, so that no attribute call happens
+// while a step is being captured into a graph.
 template <typename K>
 void set_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (bytes <= 48 * 1024) return;
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = done[{reinterpret_cast<const void*>(kernel), dev}];
+  if (bytes > cur) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cur = bytes;
+  }
 }
 
 template <typename R>

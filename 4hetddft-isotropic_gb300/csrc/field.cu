@@ -535,11 +535,14 @@ __global__ void __launch_bounds__(kFinalThreads) k_imp_force(ImpState* s, const 
   }
 }
 
-__global__ void k_imp_record(ImpState* s, double* ring, long long step) {
+// one trajectory row per step; the step number is the count of rows written
+// since set_state, kept on the device so that a captured step graph records
+// the right number on every replay
+__global__ void k_imp_record(ImpState* s, double* ring) {
   if (threadIdx.x != 0) return;
   const long long row = s->ring_head % kRingRows;
   double* r = ring + row * kRingCols;
-  r[0] = (double)step;
+  r[0] = (double)(s->ring_head + 1);
   for (int a = 0; a < 3; ++a) {
     r[1 + a] = s->rimp[a];
     r[4 + a] = s->vimp[a];
@@ -674,8 +677,8 @@ void launch_imp_force(ImpState* imp, const double* partials, int nblocks, double
                       int store_accel, cudaStream_t s) {
   k_imp_force<<<1, kFinalThreads, 0, s>>>(imp, partials, nblocks, dxyz, mass, store_accel);
 }
-void launch_imp_record(ImpState* imp, double* ring, long long step, cudaStream_t s) {
-  k_imp_record<<<1, 32, 0, s>>>(imp, ring, step);
+void launch_imp_record(ImpState* imp, double* ring, cudaStream_t s) {
+  k_imp_record<<<1, 32, 0, s>>>(imp, ring);
 }
 
 }  // namespace he4g

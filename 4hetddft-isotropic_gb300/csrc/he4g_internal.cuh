@@ -163,7 +163,7 @@ void launch_imp_pc_correct(ImpState* imp, const double* err_partials, int nblock
                            double c9, double nxyz, cudaStream_t s);
 void launch_imp_force(ImpState* imp, const double* partials, int nblocks, double dxyz, double mass,
                       int store_accel, cudaStream_t s);
-void launch_imp_record(ImpState* imp, double* ring, long long step, cudaStream_t s);
+void launch_imp_record(ImpState* imp, double* ring, cudaStream_t s);
 
 // ------------------------- mixed-precision field kernels (fieldmp.cu)
 void launch_pc_predict_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,

@@ -13,7 +13,7 @@ import numpy as np
 from . import abi
 from .abi import CORE_OT, CORE_OTC, Config  # noqa: F401
 from .initial import (PS_TO_K, KELVIN_PER_PS, woods_saxon_psi, collision_case,  # noqa: F401
-                      config_for_case)
+                      config_for_case, make_meta, state_for, batch_cases, serve_stream)
 
 
 class He4gError(RuntimeError):
@@ -34,6 +34,16 @@ def default_config(nx, ny, nz, xmax, ymax=None, zmax=None, **overrides):
             raise KeyError(k)
         setattr(cfg, k, v)
     return cfg
+
+
+def footprint(cfg):
+    """Device bytes a run of this configuration allocates (he4g_footprint)."""
+    lib = abi.load()
+    b = C.c_uint64()
+    rc = lib.he4g_footprint(C.byref(cfg), C.byref(b))
+    if rc:
+        raise He4gError(rc, "footprint")
+    return int(b.value)
 
 
 def build_tables(cfg, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463, with_kalfs=None):
@@ -129,6 +139,21 @@ class Run:
     @property
     def launch_count(self):
         return int(self.lib.he4g_launch_count(self.h))
+
+    def enable_graphs(self, on=True):
+        self._ck(self.lib.he4g_enable_graphs(self.h, 1 if on else 0))
+
+
+def step_many(runs, nsteps):
+    """he4g_step_many: advance several runs together (their kernels overlap)."""
+    if not runs:
+        return
+    lib = runs[0].lib
+    arr = (C.c_void_p * len(runs))(*[r.h.value if isinstance(r.h, C.c_void_p) else r.h for r in runs])
+    rc = lib.he4g_step_many(arr, len(runs), nsteps)
+    if rc:
+        msgs = [r.lib.he4g_last_error(r.h) for r in runs]
+        raise He4gError(rc, "; ".join(m.decode() for m in msgs if m))
 
     def energy(self):
         en = abi.Energies()

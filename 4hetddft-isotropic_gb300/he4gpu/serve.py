@@ -1,0 +1,193 @@
+"""Continuous-batching request loop for collision jobs.
+
+Jobs arrive as a seeded Poisson stream. The loop admits an arrived job when
+its device footprint (he4g_footprint) fits the HBM budget and a slot is free.
+An admitted job's psi and history stay resident until it completes. All
+resident jobs advance together, a chunk of steps at a time (he4g_step_many:
+one stream per job, predictor-corrector steps replayed from CUDA graphs), so
+that jobs that arrive while others run share the device. A finished job is
+evicted, which frees its memory for the next arrival.
+
+The report gives jobs/h, p50/p99 per-step latency (a resident job's share of
+a chunk: chunk wall time / steps in the chunk) and p50/p99 time to completion
+(arrival to last step). It also gives the same stream served one job at a
+time in plain FP64: a FIFO single server whose per-step times are measured
+on this GPU for each grid size.
+
+  python -m he4gpu.serve --jobs 200 --step-scale 0.1
+"""
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+
+from . import Run, config_for_case, default_config, footprint, serve_stream, state_for, step_many
+
+MIXED = 1
+FP64 = 0
+
+
+def make_run(meta, precision, graphs=True):
+    kw, tk = config_for_case(meta)
+    cfg = default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], meta["ymax"], meta["zmax"],
+                         precision=precision, **kw)
+    run = Run(cfg, selec=tk["selec"], r_cutoff=tk["r_cutoff"], umax=tk["umax"])
+    if graphs:
+        run.enable_graphs(True)
+    return run, cfg
+
+
+def job_config(meta, precision):
+    kw, _ = config_for_case(meta)
+    return default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], meta["ymax"], meta["zmax"],
+                          precision=precision, **kw)
+
+
+def pct(xs, q):
+    return float(np.percentile(np.asarray(xs, dtype=float), q)) if xs else None
+
+
+def serve(stream, hbm_budget, max_active=64, chunk=16, precision=MIXED, keep_results=(0,)):
+    """Runs the request loop over `stream` [(arrival_s, meta)] in wall-clock
+    time; returns (report, results of the jobs listed in keep_results)."""
+    pending = list(enumerate(stream))
+    active = []  # dicts: id, run, left, arrival, admitted, bytes, points
+    step_lat = []
+    done = []
+    kept = {}
+    used = 0
+    t0 = time.perf_counter()
+    grid_updates = 0
+    while pending or active:
+        now = time.perf_counter() - t0
+        # admit arrived jobs in arrival order while memory and slots allow
+        while pending and pending[0][1][0] <= now and len(active) < max_active:
+            jid, (arr, meta) = pending[0]
+            need = footprint(job_config(meta, precision))
+            if used + need > hbm_budget and active:
+                break
+            pending.pop(0)
+            run, cfg = make_run(meta, precision)
+            psi, r, v = state_for(meta)
+            run.set_state(psi, r, v)
+            used += need
+            active.append({"id": jid, "run": run, "left": meta["steps"], "arrival": arr,
+                           "admitted": time.perf_counter() - t0, "bytes": need,
+                           "points": cfg.nx * cfg.ny * cfg.nz, "meta": meta})
+        if not active:
+            # idle until the next arrival
+            wait = pending[0][1][0] - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(min(wait, 0.05))
+            continue
+        k = min(chunk, min(a["left"] for a in active))
+        ts = time.perf_counter()
+        step_many([a["run"] for a in active], k)
+        dt = time.perf_counter() - ts
+        for a in active:
+            a["left"] -= k
+            step_lat.extend([dt / k] * k)
+            grid_updates += a["points"] * k
+        finished = [a for a in active if a["left"] == 0]
+        active = [a for a in active if a["left"] > 0]
+        tnow = time.perf_counter() - t0
+        for a in finished:
+            if a["id"] in keep_results:
+                rr, vv, _ = a["run"].impurity()
+                kept[a["id"]] = {"psi": a["run"].psi, "rimp": rr, "vimp": vv, "etot": a["run"].energy()["etot"]}
+            a["run"].close()
+            used -= a["bytes"]
+            done.append({"id": a["id"], "arrival": a["arrival"], "finish": tnow, "ttc": tnow - a["arrival"],
+                         "queue": a["admitted"] - a["arrival"], "steps": a["meta"]["steps"],
+                         "grid": a["meta"]["nx"]})
+    makespan = time.perf_counter() - t0
+    ttc = [d["ttc"] for d in done]
+    rep = {
+        "jobs": len(done),
+        "makespan_s": makespan,
+        "jobs_per_h": len(done) / makespan * 3600.0,
+        "step_latency_ms_p50": 1e3 * pct(step_lat, 50),
+        "step_latency_ms_p99": 1e3 * pct(step_lat, 99),
+        "ttc_s_p50": pct(ttc, 50),
+        "ttc_s_p99": pct(ttc, 99),
+        "grid_point_updates_per_s": grid_updates / makespan,
+        "precision": "mixed" if precision == MIXED else "fp64",
+    }
+    return rep, kept
+
+
+def fp64_step_seconds(grids, steps=6):
+    """Measured FP64 step time per grid size (one run alone, direct launches)."""
+    out = {}
+    from .initial import make_meta
+    for g in grids:
+        meta = make_meta(g, 0.42, min(5000.0, ((g * 0.42 / 2 - 8) / 2.22) ** 3 * 0.6), "Xe", 0.3, 3.0)
+        run, _ = make_run(meta, FP64, graphs=False)
+        psi, r, v = state_for(meta)
+        run.set_state(psi, r, v)
+        run.step(4)
+        ms = run.step_timed(steps)
+        out[g] = ms / 1e3 / steps
+        run.close()
+    return out
+
+
+def one_at_a_time(stream, step_s):
+    """FIFO single server in plain FP64 over the same arrivals."""
+    t = 0.0
+    ttc = []
+    for arr, meta in stream:
+        start = max(t, arr)
+        t = start + meta["steps"] * step_s[meta["nx"]]
+        ttc.append(t - arr)
+    return {"jobs": len(stream), "makespan_s": t, "jobs_per_h": len(stream) / t * 3600.0,
+            "step_latency_ms_by_grid": {str(g): 1e3 * s for g, s in step_s.items()},
+            "ttc_s_p50": pct(ttc, 50), "ttc_s_p99": pct(ttc, 99), "precision": "fp64"}
+
+
+def alone_vs_mix(stream, kept, precision=MIXED):
+    """Re-runs the kept jobs alone and compares their final state bit for bit."""
+    out = {}
+    for jid, res in kept.items():
+        meta = stream[jid][1]
+        run, _ = make_run(meta, precision)
+        psi, r, v = state_for(meta)
+        run.set_state(psi, r, v)
+        run.step(meta["steps"])
+        same = bool(np.array_equal(run.psi, res["psi"]) and np.array_equal(run.impurity()[0], res["rimp"]))
+        out[str(jid)] = {"identical": same, "etot_alone": run.energy()["etot"], "etot_mix": res["etot"]}
+        run.close()
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--jobs", type=int, default=200)
+    ap.add_argument("--rate", type=float, default=4.0, help="arrivals per second")
+    ap.add_argument("--step-scale", type=float, default=1.0, help="scales each job's 500-5000 steps")
+    ap.add_argument("--chunk", type=int, default=16)
+    ap.add_argument("--max-active", type=int, default=64)
+    ap.add_argument("--hbm-gb", type=float, default=0.0, help="budget; 0 = 90%% of the free memory")
+    ap.add_argument("--seed", type=int, default=7)
+    args = ap.parse_args(argv)
+    stream = serve_stream(args.jobs, seed=args.seed, rate_per_s=args.rate, step_scale=args.step_scale)
+    if args.hbm_gb > 0:
+        budget = int(args.hbm_gb * 1e9)
+    else:
+        import torch
+        free, _ = torch.cuda.mem_get_info()
+        budget = int(0.9 * free)
+    rep, kept = serve(stream, budget, max_active=args.max_active, chunk=args.chunk, keep_results=(0, 1))
+    base = one_at_a_time(stream, fp64_step_seconds(sorted({m["nx"] for _, m in stream})))
+    check = alone_vs_mix(stream, kept)
+    out = {"serve_mixed": rep, "one_at_a_time_fp64": base, "speedup_jobs_per_h": rep["jobs_per_h"] / base["jobs_per_h"],
+           "alone_vs_mix": check, "stream": {"jobs": args.jobs, "rate_per_s": args.rate, "step_scale": args.step_scale,
+                                             "seed": args.seed, "hbm_budget_gb": budget / 1e9}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

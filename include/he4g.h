@@ -118,6 +118,10 @@ void he4g_default_config(he4g_config* cfg, int nx, int ny, int nz, double xmax, 
 int he4g_build_tables(const he4g_config* cfg, const char* selec, double r_cutoff, double umax,
                       double* fvlj4, double* wcgk, double* kalfs, double* potion);
 
+/* Device bytes he4g_create allocates for cfg (admission by HBM footprint);
+ * host arithmetic only. */
+int he4g_footprint(const he4g_config* cfg, uint64_t* bytes);
+
 /* Allocates the run on the current CUDA device and uploads the tables
  * (replaces dimen.f90, fftini fft.f90:5-76 and the table set-up calls of
  * DFT4He3d.f90:518-596). kalfs is required for core OTC, else may be NULL. */
@@ -201,6 +205,18 @@ int he4g_forceimp_noalloc(const double* den, const double* uimp, int nx, int ny,
 /* he4g_step with CUDA events recorded on the run's stream before its first
  * and after its last launch; *device_ms receives the elapsed device time. */
 int he4g_step_timed(he4g_run* run, int nsteps, double* device_ms);
+
+/* on = 1: each predictor-corrector step (with the trailing re-evaluation) is
+ * captured once per history-slot arrangement (10 arrangements recur) as a
+ * CUDA graph and replayed, removing per-kernel launch cost. Ignored while
+ * kernel timing is on. */
+int he4g_enable_graphs(he4g_run* run, int on);
+
+/* Advances n runs by nsteps each. Their launches go to their own streams,
+ * interleaved step by step, so kernels of different runs (e.g. collisions on
+ * uneven grids) overlap on the device; one host synchronisation at the end.
+ * Returns the first error of any run. */
+int he4g_step_many(he4g_run** runs, int n, int nsteps);
 
 /* Kernel launches issued by this run since it was created. */
 long long he4g_launch_count(const he4g_run* run);
