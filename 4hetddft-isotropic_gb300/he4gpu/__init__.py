@@ -143,18 +143,6 @@ class Run:
     def enable_graphs(self, on=True):
         self._ck(self.lib.he4g_enable_graphs(self.h, 1 if on else 0))
 
-
-def step_many(runs, nsteps):
-    """he4g_step_many: advance several runs together (their kernels overlap)."""
-    if not runs:
-        return
-    lib = runs[0].lib
-    arr = (C.c_void_p * len(runs))(*[r.h.value if isinstance(r.h, C.c_void_p) else r.h for r in runs])
-    rc = lib.he4g_step_many(arr, len(runs), nsteps)
-    if rc:
-        msgs = [r.lib.he4g_last_error(r.h) for r in runs]
-        raise He4gError(rc, "; ".join(m.decode() for m in msgs if m))
-
     def energy(self):
         en = abi.Energies()
         self._ck(self.lib.he4g_energy(self.h, C.byref(en)))
@@ -223,3 +211,15 @@ def step_many(runs, nsteps):
         if k < 0:
             self._ck(k)
         return {names[i].decode(): (float(ms[i]), int(launches[i])) for i in range(k)}
+
+
+def step_many(runs, nsteps):
+    """he4g_step_many: advance several runs together (their kernels overlap)."""
+    if not runs:
+        return
+    lib = runs[0].lib
+    arr = (C.c_void_p * len(runs))(*[r.h.value if isinstance(r.h, C.c_void_p) else r.h for r in runs])
+    rc = lib.he4g_step_many(arr, len(runs), nsteps)
+    if rc:
+        msgs = [r.lib.he4g_last_error(r.h) for r in runs]
+        raise He4gError(rc, "; ".join(m.decode() for m in msgs if m))
