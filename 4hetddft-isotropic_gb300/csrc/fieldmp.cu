@@ -217,9 +217,12 @@ __global__ void __launch_bounds__(256) k_rk_stage_mp(Grid g, StencilF st, Functi
   psi_out[t.p] = pn;
   const float2 p32 = make_float2((float)pn.x, (float)pn.y);
   psi32_out[t.p] = p32;
-  const float d = fmaf(p32.x, p32.x, p32.y * p32.y);
-  den[t.p] = d;
-  const int h = den_health(d);
+  den[t.p] = fmaf(p32.x, p32.x, p32.y * p32.y);
+  // the steprk.f90:89-92 check on |psi|^2 in FP64: far droplet tails reach
+  // |psi|^2 ~ 1e-50, which is positive in FP64 but underflows the FP32 den
+  const double d64 = fma(pn.x, pn.x, pn.y * pn.y);
+  const long long b = __double_as_longlong(d64);
+  const int h = (b > 0 && b < 0x7FF0000000000000LL) ? 0 : (((b & 0x7FF0000000000000LL) == 0x7FF0000000000000LL) ? 3 : 1);
   if (h) atomicOr(health, h);
 }
 
