@@ -946,6 +946,8 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
     r->plan.twx = d;
     r->plan.twxf = df;
   }
+  r->plan.tiles = fft_default_tiles(r->prec, r->plan);
+  fft_prepare(r->prec, r->plan);
   cudaError_t e = cudaStreamSynchronize(r->s);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -1090,6 +1092,122 @@ int he4g_step_timed(he4g_run* r, int nsteps, double* device_ms) {
 int he4g_enable_graphs(he4g_run* r, int on) {
   if (!r) return HE4G_EINVAL;
   r->use_graphs = on != 0;
+  return HE4G_OK;
+}
+
+extern "C++" {
+namespace {
+constexpr int kMaxLpb = 64;
+constexpr int kMaxLtx = 5;
+
+bool tiles_fit(const he4g_run* r, const FftTiles& t) {
+  if (t.lpb_r2c < 1 || t.lpb_r2c > kMaxLpb || t.lpb_c2r < 1 || t.lpb_c2r > kMaxLpb) return false;
+  if (t.ltx_y < 0 || t.ltx_y > kMaxLtx || t.ltx_z < 0 || t.ltx_z > kMaxLtx) return false;
+  return fft_smem_bytes(r->prec, PASS_R2C, r->plan, t.lpb_r2c) && fft_smem_bytes(r->prec, PASS_C2R, r->plan, t.lpb_c2r) &&
+         fft_smem_bytes(r->prec, PASS_Y, r->plan, t.ltx_y) && fft_smem_bytes(r->prec, PASS_Z, r->plan, t.ltx_z);
+}
+
+// Captured graphs hold the launch shapes they were captured with.
+void apply_tiles(he4g_run* r, const FftTiles& t) {
+  r->plan.tiles = t;
+  fft_prepare(r->prec, r->plan);
+  for (auto& e : r->graphs) cudaGraphExecDestroy(e.exec);
+  r->graphs.clear();
+}
+
+// device time per launch of fn: one untimed launch, then `reps` timed ones
+template <typename F>
+float per_launch_ms(he4g_run* r, cudaEvent_t a, cudaEvent_t b, int reps, F fn) {
+  fn();
+  cudaEventRecord(a, r->s);
+  for (int i = 0; i < reps; ++i) fn();
+  cudaEventRecord(b, r->s);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms / reps;
+}
+
+void tiles_to(const FftTiles& t, int out[4]) {
+  out[0] = t.lpb_r2c;
+  out[1] = t.lpb_c2r;
+  out[2] = t.ltx_y;
+  out[3] = t.ltx_z;
+}
+}  // namespace
+}  // extern "C++"
+
+int he4g_autotune(he4g_run* r, int reps, int tiles[4]) {
+  if (!r || reps < 0) return HE4G_EINVAL;
+  if (reps == 0) reps = 5;
+  cudaError_t e0 = cudaStreamSynchronize(r->s);
+  if (e0 != cudaSuccess) return fail(r, HE4G_ECUDA, cudaGetErrorString(e0));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const Grid& g = r->g;
+  const int prec = r->prec;
+  FftTiles best = r->plan.tiles;
+  FftTiles trial = best;
+  // Each pass runs on the run's scratch spectra with the run's own geometry:
+  // r2c of the density into spec0, y on spec0, the z convolution of spec0
+  // with the Lennard-Jones table into spec1, c2r of spec0 into spec1. Every
+  // line is transformed by the same arithmetic whatever the tile, so the
+  // choice changes timing only.
+  void* sp[1] = {r->spec0};
+  void* zo[1] = {r->spec1};
+  const void* zf[1] = {r->fvlj4};
+  const void* ci[1] = {r->spec0};
+  void* co[1] = {r->spec1};
+  auto sweep = [&](int pass, int lo, int hi, bool pow2, int FftTiles::*field) {
+    float best_ms = 0.f;
+    int best_tile = best.*field;
+    for (int t = lo; t <= hi; t = pow2 ? t * 2 : t + 1) {
+      if (!fft_smem_bytes(prec, pass, r->plan, t)) continue;
+      trial = best;
+      trial.*field = t;
+      r->plan.tiles = trial;
+      fft_prepare(prec, r->plan);
+      float ms = per_launch_ms(r, a, b, reps, [&] {
+        switch (pass) {
+          case PASS_R2C: fft_x_r2c(g, r->plan, prec, r->den, r->spec0, r->s); break;
+          case PASS_Y: fft_y(g, r->plan, prec, sp, 1, -1, r->s); break;
+          case PASS_Z: fft_z_conv(g, r->plan, prec, r->spec0, zo, zf, 1, 0.5 * g.renor, nullptr, r->s); break;
+          default: fft_x_c2r(g, r->plan, prec, ci, co, 1, r->s); break;
+        }
+      });
+      if (best_ms == 0.f || ms < best_ms) {
+        best_ms = ms;
+        best_tile = t;
+      }
+    }
+    best.*field = best_tile;
+  };
+  sweep(PASS_R2C, 1, kMaxLpb, true, &FftTiles::lpb_r2c);
+  sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y);
+  sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z);
+  sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  apply_tiles(r, best);
+  cudaError_t e = cudaStreamSynchronize(r->s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(r, HE4G_ECUDA, cudaGetErrorString(e));
+  if (tiles) tiles_to(best, tiles);
+  return HE4G_OK;
+}
+
+int he4g_get_tiles(const he4g_run* r, int tiles[4]) {
+  if (!r || !tiles) return HE4G_EINVAL;
+  tiles_to(r->plan.tiles, tiles);
+  return HE4G_OK;
+}
+
+int he4g_set_tiles(he4g_run* r, const int tiles[4]) {
+  if (!r || !tiles) return HE4G_EINVAL;
+  const FftTiles t{tiles[0], tiles[1], tiles[2], tiles[3]};
+  if (!tiles_fit(r, t)) return fail(r, HE4G_EINVAL, "tile shape out of range or over the shared-memory limit");
+  apply_tiles(r, t);
   return HE4G_OK;
 }
 

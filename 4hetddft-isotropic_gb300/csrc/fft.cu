@@ -396,11 +396,11 @@ struct SpecList {
 
 // In-place transform along y of the spectra in `specs` (blockIdx.z picks one).
 template <typename R, int SIGN>
-__global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> specs) {
+__global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> specs, int ltx) {
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
-  constexpr int TX = Cx<R>::kTile;
-  const int n = ax.n;  // ny
+  const int TX = 1 << ltx;  // kx columns of this block
+  const int n = ax.n;       // ny
   const int ld = padded_len<R>(n);
   C2<R>* a = sm;
   C2<R>* b = sm + TX * ld;
@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> 
   const int ncol = min(TX, g.nxh - kx0);
   const long long base = (long long)blockIdx.y * g.ny * g.nxh + kx0;
   for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
-    const int c = w % TX, j = w / TX;
+    const int c = w & (TX - 1), j = w >> ltx;
     if (c < ncol) a[c * ld + pidx<R>(j)] = sp[base + (long long)j * g.nxh + c];
   }
   C2<R>* tws = sm + 2 * TX * ld;
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> 
   __syncthreads();
   C2<R>* r = fft_smem<R, SIGN>(a, b, ncol, ld, ax, tws);
   for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
-    const int c = w % TX, j = w / TX;
+    const int c = w & (TX - 1), j = w >> ltx;
     if (c < ncol) sp[base + (long long)j * g.nxh + c] = r[c * ld + pidx<R>(j)];
   }
 }
@@ -433,11 +433,11 @@ struct FactorList {
 // in the same (kx, ky, z) space that is added to output 0.
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C2<R>* in, FactorList<R> fl,
-                                                     int nout, R scale, const C2<R>* __restrict__ add) {
+                                                     int nout, R scale, const C2<R>* __restrict__ add, int ltx) {
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<R>* sm = reinterpret_cast<C2<R>*>(smraw);
-  constexpr int TX = Cx<R>::kTile;
-  const int n = ax.n;  // nz
+  const int TX = 1 << ltx;  // kx columns of this block
+  const int n = ax.n;       // nz
   const int ld = padded_len<R>(n);
   C2<R>* a = sm;
   C2<R>* b = sm + TX * ld;
@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   const long long plane = (long long)g.ny * g.nxh;
   const long long base = (long long)blockIdx.y * g.nxh + kx0;
   for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
-    const int cc = w % TX, k = w / TX;
+    const int cc = w & (TX - 1), k = w >> ltx;
     if (cc < ncol) a[cc * ld + pidx<R>(k)] = in[base + (long long)k * plane + cc];
   }
   C2<R>* tws = sm + 3 * TX * ld;
@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   for (int o = 0; o < nout; ++o) {
     const R* fac = fl.f[o];
     for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
-      const int cc = w % TX, k = w / TX;
+      const int cc = w & (TX - 1), k = w >> ltx;
       if (cc < ncol) {
         const R f = __ldg(&fac[base + (long long)k * plane + cc]) * scale;
         const C2<R> v = fwd[cc * ld + pidx<R>(k)];
@@ -469,7 +469,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
     C2<R>* r = fft_smem<R, 1>(s1, c, ncol, ld, ax, tws);
     C2<R>* dst = fl.out[o];
     for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
-      const int cc = w % TX, k = w / TX;
+      const int cc = w & (TX - 1), k = w >> ltx;
       if (cc < ncol) {
         const long long e = base + (long long)k * plane + cc;
         C2<R> v = r[cc * ld + pidx<R>(k)];
@@ -479,13 +479,6 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
     }
     __syncthreads();  // fwd stays intact; s1 and c are free again
   }
-}
-
-int x_lines_per_block(int m) {
-  int lpb = 2048 / m;
-  if (lpb < 1) lpb = 1;
-  if (lpb > 32) lpb = 32;
-  return lpb;
 }
 
 // Raises a kernel's dynamic shared-memory limit once per (kernel, device) to
@@ -517,11 +510,24 @@ const float2* twx_of<float>(const FftPlan& p) {
   return p.twxf;
 }
 
+// Shared memory of one block of each pass for a tile (lines per block for the
+// x passes, log2 of the kx columns for y/z); twiddles included.
+template <typename R>
+size_t smem_of(int pass, const FftPlan& p, int tile) {
+  const int m = p.xh.n;
+  switch (pass) {
+    case PASS_R2C: return sizeof(C2<R>) * (2 * (size_t)tile * padded_len<R>(m) + m);
+    case PASS_C2R: return sizeof(C2<R>) * (2 * (size_t)tile * padded_len<R>(m + 1) + m);
+    case PASS_Y: return sizeof(C2<R>) * (2 * ((size_t)1 << tile) * padded_len<R>(p.y.n) + p.y.n);
+    case PASS_Z: return sizeof(C2<R>) * (3 * ((size_t)1 << tile) * padded_len<R>(p.z.n) + p.z.n);
+  }
+  return 0;
+}
+
 template <typename R, int PRO>
 void launch_r2c(const Grid& g, const FftPlan& p, const R* a, const R* b, R c0, R c1, C2<R>* out, cudaStream_t s) {
-  const int m = p.xh.n;
-  const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(C2<R>) * (2 * lpb * padded_len<R>(m) + m);
+  const int lpb = p.tiles.lpb_r2c;
+  const size_t smem = smem_of<R>(PASS_R2C, p, lpb);
   set_smem(k_x_r2c<R, PRO>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb));
@@ -530,41 +536,42 @@ void launch_r2c(const Grid& g, const FftPlan& p, const R* a, const R* b, R c0, R
 
 template <typename R>
 void y_impl(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int sign, cudaStream_t s) {
-  constexpr int TX = Cx<R>::kTile;
+  const int ltx = p.tiles.ltx_y;
+  const int TX = 1 << ltx;
   SpecList<R> sl{};
   for (int i = 0; i < nspec; ++i) sl.p[i] = static_cast<C2<R>*>(specs[i]);
-  const size_t smem = sizeof(C2<R>) * (2 * TX * padded_len<R>(p.y.n) + p.y.n);
+  const size_t smem = smem_of<R>(PASS_Y, p, ltx);
   dim3 grid((g.nxh + TX - 1) / TX, g.nz, nspec);
   if (sign < 0) {
     set_smem(k_y<R, -1>, smem);
-    k_y<R, -1><<<grid, kThreads, smem, s>>>(g, p.y, sl);
+    k_y<R, -1><<<grid, kThreads, smem, s>>>(g, p.y, sl, ltx);
   } else {
     set_smem(k_y<R, 1>, smem);
-    k_y<R, 1><<<grid, kThreads, smem, s>>>(g, p.y, sl);
+    k_y<R, 1><<<grid, kThreads, smem, s>>>(g, p.y, sl, ltx);
   }
 }
 
 template <typename R>
 void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors,
                 int nout, double scale, const void* add, cudaStream_t s) {
-  constexpr int TX = Cx<R>::kTile;
+  const int ltx = p.tiles.ltx_z;
+  const int TX = 1 << ltx;
   FactorList<R> fl{};
   for (int i = 0; i < nout; ++i) {
     fl.f[i] = static_cast<const R*>(factors[i]);
     fl.out[i] = static_cast<C2<R>*>(outs[i]);
   }
-  const size_t smem = sizeof(C2<R>) * (3 * TX * padded_len<R>(p.z.n) + p.z.n);
+  const size_t smem = smem_of<R>(PASS_Z, p, ltx);
   set_smem(k_z_conv<R>, smem);
   dim3 grid((g.nxh + TX - 1) / TX, g.ny);
   k_z_conv<R><<<grid, kThreads, smem, s>>>(g, p.z, static_cast<const C2<R>*>(in), fl, nout, (R)scale,
-                                           static_cast<const C2<R>*>(add));
+                                           static_cast<const C2<R>*>(add), ltx);
 }
 
 template <typename R>
 void c2r_impl(const Grid& g, const FftPlan& p, const void* const* ins, void* const* outs, int nspec, cudaStream_t s) {
-  const int m = p.xh.n;
-  const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(C2<R>) * (2 * lpb * padded_len<R>(m + 1) + m);
+  const int lpb = p.tiles.lpb_c2r;
+  const size_t smem = smem_of<R>(PASS_C2R, p, lpb);
   set_smem(k_x_c2r<R, EPI_STORE>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb), nspec);
@@ -579,9 +586,8 @@ void c2r_impl(const Grid& g, const FftPlan& p, const void* const* ins, void* con
 template <typename R>
 void pot4_impl(const Grid& g, const FftPlan& p, const void* conv, const void* dencg, const void* den,
                const Functional& fn, void* pot4, cudaStream_t s) {
-  const int m = p.xh.n;
-  const int lpb = x_lines_per_block(m);
-  const size_t smem = sizeof(C2<R>) * (2 * lpb * padded_len<R>(m + 1) + m);
+  const int lpb = p.tiles.lpb_c2r;
+  const size_t smem = smem_of<R>(PASS_C2R, p, lpb);
   set_smem(k_x_c2r<R, EPI_POT4>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb), 1);
@@ -646,6 +652,51 @@ void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv,
     pot4_impl<double>(g, p, conv, dencg, den, fn, pot4, s);
   else
     pot4_impl<float>(g, p, conv, dencg, den, fn, pot4, s);
+}
+
+size_t fft_smem_bytes(int prec, int pass, const FftPlan& p, int tile) {
+  const size_t b = prec == HE4G_PREC_FP64 ? smem_of<double>(pass, p, tile) : smem_of<float>(pass, p, tile);
+  return b <= kMaxSmemPerBlock ? b : 0;
+}
+
+namespace {
+template <typename R>
+void prepare_impl(const FftPlan& p) {
+  const size_t r2c = smem_of<R>(PASS_R2C, p, p.tiles.lpb_r2c);
+  const size_t c2r = smem_of<R>(PASS_C2R, p, p.tiles.lpb_c2r);
+  const size_t y = smem_of<R>(PASS_Y, p, p.tiles.ltx_y);
+  set_smem(k_x_r2c<R, PRO_PLAIN>, r2c);
+  set_smem(k_x_r2c<R, PRO_CORR>, r2c);
+  set_smem(k_x_r2c<R, PRO_PROD>, r2c);
+  set_smem(k_y<R, -1>, y);
+  set_smem(k_y<R, 1>, y);
+  set_smem(k_z_conv<R>, smem_of<R>(PASS_Z, p, p.tiles.ltx_z));
+  set_smem(k_x_c2r<R, EPI_STORE>, c2r);
+  set_smem(k_x_c2r<R, EPI_POT4>, c2r);
+}
+}  // namespace
+
+void fft_prepare(int prec, const FftPlan& p) {
+  if (prec == HE4G_PREC_FP64)
+    prepare_impl<double>(p);
+  else
+    prepare_impl<float>(p);
+}
+
+FftTiles fft_default_tiles(int prec, const FftPlan& p) {
+  FftTiles t;
+  // x passes: about 2048 complex elements per block
+  int lpb = 2048 / p.xh.n;
+  lpb = lpb < 1 ? 1 : (lpb > 32 ? 32 : lpb);
+  t.lpb_r2c = t.lpb_c2r = lpb;
+  // y/z passes: 8 kx columns (128-byte rows in FP64, 64-byte in FP32)
+  t.ltx_y = t.ltx_z = 3;
+  // shrink until every pass fits in shared memory
+  while (t.lpb_r2c > 1 && !fft_smem_bytes(prec, PASS_R2C, p, t.lpb_r2c)) t.lpb_r2c >>= 1;
+  while (t.lpb_c2r > 1 && !fft_smem_bytes(prec, PASS_C2R, p, t.lpb_c2r)) t.lpb_c2r >>= 1;
+  while (t.ltx_y > 0 && !fft_smem_bytes(prec, PASS_Y, p, t.ltx_y)) --t.ltx_y;
+  while (t.ltx_z > 0 && !fft_smem_bytes(prec, PASS_Z, p, t.ltx_z)) --t.ltx_z;
+  return t;
 }
 
 }  // namespace he4g

@@ -82,12 +82,31 @@ struct ImpState {
 constexpr int kRingRows = 8192;
 constexpr int kRingCols = 10;
 
+// Tile shapes of the line passes, chosen per run (he4g_autotune):
+// lines per block of the x passes, log2 of the kx columns per y/z block.
+struct FftTiles {
+  int lpb_r2c, lpb_c2r;
+  int ltx_y, ltx_z;
+};
+
 struct FftPlan {
   FftAxis xh;  // packed half-length nx/2 along x
   FftAxis y, z;
   const double2* twx;  // exp(-2 pi i k / nx), k < nx/2 (r2c/c2r packing)
   const float2* twxf;
+  FftTiles tiles;
 };
+
+// opt-in dynamic shared memory per block on sm_103a
+constexpr size_t kMaxSmemPerBlock = 232448;
+
+// shared memory a pass needs with the given tile (0 when it does not fit)
+enum { PASS_R2C = 0, PASS_C2R = 1, PASS_Y = 2, PASS_Z = 3 };
+size_t fft_smem_bytes(int prec, int pass, const FftPlan& p, int tile);
+// tiles used until he4g_autotune picks others
+FftTiles fft_default_tiles(int prec, const FftPlan& p);
+// raises the kernels' shared-memory limits for p.tiles (outside any capture)
+void fft_prepare(int prec, const FftPlan& p);
 
 // ------------------------------------------------- FFT passes (fft.cu)
 // prec: HE4G_PREC_FP64 (double fields, double2 spectra) or HE4G_PREC_MIXED

@@ -143,6 +143,25 @@ class Run:
     def enable_graphs(self, on=True):
         self._ck(self.lib.he4g_enable_graphs(self.h, 1 if on else 0))
 
+    def autotune(self, reps=5):
+        """Time every FFT tile shape on this run's buffers and keep the fastest.
+
+        Returns (lpb_r2c, lpb_c2r, log2 cols y, log2 cols z)."""
+        t = (C.c_int * 4)()
+        self._ck(self.lib.he4g_autotune(self.h, reps, t))
+        return tuple(t)
+
+    @property
+    def tiles(self):
+        t = (C.c_int * 4)()
+        self._ck(self.lib.he4g_get_tiles(self.h, t))
+        return tuple(t)
+
+    @tiles.setter
+    def tiles(self, value):
+        t = (C.c_int * 4)(*[int(v) for v in value])
+        self._ck(self.lib.he4g_set_tiles(self.h, t))
+
     def energy(self):
         en = abi.Energies()
         self._ck(self.lib.he4g_energy(self.h, C.byref(en)))

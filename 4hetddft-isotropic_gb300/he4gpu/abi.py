@@ -103,6 +103,9 @@ SIGNATURES = {
     "he4g_enable_graphs": (C.c_int, [_P, C.c_int]),
     "he4g_footprint": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_uint64)]),
     "he4g_step_many": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int]),
+    "he4g_autotune": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int)]),
+    "he4g_get_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "he4g_set_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "he4g_steps_taken": (C.c_int, [_P]),
     "he4g_kernel_times": (C.c_int, [_P, C.POINTER(C.c_char_p), _D, C.POINTER(C.c_int), C.c_int]),
     "he4g_enable_timing": (C.c_int, [_P, C.c_int]),

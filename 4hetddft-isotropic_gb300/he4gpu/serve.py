@@ -29,11 +29,21 @@ MIXED = 1
 FP64 = 0
 
 
-def make_run(meta, precision, graphs=True):
+# FFT tile shapes tuned once per (grid, precision) and shared by later runs
+_TILES = {}
+
+
+def make_run(meta, precision, graphs=True, tune=True):
     kw, tk = config_for_case(meta)
     cfg = default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], meta["ymax"], meta["zmax"],
                          precision=precision, **kw)
     run = Run(cfg, selec=tk["selec"], r_cutoff=tk["r_cutoff"], umax=tk["umax"])
+    if tune:
+        key = (cfg.nx, cfg.ny, cfg.nz, precision)
+        if key in _TILES:
+            run.tiles = _TILES[key]
+        else:
+            _TILES[key] = run.autotune()
     if graphs:
         run.enable_graphs(True)
     return run, cfg

@@ -159,6 +159,7 @@ def make_run(prec=FP64):
     kw, tk = he4gpu.config_for_case(meta)
     cfg = he4gpu.default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], precision=prec, **kw)
     run = he4gpu.Run(cfg, selec=tk["selec"], r_cutoff=tk["r_cutoff"], umax=tk["umax"])
+    run.autotune()
     return run, cfg, psi, r, v, meta
 
 
@@ -360,7 +361,7 @@ def ours(args):
                        "grid": [cfg.nx, cfg.ny, cfg.nz], "h": meta["h"], "n4": meta["n4"], "impurity": meta["imp"],
                        "v_A_per_ps": meta["v"], "impact_parameter": f"{meta['b_frac']} R",
                        "l2": "inputs larger than L2 (psi 268 MB, history 1.9 GB); no flush",
-                       "parallelism": f"replicas x{ws}"},
+                       "parallelism": f"replicas x{ws}", "fft_tiles": list(run.tiles)},
             "grid_point_updates_per_s": value * cfg.nx * cfg.ny * cfg.nz,
             "hbm_gbs": rf["step_gbs"],
             "roofline": rf,
@@ -410,10 +411,12 @@ def mixed_measure(args, run64, barrier, gpu):
         "rimp_abs_A": float(np.max(np.abs(rmx - r64))),
     }
     ms = res["ms"]
+    tiles = list(run.tiles)
     run.close()
     rf = res["roofline"]
     return {"value": args.steps / (ms * 1e-3), "unit": "steps/s", "ms_per_step": ms / args.steps,
             "dtype": "f32 fields/stencils/FFTs; f64 psi accumulator, reductions, force sum, trajectory",
+            "fft_tiles": tiles,
             "hbm_gbs": rf["step_gbs"], "roofline": rf, "gpu_launches": res["launches"],
             "clocks": res["clocks"], "vs_fp64": dev}
 
