@@ -286,11 +286,15 @@ bool radix_ok(int n) {
 }
 
 // ----------------------------------------------------------------- pieces
+ImpTable imp_table(const he4g_run* r) {
+  return ImpTable{r->xsf, r->ysf, r->zsf, static_cast<const float*>(r->potion), r->cfg.npot,
+                  static_cast<float>(1.0 / r->cfg.delinter)};
+}
+
 void potenimp_dev(he4g_run* r, int sel) {
   Tick t(r, F_POTENIMP);
   if (mixed(r))
-    launch_potenimp_mp(r->g, r->xsf, r->ysf, r->zsf, static_cast<const float*>(r->potion), r->cfg.npot,
-                       static_cast<float>(r->cfg.delinter), r->imp, sel, static_cast<float*>(r->uimp), r->s);
+    launch_potenimp_mp(r->g, imp_table(r), r->imp, sel, static_cast<float*>(r->uimp), r->s);
   else
     launch_potenimp(r->g, r->xs, r->ys, r->zs, static_cast<const double*>(r->potion), r->cfg.npot, r->cfg.delinter,
                     r->imp, sel, static_cast<double*>(r->uimp), r->s);
@@ -466,31 +470,40 @@ void delj4_dev(he4g_run* r) {
   r->delj4_valid = true;
 }
 
-// forceimp (potenimp.f90:24-55); store_accel: aimp = F / m on the device
-void force_dev(he4g_run* r, int store_accel) {
+// forceimp (potenimp.f90:24-55); store_accel: aimp = F / m on the device.
+// The mixed form evaluates uimp inside the force kernel about centre `sel`
+// (potenimp_dev's selector) and stores it when `store_uimp` is set, which
+// replaces a separate potenimp launch; the FP64 form reads the stored uimp.
+void force_dev(he4g_run* r, int store_accel, int sel = 1, bool store_uimp = false) {
   int nb;
   {
     Tick t(r, F_FORCE);
     if (mixed(r)) {
-      launch_force_mp(r->g, r->stf, static_cast<const float*>(r->den), static_cast<const float*>(r->uimp),
-                      r->partials, r->s);
+      launch_force_mp(r->g, r->stf, static_cast<const float*>(r->den), imp_table(r), r->imp, sel,
+                      store_uimp ? static_cast<float*>(r->uimp) : nullptr, r->partials, r->s);
       nb = r->fblocks;
     } else {
       launch_force(r->g, r->st, static_cast<const double*>(r->den), static_cast<const double*>(r->uimp), nullptr,
                    nullptr, nullptr, r->partials, r->s);
-      nb = r->pblocks;
+      nb = r->fblocks;
     }
   }
   Tick t(r, F_SCALAR);
   launch_imp_force(r->imp, r->partials, nb, r->g.dxyz, r->mass, store_accel, r->s);
 }
 
-// potenimp(rimp); poten(); forceimp(rimp, aimp); aimp /= m
-void evaluate_dev(he4g_run* r) {
-  potenimp_dev(r, 0);
-  poten_dev(r);
-  force_dev(r, 1);
+// potenimp(centre sel); poten(); forceimp(rimp, aimp); aimp /= m
+void evaluate_at(he4g_run* r, int sel) {
+  if (mixed(r)) {
+    poten_dev(r);  // does not read uimp
+    force_dev(r, 1, sel, true);
+  } else {
+    potenimp_dev(r, sel);
+    poten_dev(r);
+    force_dev(r, 1);
+  }
 }
+void evaluate_dev(he4g_run* r) { evaluate_at(r, 0); }
 
 int health_check(he4g_run* r) {
   ImpState h;
@@ -597,9 +610,7 @@ void steppc_dev(he4g_run* r, double dt) {
     Tick t(r, F_SCALAR);
     launch_imp_pc_predict(r->imp, c4o3 * dt, c112, r->s);
   }
-  potenimp_dev(r, 1);
-  poten_dev(r);
-  force_dev(r, 1);
+  evaluate_at(r, 1);
   {
     Tick t(r, F_PC_CORRECT);
     if (mp) {
@@ -878,7 +889,7 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
       chk(*p = dalloc_bytes(r, rs * n));
   }
   r->pblocks = pc_blocks(g);
-  r->fblocks = force_blocks_mp(g);
+  r->fblocks = r->prec == HE4G_PREC_MIXED ? force_blocks_mp(g) : force_blocks(g);
   chk(r->partials = dalloc<double>(r, (size_t)r->pblocks * 12));
   chk(r->small = dalloc<double>(r, 64));
   chk(r->imp = dalloc<ImpState>(r, 1));

@@ -251,6 +251,27 @@ __device__ __forceinline__ C2<R> ld_pair(const R* p) {
   return __ldg(reinterpret_cast<const C2<R>*>(p));
 }
 
+// Block-strided loop over w < total that issues the global loads of kStage
+// iterations (ld(w)) before consuming any of them (st(w, value)), so that
+// each thread keeps kStage loads in flight instead of one.
+constexpr int kStage = 8;
+template <typename LD, typename ST>
+__device__ __forceinline__ void staged_loop(int total, LD ld, ST st) {
+  for (int w0 = threadIdx.x; w0 < total; w0 += kStage * blockDim.x) {
+    decltype(ld(0)) v[kStage];
+#pragma unroll
+    for (int u = 0; u < kStage; ++u) {
+      const int w = w0 + u * blockDim.x;
+      if (w < total) v[u] = ld(w);
+    }
+#pragma unroll
+    for (int u = 0; u < kStage; ++u) {
+      const int w = w0 + u * blockDim.x;
+      if (w < total) st(w, v[u]);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ x pass
 enum { PRO_PLAIN = 0, PRO_CORR = 1, PRO_PROD = 2 };
 
@@ -269,24 +290,26 @@ __global__ void __launch_bounds__(kThreads) k_x_r2c(Grid g, FftAxis ax, const C2
   const long long nlines = (long long)g.ny * g.nz;
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
-  for (int w = threadIdx.x; w < nl * m; w += blockDim.x) {
-    const int l = w / m, j = w - l * m;
-    const long long e = (l0 + l) * g.nx + 2 * j;  // even: aligned pair
-    C2<R> v;
-    if (PRO == PRO_PLAIN) {
-      v = ld_pair<R>(in0 + e);
-    } else if (PRO == PRO_CORR) {
-      // g = den*dencg*(cp4 + cpp4*dencg) (poten.f90:62-64)
-      const C2<R> d = ld_pair<R>(in0 + e);
-      const C2<R> c = ld_pair<R>(in1 + e);
-      v = mk<R>(d.x * c.x * fma(c1, c.x, c0), d.y * c.y * fma(c1, c.y, c0));
-    } else {
-      const C2<R> p = ld_pair<R>(in0 + e);
-      const C2<R> q = ld_pair<R>(in1 + e);
-      v = mk<R>(p.x * q.x, p.y * q.y);
-    }
-    a[l * ld + pidx<R>(j)] = v;
-  }
+  staged_loop(
+      nl * m,
+      [&](int w) {
+        const int l = w / m, j = w - l * m;
+        const long long e = (l0 + l) * g.nx + 2 * j;  // even: aligned pair
+        if (PRO == PRO_PLAIN) return ld_pair<R>(in0 + e);
+        if (PRO == PRO_CORR) {
+          // g = den*dencg*(cp4 + cpp4*dencg) (poten.f90:62-64)
+          const C2<R> d = ld_pair<R>(in0 + e);
+          const C2<R> c = ld_pair<R>(in1 + e);
+          return mk<R>(d.x * c.x * fma(c1, c.x, c0), d.y * c.y * fma(c1, c.y, c0));
+        }
+        const C2<R> p = ld_pair<R>(in0 + e);
+        const C2<R> q = ld_pair<R>(in1 + e);
+        return mk<R>(p.x * q.x, p.y * q.y);
+      },
+      [&](int w, C2<R> v) {
+        const int l = w / m, j = w - l * m;
+        a[l * ld + pidx<R>(j)] = v;
+      });
   C2<R>* tws = sm + 2 * lpb * ld;
   stage_twiddles<R>(tws, ax);
   __syncthreads();
@@ -339,10 +362,16 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
   const long long nlines = (long long)g.ny * g.nz;
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
-  for (int w = threadIdx.x; w < nl * (m + 1); w += blockDim.x) {
-    const int l = w / (m + 1), k = w - l * (m + 1);
-    b[l * ld + pidx<R>(k)] = __ldg(&in[(l0 + l) * g.nxh + k]);
-  }
+  staged_loop(
+      nl * (m + 1),
+      [&](int w) {
+        const int l = w / (m + 1), k = w - l * (m + 1);
+        return __ldg(&in[(l0 + l) * g.nxh + k]);
+      },
+      [&](int w, C2<R> v) {
+        const int l = w / (m + 1), k = w - l * (m + 1);
+        b[l * ld + pidx<R>(k)] = v;
+      });
   C2<R>* tws = sm + 2 * lpb * ld;
   stage_twiddles<R>(tws, ax);
   __syncthreads();
@@ -364,18 +393,33 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
   }
   __syncthreads();
   C2<R>* r = fft_smem<R, 1>(a, b, nl, ld, ax, tws);
-  for (int w = threadIdx.x; w < nl * m; w += blockDim.x) {
+  struct Pot4In {
+    C2<R> cg, d;
+  };
+  staged_loop(
+      nl * m,
+      [&](int w) {
+        Pot4In in{};
+        if (EPI == EPI_POT4) {
+          const int l = w / m, j = w - l * m;
+          const long long e = (l0 + l) * g.nx + 2 * j;
+          in.cg = ld_pair<R>(pa.dencg + e);
+          if (pa.fn.lsolid) in.d = ld_pair<R>(pa.den + e);
+        }
+        return in;
+      },
+      [&](int w, const Pot4In& in) {
     const int l = w / m, j = w - l * m;
     const long long e = (l0 + l) * g.nx + 2 * j;
     C2<R> v = r[l * ld + pidx<R>(j)];
     if (EPI == EPI_POT4) {
       const Functional& fn = pa.fn;
-      const C2<R> cg = ld_pair<R>(pa.dencg + e);
+      const C2<R> cg = in.cg;
       const R a0 = (R)fn.a0, a1 = (R)fn.a1;
       R p0 = fma(cg.x * cg.x, fma(a1, cg.x, a0), v.x);
       R p1 = fma(cg.y * cg.y, fma(a1, cg.y, a0), v.y);
       if (fn.lsolid) {
-        const C2<R> d = ld_pair<R>(pa.den + e);
+        const C2<R> d = in.d;
         const R beta = (R)fn.beta_solid, dm = (R)fn.den_m, cs = (R)fn.c_solid;
         const R t0 = tanh(beta * (d.x - dm));
         const R t1 = tanh(beta * (d.y - dm));
@@ -385,7 +429,7 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
       v = mk<R>(p0, p1);
     }
     *reinterpret_cast<C2<R>*>(out + e) = v;
-  }
+      });
 }
 
 // ------------------------------------------------------------- y / z passes
@@ -408,10 +452,16 @@ __global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> 
   const int kx0 = blockIdx.x * TX;
   const int ncol = min(TX, g.nxh - kx0);
   const long long base = (long long)blockIdx.y * g.ny * g.nxh + kx0;
-  for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
-    const int c = w & (TX - 1), j = w >> ltx;
-    if (c < ncol) a[c * ld + pidx<R>(j)] = sp[base + (long long)j * g.nxh + c];
-  }
+  staged_loop(
+      TX * n,
+      [&](int w) {
+        const int c = w & (TX - 1), j = w >> ltx;
+        return c < ncol ? sp[base + (long long)j * g.nxh + c] : mk<R>(0, 0);
+      },
+      [&](int w, C2<R> v) {
+        const int c = w & (TX - 1), j = w >> ltx;
+        if (c < ncol) a[c * ld + pidx<R>(j)] = v;
+      });
   C2<R>* tws = sm + 2 * TX * ld;
   stage_twiddles<R>(tws, ax);
   __syncthreads();
@@ -446,10 +496,16 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   const int ncol = min(TX, g.nxh - kx0);
   const long long plane = (long long)g.ny * g.nxh;
   const long long base = (long long)blockIdx.y * g.nxh + kx0;
-  for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
-    const int cc = w & (TX - 1), k = w >> ltx;
-    if (cc < ncol) a[cc * ld + pidx<R>(k)] = in[base + (long long)k * plane + cc];
-  }
+  staged_loop(
+      TX * n,
+      [&](int w) {
+        const int cc = w & (TX - 1), k = w >> ltx;
+        return cc < ncol ? in[base + (long long)k * plane + cc] : mk<R>(0, 0);
+      },
+      [&](int w, C2<R> v) {
+        const int cc = w & (TX - 1), k = w >> ltx;
+        if (cc < ncol) a[cc * ld + pidx<R>(k)] = v;
+      });
   C2<R>* tws = sm + 3 * TX * ld;
   stage_twiddles<R>(tws, ax);
   __syncthreads();
@@ -457,26 +513,38 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   C2<R>* s1 = fwd == a ? b : a;
   for (int o = 0; o < nout; ++o) {
     const R* fac = fl.f[o];
-    for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
-      const int cc = w & (TX - 1), k = w >> ltx;
-      if (cc < ncol) {
-        const R f = __ldg(&fac[base + (long long)k * plane + cc]) * scale;
-        const C2<R> v = fwd[cc * ld + pidx<R>(k)];
-        s1[cc * ld + pidx<R>(k)] = mk<R>(v.x * f, v.y * f);
-      }
-    }
+    staged_loop(
+        TX * n,
+        [&](int w) {
+          const int cc = w & (TX - 1), k = w >> ltx;
+          return cc < ncol ? __ldg(&fac[base + (long long)k * plane + cc]) : (R)0;
+        },
+        [&](int w, R f0) {
+          const int cc = w & (TX - 1), k = w >> ltx;
+          if (cc < ncol) {
+            const R f = f0 * scale;
+            const C2<R> v = fwd[cc * ld + pidx<R>(k)];
+            s1[cc * ld + pidx<R>(k)] = mk<R>(v.x * f, v.y * f);
+          }
+        });
     __syncthreads();
     C2<R>* r = fft_smem<R, 1>(s1, c, ncol, ld, ax, tws);
     C2<R>* dst = fl.out[o];
-    for (int w = threadIdx.x; w < TX * n; w += blockDim.x) {
-      const int cc = w & (TX - 1), k = w >> ltx;
-      if (cc < ncol) {
-        const long long e = base + (long long)k * plane + cc;
-        C2<R> v = r[cc * ld + pidx<R>(k)];
-        if (o == 0 && add) v = cadd<R>(v, add[e]);
-        dst[e] = v;
-      }
-    }
+    const C2<R>* addo = o == 0 ? add : nullptr;
+    staged_loop(
+        TX * n,
+        [&](int w) {
+          const int cc = w & (TX - 1), k = w >> ltx;
+          return (addo && cc < ncol) ? addo[base + (long long)k * plane + cc] : mk<R>(0, 0);
+        },
+        [&](int w, C2<R> av) {
+          const int cc = w & (TX - 1), k = w >> ltx;
+          if (cc < ncol) {
+            C2<R> v = r[cc * ld + pidx<R>(k)];
+            if (addo) v = cadd<R>(v, av);
+            dst[base + (long long)k * plane + cc] = v;
+          }
+        });
     __syncthreads();  // fwd stays intact; s1 and c are free again
   }
 }

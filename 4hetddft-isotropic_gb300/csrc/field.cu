@@ -214,6 +214,16 @@ __global__ void __launch_bounds__(256) k_rk_stage(Grid g, Stencil st, Functional
 }
 
 // -------------------------------------------------------------- impurity
+// a / d rounded to nearest, given inv = RN(1/d): q0 = RN(a*inv) lies within
+// one ulp of a/d, the residual a - q0*d is exact in one FMA, and
+// RN(q0 + residual*inv) = RN(a/d) (Markstein's theorem, IBM J. Res. Dev. 34
+// (1990) 111-119). Three FP64 instructions instead of a full division.
+__device__ __forceinline__ double div_rn(double a, double d, double inv) {
+  const double q0 = __dmul_rn(a, inv);
+  const double e = __fma_rn(-q0, d, a);
+  return __fma_rn(e, inv, q0);
+}
+
 // updatepoten (potenimp.f90:71-95): linear interpolation of the radial
 // table at r = |x - center|. Every rounding step is explicit so that uimp
 // matches a CPU evaluation of the same expression bit for bit.
@@ -221,7 +231,7 @@ __global__ void __launch_bounds__(256) k_potenimp(Grid g, const double* __restri
                                                    const double* __restrict__ ys,
                                                    const double* __restrict__ zs,
                                                    const double* __restrict__ potion, int npot,
-                                                   double delinter, ImpState* imp, int center_sel,
+                                                   double delinter, double inv, ImpState* imp, int center_sel,
                                                    double* uimp) {
   const Pt t = point(g);
   const double* c = center_sel == 0 ? imp->rimp : imp->center;
@@ -239,8 +249,14 @@ __global__ void __launch_bounds__(256) k_potenimp(Grid g, const double* __restri
   const double zt = __dmul_rn(dz, dz);
   const double yt = __dadd_rn(__dmul_rn(dy, dy), zt);
   const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), yt));
-  const long long ir = (long long)__ddiv_rn(r, delinter);
-  const double w = __ddiv_rn(fmod(r, delinter), delinter);
+  const long long ir = (long long)div_rn(r, delinter, inv);
+  // mod(r, delinter) exactly: r - ir*delinter is representable and one FMA
+  // gives it, except when r/delinter rounded up onto an integer; then the
+  // true remainder (in [delinter/2, delinter)) is that negative value plus
+  // delinter, again exact
+  double rem = __fma_rn(-(double)ir, delinter, r);
+  if (rem < 0.0) rem = __dadd_rn(rem, delinter);
+  const double w = div_rn(rem, delinter, inv);
   double u = 0.0;
   if (ir >= 0 && ir + 1 < npot) {
     u = __dadd_rn(__dmul_rn(__ldg(potion + ir), __dadd_rn(1.0, -w)), __dmul_rn(__ldg(potion + ir + 1), w));
@@ -251,35 +267,55 @@ __global__ void __launch_bounds__(256) k_potenimp(Grid g, const double* __restri
 }
 
 // derden (derden.f90:26-28) fused with the force sums of forceimp
-// (potenimp.f90:44-46); the gradient is stored when dx != nullptr.
+// (potenimp.f90:44-46); the gradient is stored when dx != nullptr. Each
+// thread walks kZD z-planes of one (x, y) column, with the z neighbours in a
+// sliding register window, so the block reduction is paid once per kZD
+// points.
+constexpr int kZD = 8;
+
 __global__ void __launch_bounds__(256) k_force(Grid g, Stencil st, const double* __restrict__ den,
                                                 const double* __restrict__ uimp, double* dx, double* dy,
                                                 double* dz, double* partials) {
-  const Pt t = point(g);
+  const int i = blockIdx.x * kBX + threadIdx.x;
+  const int j = blockIdx.y * kBY + threadIdx.y;
+  const int k0 = blockIdx.z * kZD;
   double v[3] = {0.0, 0.0, 0.0};
-  if (t.ok) {
+  if (i < g.nx && j < g.ny) {
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
-    double gx = 0.0, gy = 0.0, gz = 0.0;
+    const long long col = (long long)j * g.nx + i;
+    constexpr int W = kZD + 2 * kStencilHalf;
+    double wz[W];  // den at planes k0-6 .. k0+kZD+5 of this column
 #pragma unroll
-    for (int o = 1; o <= kStencilHalf; ++o) {
-      double a = t.i - o >= 0 ? __ldg(den + t.p - o) : 0.0;
-      double b = t.i + o < g.nx ? __ldg(den + t.p + o) : 0.0;
-      gx = fma(st.d1[0][o], b - a, gx);
-      a = t.j - o >= 0 ? __ldg(den + t.p - o * sy) : 0.0;
-      b = t.j + o < g.ny ? __ldg(den + t.p + o * sy) : 0.0;
-      gy = fma(st.d1[1][o], b - a, gy);
-      a = t.k - o >= 0 ? __ldg(den + t.p - o * sz) : 0.0;
-      b = t.k + o < g.nz ? __ldg(den + t.p + o * sz) : 0.0;
-      gz = fma(st.d1[2][o], b - a, gz);
+    for (int m = 0; m < W; ++m) {
+      const int k = k0 - kStencilHalf + m;
+      wz[m] = (k >= 0 && k < g.nz) ? __ldg(den + col + k * sz) : 0.0;
     }
-    const double u = __ldg(uimp + t.p);
-    v[0] = gx * u;
-    v[1] = gy * u;
-    v[2] = gz * u;
-    if (dx) {
-      dx[t.p] = gx;
-      dy[t.p] = gy;
-      dz[t.p] = gz;
+#pragma unroll
+    for (int m = 0; m < kZD; ++m) {
+      const int k = k0 + m;
+      if (k < g.nz) {
+        const long long p = col + k * sz;
+        double gx = 0.0, gy = 0.0, gz = 0.0;
+#pragma unroll
+        for (int o = 1; o <= kStencilHalf; ++o) {
+          double a = i - o >= 0 ? __ldg(den + p - o) : 0.0;
+          double b = i + o < g.nx ? __ldg(den + p + o) : 0.0;
+          gx = fma(st.d1[0][o], b - a, gx);
+          a = j - o >= 0 ? __ldg(den + p - o * sy) : 0.0;
+          b = j + o < g.ny ? __ldg(den + p + o * sy) : 0.0;
+          gy = fma(st.d1[1][o], b - a, gy);
+          gz = fma(st.d1[2][o], wz[m + kStencilHalf + o] - wz[m + kStencilHalf - o], gz);
+        }
+        const double u = __ldg(uimp + p);
+        v[0] = fma(gx, u, v[0]);
+        v[1] = fma(gy, u, v[1]);
+        v[2] = fma(gz, u, v[2]);
+        if (dx) {
+          dx[p] = gx;
+          dy[p] = gy;
+          dz[p] = gz;
+        }
+      }
     }
   }
   block_sum<3>(v, partials);
@@ -590,7 +626,9 @@ __global__ void k_ualphas_b(Grid g, double* u, const double* s4, const double* s
 }  // namespace
 
 int pc_blocks(const Grid& g) { return point_blocks(g); }
-int force_blocks(const Grid& g) { return point_blocks(g); }
+int force_blocks(const Grid& g) {
+  return ((g.nx + kBX - 1) / kBX) * ((g.ny + kBY - 1) / kBY) * ((g.nz + kZD - 1) / kZD);
+}
 int energy_blocks(const Grid& g) { return point_blocks(g); }
 
 void launch_pc_predict(const Grid& g, const Stencil& st, const Functional& fn, const double2* psi,
@@ -618,12 +656,14 @@ void launch_rk_stage(const Grid& g, const Stencil& st, const Functional& fn, con
 void launch_potenimp(const Grid& g, const double* x, const double* y, const double* z, const double* potion,
                      int npot, double delinter, const ImpState* imp, int center_sel, double* uimp,
                      cudaStream_t s) {
-  k_potenimp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, x, y, z, potion, npot, delinter,
+  const double inv = 1.0 / delinter;  // correctly rounded (IEEE division)
+  k_potenimp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, x, y, z, potion, npot, delinter, inv,
                                                       const_cast<ImpState*>(imp), center_sel, uimp);
 }
 void launch_force(const Grid& g, const Stencil& st, const double* den, const double* uimp, double* dx,
                   double* dy, double* dz, double* partials, cudaStream_t s) {
-  k_force<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, den, uimp, dx, dy, dz, partials);
+  dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZD - 1) / kZD);
+  k_force<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, uimp, dx, dy, dz, partials);
 }
 void launch_grad1(const Grid& g, const Stencil& st, int axis, const double* in, double* out, cudaStream_t s) {
   k_grad1<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, axis, in, out);

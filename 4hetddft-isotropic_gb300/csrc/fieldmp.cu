@@ -17,7 +17,6 @@ namespace he4g {
 namespace {
 
 constexpr int kBX = 64, kBY = 4;  // 256-thread point blocks
-constexpr int kZ = 8;             // z-planes per thread in the force sums
 
 struct Pt {
   int i, j, k;
@@ -236,43 +235,61 @@ __global__ void k_split_mp(Grid g, const double2* __restrict__ psi, float2* psi3
   den[t.p] = fmaf(p32.x, p32.x, p32.y * p32.y);
 }
 
-// updatepoten (potenimp.f90:71-95) in FP32
-__global__ void __launch_bounds__(256) k_potenimp_mp(Grid g, const float* __restrict__ xs,
-                                                      const float* __restrict__ ys, const float* __restrict__ zs,
-                                                      const float* __restrict__ potion, int npot, float delinter,
-                                                      ImpState* imp, int center_sel, float* uimp) {
-  const Pt t = point(g);
-  const double* c = center_sel == 0 ? imp->rimp : imp->center;
-  const double c0 = c[0], c1 = c[1], c2 = c[2];
-  if (center_sel == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 &&
-      threadIdx.y == 0) {
-    imp->center[0] = c0;
-    imp->center[1] = c1;
-    imp->center[2] = c2;
-  }
-  if (!t.ok) return;
-  const float dz = __ldg(zs + t.k) - (float)c2;
-  const float dy = __ldg(ys + t.j) - (float)c1;
-  const float dx = __ldg(xs + t.i) - (float)c0;
-  const float r = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-  // node and weight from one quotient: the reference's int(r/d), mod(r,d)/d
-  // pair disagrees at table nodes whenever r/d rounds up, and in FP32 that
-  // happens often enough to put a full table step into uimp
-  const float qd = r / delinter;
+// updatepoten (potenimp.f90:71-95) in FP32 at offset (dx, dy, dz) from the
+// centre. Node and weight come from one quotient: the reference's
+// int(r/d), mod(r,d)/d pair disagrees at table nodes whenever r/d rounds up,
+// and in FP32 that happens often enough to put a full table step into uimp.
+// r = r2 * rsqrt(r2) and r * (1/d) are within a few FP32 ulps, far inside the
+// mixed form's tolerance; the standalone potenimp and the force kernel use
+// this same function, so their uimp agree bit for bit.
+__device__ __forceinline__ float uimp_at(const ImpTable& t, float dx, float dy, float dz, int* health) {
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+  const float qd = r * t.inv;
   const int ir = (int)qd;
   const float w = qd - (float)ir;
-  float u = 0.f;
-  if (ir >= 0 && ir + 1 < npot) {
-    u = fmaf(__ldg(potion + ir), 1.f - w, __ldg(potion + ir + 1) * w);
-  } else {
-    atomicOr(&imp->health, 4);
-  }
-  uimp[t.p] = u;
+  if (ir >= 0 && ir + 1 < t.npot) return fmaf(__ldg(t.potion + ir), 1.f - w, __ldg(t.potion + ir + 1) * w);
+  atomicOr(health, 4);
+  return 0.f;
 }
 
-// grad(den) . uimp summed per block: each thread walks kZ z-planes with a
-// compensated (Kahan) FP32 sum of its products, then the block and the grid
-// sum in FP64
+// The block's centre in FP32 (conversions from FP64 issue at the FP64 rate,
+// so they are done once per block). center_sel 0: rimp, which block 0 also
+// records as the centre of the new uimp; 1: the recorded centre.
+__device__ __forceinline__ void load_center(ImpState* imp, int center_sel, float* cf) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  if (tid < 3) {
+    const double c = center_sel == 0 ? imp->rimp[tid] : imp->center[tid];
+    cf[tid] = (float)c;
+    if (center_sel == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) imp->center[tid] = c;
+  }
+  __syncthreads();
+}
+
+constexpr int kZF = 8;  // z-planes per thread of the impurity kernels
+
+__global__ void __launch_bounds__(256) k_potenimp_mp(Grid g, ImpTable tab, ImpState* imp, int center_sel,
+                                                      float* uimp) {
+  __shared__ float cf[3];
+  load_center(imp, center_sel, cf);
+  const int i = blockIdx.x * kBX + threadIdx.x;
+  const int j = blockIdx.y * kBY + threadIdx.y;
+  if (i >= g.nx || j >= g.ny) return;
+  const float dx = __ldg(tab.xs + i) - cf[0];
+  const float dy = __ldg(tab.ys + j) - cf[1];
+  float* col = uimp + (long long)j * g.nx + i;
+  const int sz = g.nx * g.ny;
+  const int k0 = blockIdx.z * kZF, k1 = min(k0 + kZF, g.nz);
+  for (int k = k0; k < k1; ++k) col[(long long)k * sz] = uimp_at(tab, dx, dy, __ldg(tab.zs + k) - cf[2], &imp->health);
+}
+
+// forceimp (potenimp.f90:24-55 with derden.f90:26-28) fused with updatepoten:
+// grad(den) . uimp summed per block, with uimp evaluated in place (and
+// stored when uimp_out != nullptr). Each thread walks kZF z-planes of one
+// (x, y) column with the z neighbours of den in a sliding register window and
+// sums its products with a compensated (Kahan) FP32 sum. Warps combine the
+// (sum, -compensation) pairs as FP32 double-word numbers; FP64 starts at the
+// warp totals.
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   const float y = x - c;
   const float t = s + y;
@@ -280,39 +297,88 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   s = t;
 }
 
-__global__ void __launch_bounds__(256) k_force_mp(Grid g, StencilF st, const float* __restrict__ den,
-                                                   const float* __restrict__ uimp, double* partials) {
+// (h, l) += (bh, bl), double-word addition (Knuth's two-sum on the heads)
+__device__ __forceinline__ void dw_add(float& h, float& l, float bh, float bl) {
+  const float s = h + bh;
+  const float bb = s - h;
+  const float e = (h - (s - bb)) + (bh - bb);
+  const float t = l + bl + e;
+  h = s + t;
+  l = t - (h - s);
+}
+
+template <int NV>
+__device__ __forceinline__ void block_sum_dw(float (&h)[NV], float (&l)[NV], double* partials) {
+  __shared__ double sh[NV][8];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int a = 0; a < NV; ++a) {
+    float x = h[a], y = l[a];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float bx = __shfl_down_sync(0xffffffffu, x, o);
+      const float by = __shfl_down_sync(0xffffffffu, y, o);
+      dw_add(x, y, bx, by);
+    }
+    if (lane == 0) sh[a][wid] = (double)x + (double)y;
+  }
+  __syncthreads();
+  if (tid < NV) {
+    double s = 0.0;
+    for (int w = 0; w < 8; ++w) s += sh[tid][w];
+    partials[(long long)block_linear() * NV + tid] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256, 3) k_force_mp(Grid g, StencilF st, const float* __restrict__ den, ImpTable tab,
+                                                      ImpState* imp, int center_sel, float* uimp_out,
+                                                      double* partials) {
+  __shared__ float cf[3];
+  load_center(imp, center_sel, cf);
   const int i = blockIdx.x * kBX + threadIdx.x;
   const int j = blockIdx.y * kBY + threadIdx.y;
-  const int k0 = blockIdx.z * kZ;
-  double v[3] = {0.0, 0.0, 0.0};
+  const int k0 = blockIdx.z * kZF;
   float s[3] = {0.f, 0.f, 0.f}, cc[3] = {0.f, 0.f, 0.f};
   if (i < g.nx && j < g.ny) {
-    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
-    for (int k = k0; k < min(k0 + kZ, g.nz); ++k) {
-      const long long p = ((long long)k * g.ny + j) * g.nx + i;
-      float gx = 0.f, gy = 0.f, gz = 0.f;
+    const int sy = g.nx, sz = g.nx * g.ny;
+    const long long colo = (long long)j * g.nx + i;
+    const float* col = den + colo;
+    const float dx = __ldg(tab.xs + i) - cf[0];
+    const float dy = __ldg(tab.ys + j) - cf[1];
+    constexpr int W = kZF + 2 * kStencilHalf;
+    float wz[W];  // den at planes k0-6 .. k0+kZF+5 of this column
 #pragma unroll
-      for (int o = 1; o <= kStencilHalf; ++o) {
-        float a = i - o >= 0 ? __ldg(den + p - o) : 0.f;
-        float b = i + o < g.nx ? __ldg(den + p + o) : 0.f;
-        gx = fmaf(st.d1[0][o], b - a, gx);
-        a = j - o >= 0 ? __ldg(den + p - o * sy) : 0.f;
-        b = j + o < g.ny ? __ldg(den + p + o * sy) : 0.f;
-        gy = fmaf(st.d1[1][o], b - a, gy);
-        a = k - o >= 0 ? __ldg(den + p - o * sz) : 0.f;
-        b = k + o < g.nz ? __ldg(den + p + o * sz) : 0.f;
-        gz = fmaf(st.d1[2][o], b - a, gz);
-      }
-      const float u = __ldg(uimp + p);
-      kahan_add(s[0], cc[0], gx * u);
-      kahan_add(s[1], cc[1], gy * u);
-      kahan_add(s[2], cc[2], gz * u);
+    for (int m = 0; m < W; ++m) {
+      const int k = k0 - kStencilHalf + m;
+      wz[m] = (k >= 0 && k < g.nz) ? __ldg(col + (long long)k * sz) : 0.f;
     }
 #pragma unroll
-    for (int a = 0; a < 3; ++a) v[a] = (double)s[a] - (double)cc[a];
+    for (int m = 0; m < kZF; ++m) {
+      const int k = k0 + m;
+      if (k < g.nz) {
+        const float* q = col + (long long)k * sz;
+        float gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+        for (int o = 1; o <= kStencilHalf; ++o) {
+          float a = i - o >= 0 ? __ldg(q - o) : 0.f;
+          float b = i + o < g.nx ? __ldg(q + o) : 0.f;
+          gx = fmaf(st.d1[0][o], b - a, gx);
+          a = j - o >= 0 ? __ldg(q - o * sy) : 0.f;
+          b = j + o < g.ny ? __ldg(q + o * sy) : 0.f;
+          gy = fmaf(st.d1[1][o], b - a, gy);
+          gz = fmaf(st.d1[2][o], wz[m + kStencilHalf + o] - wz[m + kStencilHalf - o], gz);
+        }
+        const float u = uimp_at(tab, dx, dy, __ldg(tab.zs + k) - cf[2], &imp->health);
+        if (uimp_out) uimp_out[colo + (long long)k * sz] = u;
+        kahan_add(s[0], cc[0], gx * u);
+        kahan_add(s[1], cc[1], gy * u);
+        kahan_add(s[2], cc[2], gz * u);
+      }
+    }
   }
-  block_sum_d<3>(v, partials);
+  float lo[3] = {-cc[0], -cc[1], -cc[2]};
+  block_sum_dw<3>(s, lo, partials);
 }
 
 __global__ void __launch_bounds__(256) k_grad1_f(Grid g, StencilF st, int axis, const float* __restrict__ in,
@@ -401,7 +467,7 @@ __global__ void __launch_bounds__(256) k_energy_point_mp(Grid g, Functional fn, 
 }  // namespace
 
 int force_blocks_mp(const Grid& g) {
-  return ((g.nx + kBX - 1) / kBX) * ((g.ny + kBY - 1) / kBY) * ((g.nz + kZ - 1) / kZ);
+  return ((g.nx + kBX - 1) / kBX) * ((g.ny + kBY - 1) / kBY) * ((g.nz + kZF - 1) / kZF);
 }
 
 void launch_pc_predict_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
@@ -430,15 +496,15 @@ void launch_rk_stage_mp(const Grid& g, const StencilF& st, const Functional& fn,
 void launch_split_mp(const Grid& g, const double2* psi, float2* psi32, float* den, cudaStream_t s) {
   k_split_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, psi, psi32, den);
 }
-void launch_potenimp_mp(const Grid& g, const float* x, const float* y, const float* z, const float* potion,
-                        int npot, float delinter, ImpState* imp, int center_sel, float* uimp, cudaStream_t s) {
-  k_potenimp_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, x, y, z, potion, npot, delinter, imp, center_sel,
-                                                         uimp);
+void launch_potenimp_mp(const Grid& g, const ImpTable& tab, ImpState* imp, int center_sel, float* uimp,
+                        cudaStream_t s) {
+  dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZF - 1) / kZF);
+  k_potenimp_mp<<<grid, dim3(kBX, kBY), 0, s>>>(g, tab, imp, center_sel, uimp);
 }
-void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const float* uimp, double* partials,
-                     cudaStream_t s) {
-  dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZ - 1) / kZ);
-  k_force_mp<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, uimp, partials);
+void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const ImpTable& tab, ImpState* imp,
+                     int center_sel, float* uimp_out, double* partials, cudaStream_t s) {
+  dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZF - 1) / kZF);
+  k_force_mp<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, tab, imp, center_sel, uimp_out, partials);
 }
 void launch_grad1_f(const Grid& g, const StencilF& st, int axis, const float* in, float* out, cudaStream_t s) {
   k_grad1_f<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, axis, in, out);

@@ -199,11 +199,20 @@ void launch_rk_stage_mp(const Grid& g, const StencilF& st, const Functional& fn,
                         const float* pot4, const float* uimp, const float* timec, float* den, double ar, double br,
                         double cr, double dt, int* health, cudaStream_t s);
 void launch_split_mp(const Grid& g, const double2* psi, float2* psi32, float* den, cudaStream_t s);
-void launch_potenimp_mp(const Grid& g, const float* x, const float* y, const float* z, const float* potion,
-                        int npot, float delinter, ImpState* imp, int center_sel, float* uimp, cudaStream_t s);
+// FP32 grid coordinates and radial table of the impurity potential
+struct ImpTable {
+  const float *xs, *ys, *zs;
+  const float* potion;
+  int npot;
+  float inv;  // 1 / delinter
+};
+void launch_potenimp_mp(const Grid& g, const ImpTable& tab, ImpState* imp, int center_sel, float* uimp,
+                        cudaStream_t s);
 int force_blocks_mp(const Grid& g);
-void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const float* uimp, double* partials,
-                     cudaStream_t s);
+// potenimp fused into the force sum: uimp is evaluated in place from the
+// centre (stored to uimp_out when not null)
+void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const ImpTable& tab, ImpState* imp,
+                     int center_sel, float* uimp_out, double* partials, cudaStream_t s);
 void launch_grad1_f(const Grid& g, const StencilF& st, int axis, const float* in, float* out, cudaStream_t s);
 void launch_falfs_f(const Grid& g, const float* denalf, float den0s, float* falfs, cudaStream_t s);
 void launch_dot3_f(const Grid& g, const float* ax, const float* ay, const float* az, const float* bx,

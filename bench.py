@@ -153,13 +153,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+TILES = None  # fixed FFT tiles (profiling runs) instead of autotuning
+
+
 def make_run(prec=FP64):
     import he4gpu
     psi, r, v, meta = he4gpu.collision_case(CASE)
     kw, tk = he4gpu.config_for_case(meta)
     cfg = he4gpu.default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], precision=prec, **kw)
     run = he4gpu.Run(cfg, selec=tk["selec"], r_cutoff=tk["r_cutoff"], umax=tk["umax"])
-    run.autotune()
+    if TILES:
+        run.tiles = TILES
+    else:
+        run.autotune()
     return run, cfg, psi, r, v, meta
 
 
@@ -435,8 +441,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision block")
     ap.add_argument("--case", default=CASE, help="workload (profiling runs use smaller ones)")
+    ap.add_argument("--tiles", default=None,
+                    help="FFT tiles lpb_r2c,lpb_c2r,log2cols_y,log2cols_z instead of autotuning (profiling runs)")
     args = ap.parse_args()
     set_case(args.case)
+    if args.tiles:
+        global TILES
+        TILES = tuple(int(t) for t in args.tiles.split(","))
     if args.impl == "reference":
         return reference_arm(args)
     return ours(args)
