@@ -1112,6 +1112,7 @@ constexpr int kMaxLpb = 64;
 constexpr int kMaxLtx = 5;
 
 bool tiles_fit(const he4g_run* r, const FftTiles& t) {
+  if (t.engine & ~fft_reg_engines(r->plan)) return false;
   if (t.lpb_r2c < 1 || t.lpb_r2c > kMaxLpb || t.lpb_c2r < 1 || t.lpb_c2r > kMaxLpb) return false;
   if (t.ltx_y < 0 || t.ltx_y > kMaxLtx || t.ltx_z < 0 || t.ltx_z > kMaxLtx) return false;
   return fft_smem_bytes(r->prec, PASS_R2C, r->plan, t.lpb_r2c) && fft_smem_bytes(r->prec, PASS_C2R, r->plan, t.lpb_c2r) &&
@@ -1139,16 +1140,17 @@ float per_launch_ms(he4g_run* r, cudaEvent_t a, cudaEvent_t b, int reps, F fn) {
   return ms / reps;
 }
 
-void tiles_to(const FftTiles& t, int out[4]) {
+void tiles_to(const FftTiles& t, int out[HE4G_NTILES]) {
   out[0] = t.lpb_r2c;
   out[1] = t.lpb_c2r;
   out[2] = t.ltx_y;
   out[3] = t.ltx_z;
+  out[4] = t.engine;
 }
 }  // namespace
 }  // extern "C++"
 
-int he4g_autotune(he4g_run* r, int reps, int tiles[4]) {
+int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
   if (!r || reps < 0) return HE4G_EINVAL;
   if (reps == 0) reps = 5;
   cudaError_t e0 = cudaStreamSynchronize(r->s);
@@ -1162,21 +1164,32 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[4]) {
   FftTiles trial = best;
   // Each pass runs on the run's scratch spectra with the run's own geometry:
   // r2c of the density into spec0, y on spec0, the z convolution of spec0
-  // with the Lennard-Jones table into spec1, c2r of spec0 into spec1. Every
-  // line is transformed by the same arithmetic whatever the tile, so the
-  // choice changes timing only.
+  // with the Lennard-Jones table into spec1, c2r of spec0 into spec1. The
+  // candidates are every generic tile that fits and, where the length has a
+  // specialisation, the register engine. Generic tiles change timing only;
+  // the two engines agree to rounding.
   void* sp[1] = {r->spec0};
   void* zo[1] = {r->spec1};
   const void* zf[1] = {r->fvlj4};
   const void* ci[1] = {r->spec0};
   void* co[1] = {r->spec1};
-  auto sweep = [&](int pass, int lo, int hi, bool pow2, int FftTiles::*field) {
+  const int engines = fft_reg_engines(r->plan);
+  auto sweep = [&](int pass, int lo, int hi, bool pow2, int FftTiles::*field, int bit) {
     float best_ms = 0.f;
     int best_tile = best.*field;
-    for (int t = lo; t <= hi; t = pow2 ? t * 2 : t + 1) {
-      if (!fft_smem_bytes(prec, pass, r->plan, t)) continue;
+    bool best_reg = false;
+    const int stop = (engines & bit) ? hi + 1 : hi;  // t == hi + 1: the register engine
+    for (int t = lo; t <= stop; t = (t == hi) ? hi + 1 : (pow2 ? t * 2 : t + 1)) {
+      const bool reg = t > hi;
+      if (!reg && !fft_smem_bytes(prec, pass, r->plan, t)) continue;
       trial = best;
-      trial.*field = t;
+      if (reg) {
+        trial.*field = best_tile;
+        trial.engine |= bit;
+      } else {
+        trial.*field = t;
+        trial.engine &= ~bit;
+      }
       r->plan.tiles = trial;
       fft_prepare(prec, r->plan);
       float ms = per_launch_ms(r, a, b, reps, [&] {
@@ -1189,15 +1202,21 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[4]) {
       });
       if (best_ms == 0.f || ms < best_ms) {
         best_ms = ms;
-        best_tile = t;
+        if (reg) {
+          best_reg = true;
+        } else {
+          best_tile = t;
+          best_reg = false;
+        }
       }
     }
     best.*field = best_tile;
+    best.engine = best_reg ? (best.engine | bit) : (best.engine & ~bit);
   };
-  sweep(PASS_R2C, 1, kMaxLpb, true, &FftTiles::lpb_r2c);
-  sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y);
-  sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z);
-  sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r);
+  sweep(PASS_R2C, 1, kMaxLpb, true, &FftTiles::lpb_r2c, ENGINE_R2C);
+  sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y, ENGINE_Y);
+  sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z, ENGINE_Z);
+  sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r, ENGINE_C2R);
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   apply_tiles(r, best);
@@ -1208,15 +1227,15 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[4]) {
   return HE4G_OK;
 }
 
-int he4g_get_tiles(const he4g_run* r, int tiles[4]) {
+int he4g_get_tiles(const he4g_run* r, int tiles[HE4G_NTILES]) {
   if (!r || !tiles) return HE4G_EINVAL;
   tiles_to(r->plan.tiles, tiles);
   return HE4G_OK;
 }
 
-int he4g_set_tiles(he4g_run* r, const int tiles[4]) {
+int he4g_set_tiles(he4g_run* r, const int tiles[HE4G_NTILES]) {
   if (!r || !tiles) return HE4G_EINVAL;
-  const FftTiles t{tiles[0], tiles[1], tiles[2], tiles[3]};
+  const FftTiles t{tiles[0], tiles[1], tiles[2], tiles[3], tiles[4]};
   if (!tiles_fit(r, t)) return fail(r, HE4G_EINVAL, "tile shape out of range or over the shared-memory limit");
   apply_tiles(r, t);
   return HE4G_OK;

@@ -23,257 +23,13 @@
 #include <mutex>
 #include <utility>
 
-#include "he4g_internal.cuh"
+#include "fft_common.cuh"
 
 namespace he4g {
 
 namespace {
 
-constexpr int kThreads = 256;
-
-template <typename R>
-struct Cx;
-// kTile: kx columns per y/z block (128-byte rows). kPad: shared-memory lines
-// get one padding element per 128 bytes (element i sits at i + (i >> kPad)),
-// which spreads the strided writes of the Stockham passes over all banks.
-template <>
-struct Cx<double> {
-  using T = double2;
-  static constexpr int kTile = 8;
-  static constexpr int kPad = 3;
-};
-template <>
-struct Cx<float> {
-  using T = float2;
-  static constexpr int kTile = 8;
-  static constexpr int kPad = 4;
-};
-template <typename R>
-using C2 = typename Cx<R>::T;
-
-template <typename R>
-__device__ __forceinline__ int pidx(int i) {
-  return i + (i >> Cx<R>::kPad);
-}
-// shared-memory stride of a line holding n elements
-template <typename R>
-__host__ __device__ constexpr int padded_len(int n) {
-  return n + (n >> Cx<R>::kPad) + 1;
-}
-
-template <typename R>
-__device__ __forceinline__ C2<R> mk(R x, R y) {
-  C2<R> c;
-  c.x = x;
-  c.y = y;
-  return c;
-}
-template <typename R>
-__device__ __forceinline__ C2<R> cadd(C2<R> a, C2<R> b) { return mk<R>(a.x + b.x, a.y + b.y); }
-template <typename R>
-__device__ __forceinline__ C2<R> csub(C2<R> a, C2<R> b) { return mk<R>(a.x - b.x, a.y - b.y); }
-template <typename R>
-__device__ __forceinline__ C2<R> cconj(C2<R> a) { return mk<R>(a.x, -a.y); }
-
-// a * w (SIGN < 0) or a * conj(w) (SIGN > 0)
-template <typename R, int SIGN>
-__device__ __forceinline__ C2<R> mulw(C2<R> a, C2<R> w) {
-  if (SIGN < 0) return mk<R>(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
-  return mk<R>(fma(a.x, w.x, a.y * w.y), fma(a.y, w.x, -a.x * w.y));
-}
-// a * (SIGN * i)
-template <typename R, int SIGN>
-__device__ __forceinline__ C2<R> jmul(C2<R> a) {
-  return SIGN < 0 ? mk<R>(a.y, -a.x) : mk<R>(-a.y, a.x);
-}
-
-template <typename R, int SIGN>
-__device__ __forceinline__ void bf2(C2<R>* v) {
-  C2<R> t = v[0];
-  v[0] = cadd<R>(t, v[1]);
-  v[1] = csub<R>(t, v[1]);
-}
-template <typename R, int SIGN>
-__device__ __forceinline__ void bf4(C2<R>& a0, C2<R>& a1, C2<R>& a2, C2<R>& a3) {
-  C2<R> t0 = cadd<R>(a0, a2), t1 = csub<R>(a0, a2);
-  C2<R> t2 = cadd<R>(a1, a3), t3 = jmul<R, SIGN>(csub<R>(a1, a3));
-  a0 = cadd<R>(t0, t2);
-  a2 = csub<R>(t0, t2);
-  a1 = cadd<R>(t1, t3);
-  a3 = csub<R>(t1, t3);
-}
-template <typename R, int SIGN>
-__device__ __forceinline__ void bf8(C2<R>* v) {
-  const R r = (R)0.70710678118654752440;
-  C2<R> a0 = v[0], a1 = v[2], a2 = v[4], a3 = v[6];
-  C2<R> b0 = v[1], b1 = v[3], b2 = v[5], b3 = v[7];
-  bf4<R, SIGN>(a0, a1, a2, a3);
-  bf4<R, SIGN>(b0, b1, b2, b3);
-  if (SIGN < 0) {
-    b1 = mk<R>((b1.x + b1.y) * r, (b1.y - b1.x) * r);
-    b3 = mk<R>((b3.y - b3.x) * r, -(b3.x + b3.y) * r);
-  } else {
-    b1 = mk<R>((b1.x - b1.y) * r, (b1.y + b1.x) * r);
-    b3 = mk<R>(-(b3.x + b3.y) * r, (b3.x - b3.y) * r);
-  }
-  b2 = jmul<R, SIGN>(b2);
-  v[0] = cadd<R>(a0, b0);
-  v[4] = csub<R>(a0, b0);
-  v[1] = cadd<R>(a1, b1);
-  v[5] = csub<R>(a1, b1);
-  v[2] = cadd<R>(a2, b2);
-  v[6] = csub<R>(a2, b2);
-  v[3] = cadd<R>(a3, b3);
-  v[7] = csub<R>(a3, b3);
-}
-template <typename R, int SIGN>
-__device__ __forceinline__ void bf3(C2<R>* v) {
-  const R s3 = (R)0.86602540378443864676;  // sin(2 pi / 3)
-  C2<R> b = cadd<R>(v[1], v[2]);
-  C2<R> d = csub<R>(v[1], v[2]);
-  C2<R> t = mk<R>(fma((R)-0.5, b.x, v[0].x), fma((R)-0.5, b.y, v[0].y));
-  C2<R> s = jmul<R, SIGN>(mk<R>(s3 * d.x, s3 * d.y));
-  v[0] = cadd<R>(v[0], b);
-  v[1] = cadd<R>(t, s);
-  v[2] = csub<R>(t, s);
-}
-template <typename R, int SIGN>
-__device__ __forceinline__ void bf5(C2<R>* v) {
-  const R c1 = (R)0.30901699437494742410, c2 = (R)-0.80901699437494742410;  // cos(2pi/5), cos(4pi/5)
-  const R s1 = (R)0.95105651629515357212, s2 = (R)0.58778525229247312917;   // sin(2pi/5), sin(4pi/5)
-  C2<R> b1 = cadd<R>(v[1], v[4]), b2 = cadd<R>(v[2], v[3]);
-  C2<R> d1 = csub<R>(v[1], v[4]), d2 = csub<R>(v[2], v[3]);
-  C2<R> a0 = v[0];
-  C2<R> t1 = mk<R>(fma(c2, b2.x, fma(c1, b1.x, a0.x)), fma(c2, b2.y, fma(c1, b1.y, a0.y)));
-  C2<R> t2 = mk<R>(fma(c1, b2.x, fma(c2, b1.x, a0.x)), fma(c1, b2.y, fma(c2, b1.y, a0.y)));
-  C2<R> u1 = mk<R>(fma(s2, d2.x, s1 * d1.x), fma(s2, d2.y, s1 * d1.y));
-  C2<R> u2 = mk<R>(fma(-s1, d2.x, s2 * d1.x), fma(-s1, d2.y, s2 * d1.y));
-  u1 = jmul<R, SIGN>(u1);
-  u2 = jmul<R, SIGN>(u2);
-  v[0] = mk<R>(a0.x + b1.x + b2.x, a0.y + b1.y + b2.y);
-  v[1] = cadd<R>(t1, u1);
-  v[4] = csub<R>(t1, u1);
-  v[2] = cadd<R>(t2, u2);
-  v[3] = csub<R>(t2, u2);
-}
-
-template <typename R, int RAD, int SIGN>
-__device__ __forceinline__ void butterfly(C2<R>* v) {
-  if (RAD == 2) bf2<R, SIGN>(v);
-  if (RAD == 3) bf3<R, SIGN>(v);
-  if (RAD == 4) bf4<R, SIGN>(v[0], v[1], v[2], v[3]);
-  if (RAD == 5) bf5<R, SIGN>(v);
-  if (RAD == 8) bf8<R, SIGN>(v);
-}
-
-template <typename R>
-__device__ __forceinline__ const C2<R>* twiddles(const FftAxis& ax);
-template <>
-__device__ __forceinline__ const double2* twiddles<double>(const FftAxis& ax) {
-  return ax.tw;
-}
-template <>
-__device__ __forceinline__ const float2* twiddles<float>(const FftAxis& ax) {
-  return ax.twf;
-}
-
-// One Stockham pass of radix RAD over `nlines` lines of length n held in
-// shared memory at src + l*ld (natural order in, autosorted order out).
-// w / d by multiply-high (mag = ceil(2^32/d); mag == 0 marks d == 1)
-__device__ __forceinline__ int mdiv(int w, unsigned mag) { return mag ? (int)__umulhi((unsigned)w, mag) : w; }
-
-// tw points to the n twiddles of the axis staged in shared memory.
-template <typename R, int RAD, int SIGN>
-__device__ __forceinline__ void stockham_pass(const C2<R>* __restrict__ src, C2<R>* __restrict__ dst, int n,
-                                              int ns, int nlines, int ld, const C2<R>* __restrict__ tw,
-                                              unsigned mag_nr, unsigned mag_ns) {
-  const int nr = n / RAD;
-  const int tstep = n / (ns * RAD);
-  const int total = nlines * nr;
-  for (int w = threadIdx.x; w < total; w += blockDim.x) {
-    const int l = mdiv(w, mag_nr);
-    const int j = w - l * nr;
-    const int q = mdiv(j, mag_ns);
-    const int k = j - q * ns;
-    const C2<R>* s = src + l * ld;
-    C2<R> v[RAD];
-#pragma unroll
-    for (int r = 0; r < RAD; ++r) v[r] = s[pidx<R>(j + r * nr)];
-    if (k > 0) {
-#pragma unroll
-      for (int r = 1; r < RAD; ++r) v[r] = mulw<R, SIGN>(v[r], tw[r * k * tstep]);
-    }
-    butterfly<R, RAD, SIGN>(v);
-    const int idx = q * ns * RAD + k;
-    C2<R>* d = dst + l * ld;
-#pragma unroll
-    for (int r = 0; r < RAD; ++r) d[pidx<R>(idx + r * ns)] = v[r];
-  }
-}
-
-// Copies the axis' n twiddles into shared memory (caller syncs).
-template <typename R>
-__device__ __forceinline__ void stage_twiddles(C2<R>* tws, const FftAxis& ax) {
-  const C2<R>* tw = twiddles<R>(ax);
-  for (int t = threadIdx.x; t < ax.n; t += blockDim.x) tws[t] = __ldg(&tw[t]);
-}
-
-// Full transform of nlines lines; a holds the input, b is scratch, tws the
-// staged twiddles; returns the buffer that holds the result. Ends with a
-// barrier.
-template <typename R, int SIGN>
-__device__ C2<R>* fft_smem(C2<R>* a, C2<R>* b, int nlines, int ld, const FftAxis& ax, const C2<R>* tws) {
-  int ns = 1;
-  for (int f = 0; f < ax.nf; ++f) {
-    const int rad = ax.fac[f];
-    const unsigned mnr = ax.mag_nr[f], mns = ax.mag_ns[f];
-    if (rad == 8)
-      stockham_pass<R, 8, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
-    else if (rad == 4)
-      stockham_pass<R, 4, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
-    else if (rad == 2)
-      stockham_pass<R, 2, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
-    else if (rad == 3)
-      stockham_pass<R, 3, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
-    else
-      stockham_pass<R, 5, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
-    __syncthreads();
-    C2<R>* t = a;
-    a = b;
-    b = t;
-    ns *= rad;
-  }
-  return a;
-}
-
-template <typename R>
-__device__ __forceinline__ C2<R> ld_pair(const R* p) {
-  return __ldg(reinterpret_cast<const C2<R>*>(p));
-}
-
-// Block-strided loop over w < total that issues the global loads of kStage
-// iterations (ld(w)) before consuming any of them (st(w, value)), so that
-// each thread keeps kStage loads in flight instead of one.
-constexpr int kStage = 8;
-template <typename LD, typename ST>
-__device__ __forceinline__ void staged_loop(int total, LD ld, ST st) {
-  for (int w0 = threadIdx.x; w0 < total; w0 += kStage * blockDim.x) {
-    decltype(ld(0)) v[kStage];
-#pragma unroll
-    for (int u = 0; u < kStage; ++u) {
-      const int w = w0 + u * blockDim.x;
-      if (w < total) v[u] = ld(w);
-    }
-#pragma unroll
-    for (int u = 0; u < kStage; ++u) {
-      const int w = w0 + u * blockDim.x;
-      if (w < total) st(w, v[u]);
-    }
-  }
-}
-
 // ------------------------------------------------------------------ x pass
-enum { PRO_PLAIN = 0, PRO_CORR = 1, PRO_PROD = 2 };
 
 // Forward real transform along x of ny*nz lines. Output: 2*DFT_x in the half
 // spectrum (nxh, ny, nz).
@@ -334,14 +90,7 @@ __global__ void __launch_bounds__(kThreads) k_x_r2c(Grid g, FftAxis ax, const C2
   }
 }
 
-enum { EPI_STORE = 0, EPI_POT4 = 1 };
 
-template <typename R>
-struct Pot4Args {
-  const R* dencg;
-  const R* den;
-  Functional fn;
-};
 
 // Inverse real transform along x (unnormalised c2r convention). EPI_POT4:
 // the spectrum holds delj4 + the correlation convolution; the epilogue adds
@@ -433,10 +182,6 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
 }
 
 // ------------------------------------------------------------- y / z passes
-template <typename R>
-struct SpecList {
-  C2<R>* p[4];
-};
 
 // In-place transform along y of the spectra in `specs` (blockIdx.z picks one).
 template <typename R, int SIGN>
@@ -472,11 +217,6 @@ __global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> 
   }
 }
 
-template <typename R>
-struct FactorList {
-  const R* f[3];
-  C2<R>* out[3];
-};
 
 // Forward z transform, product with each factor table (times scale), inverse
 // z transform; output 0 may alias the input. `add` (nullable) is a spectrum
@@ -549,24 +289,6 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   }
 }
 
-// Raises a kernel's dynamic shared-memory limit once per (kernel, device) to
-// the largest size requested so far, so that no attribute call happens
-// while a step is being captured into a graph.
-template <typename K>
-void set_smem(K kernel, size_t bytes) {
-  if (bytes <= 48 * 1024) return;
-  static std::mutex mu;
-  static std::map<std::pair<const void*, int>, size_t> done;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  std::lock_guard<std::mutex> lock(mu);
-  size_t& cur = done[{reinterpret_cast<const void*>(kernel), dev}];
-  if (bytes > cur) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    cur = bytes;
-  }
-}
-
 template <typename R>
 const C2<R>* twx_of(const FftPlan& p);
 template <>
@@ -594,6 +316,7 @@ size_t smem_of(int pass, const FftPlan& p, int tile) {
 
 template <typename R, int PRO>
 void launch_r2c(const Grid& g, const FftPlan& p, const R* a, const R* b, R c0, R c1, C2<R>* out, cudaStream_t s) {
+  if ((p.tiles.engine & ENGINE_R2C) && reg_r2c<R>(g, p, twx_of<R>(p), PRO, a, b, c0, c1, out, s)) return;
   const int lpb = p.tiles.lpb_r2c;
   const size_t smem = smem_of<R>(PASS_R2C, p, lpb);
   set_smem(k_x_r2c<R, PRO>, smem);
@@ -604,6 +327,7 @@ void launch_r2c(const Grid& g, const FftPlan& p, const R* a, const R* b, R c0, R
 
 template <typename R>
 void y_impl(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int sign, cudaStream_t s) {
+  if ((p.tiles.engine & ENGINE_Y) && reg_y<R>(g, p, specs, nspec, sign, s)) return;
   const int ltx = p.tiles.ltx_y;
   const int TX = 1 << ltx;
   SpecList<R> sl{};
@@ -622,6 +346,7 @@ void y_impl(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int 
 template <typename R>
 void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors,
                 int nout, double scale, const void* add, cudaStream_t s) {
+  if ((p.tiles.engine & ENGINE_Z) && reg_z<R>(g, p, in, outs, factors, nout, scale, add, s)) return;
   const int ltx = p.tiles.ltx_z;
   const int TX = 1 << ltx;
   FactorList<R> fl{};
@@ -638,29 +363,32 @@ void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* ou
 
 template <typename R>
 void c2r_impl(const Grid& g, const FftPlan& p, const void* const* ins, void* const* outs, int nspec, cudaStream_t s) {
-  const int lpb = p.tiles.lpb_c2r;
-  const size_t smem = smem_of<R>(PASS_C2R, p, lpb);
-  set_smem(k_x_c2r<R, EPI_STORE>, smem);
-  const long long nlines = (long long)g.ny * g.nz;
-  dim3 grid((unsigned)((nlines + lpb - 1) / lpb), nspec);
   Pot4Args<R> pa{};
   const C2<R>* i0 = static_cast<const C2<R>*>(ins[0]);
   const C2<R>* i1 = nspec > 1 ? static_cast<const C2<R>*>(ins[1]) : i0;
   R* o0 = static_cast<R*>(outs[0]);
   R* o1 = nspec > 1 ? static_cast<R*>(outs[1]) : o0;
+  if ((p.tiles.engine & ENGINE_C2R) && reg_c2r<R>(g, p, twx_of<R>(p), EPI_STORE, i0, i1, o0, o1, nspec, pa, s)) return;
+  const int lpb = p.tiles.lpb_c2r;
+  const size_t smem = smem_of<R>(PASS_C2R, p, lpb);
+  set_smem(k_x_c2r<R, EPI_STORE>, smem);
+  const long long nlines = (long long)g.ny * g.nz;
+  dim3 grid((unsigned)((nlines + lpb - 1) / lpb), nspec);
   k_x_c2r<R, EPI_STORE><<<grid, kThreads, smem, s>>>(g, p.xh, twx_of<R>(p), i0, i1, o0, o1, pa, lpb);
 }
 
 template <typename R>
 void pot4_impl(const Grid& g, const FftPlan& p, const void* conv, const void* dencg, const void* den,
                const Functional& fn, void* pot4, cudaStream_t s) {
+  Pot4Args<R> pa{static_cast<const R*>(dencg), static_cast<const R*>(den), fn};
+  const C2<R>* c = static_cast<const C2<R>*>(conv);
+  R* o = static_cast<R*>(pot4);
+  if ((p.tiles.engine & ENGINE_C2R) && reg_c2r<R>(g, p, twx_of<R>(p), EPI_POT4, c, c, o, o, 1, pa, s)) return;
   const int lpb = p.tiles.lpb_c2r;
   const size_t smem = smem_of<R>(PASS_C2R, p, lpb);
   set_smem(k_x_c2r<R, EPI_POT4>, smem);
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + lpb - 1) / lpb), 1);
-  Pot4Args<R> pa{static_cast<const R*>(dencg), static_cast<const R*>(den), fn};
-  const C2<R>* c = static_cast<const C2<R>*>(conv);
   k_x_c2r<R, EPI_POT4><<<grid, kThreads, smem, s>>>(g, p.xh, twx_of<R>(p), c, c, static_cast<R*>(pot4),
                                                     static_cast<R*>(pot4), pa, lpb);
 }
@@ -741,6 +469,16 @@ void prepare_impl(const FftPlan& p) {
   set_smem(k_z_conv<R>, smem_of<R>(PASS_Z, p, p.tiles.ltx_z));
   set_smem(k_x_c2r<R, EPI_STORE>, c2r);
   set_smem(k_x_c2r<R, EPI_POT4>, c2r);
+  // the register engine's kernels (no launch)
+  Grid g{};
+  void* sp[1] = {nullptr};
+  const void* f[1] = {nullptr};
+  Pot4Args<R> pa{};
+  for (int pro : {PRO_PLAIN, PRO_CORR, PRO_PROD})
+    reg_r2c<R>(g, p, nullptr, pro, nullptr, nullptr, (R)0, (R)0, nullptr, nullptr, false);
+  for (int sign : {-1, 1}) reg_y<R>(g, p, sp, 1, sign, nullptr, false);
+  reg_z<R>(g, p, nullptr, sp, f, 1, 1.0, nullptr, nullptr, false);
+  for (int epi : {EPI_STORE, EPI_POT4}) reg_c2r<R>(g, p, nullptr, epi, nullptr, nullptr, nullptr, nullptr, 1, pa, nullptr, false);
 }
 }  // namespace
 
@@ -749,6 +487,14 @@ void fft_prepare(int prec, const FftPlan& p) {
     prepare_impl<double>(p);
   else
     prepare_impl<float>(p);
+}
+
+int fft_reg_engines(const FftPlan& p) {
+  int e = 0;
+  if (fft_reg_supported(p.xh.n)) e |= ENGINE_R2C | ENGINE_C2R;
+  if (fft_reg_supported(p.y.n)) e |= ENGINE_Y;
+  if (fft_reg_supported(p.z.n)) e |= ENGINE_Z;
+  return e;
 }
 
 FftTiles fft_default_tiles(int prec, const FftPlan& p) {
@@ -764,6 +510,7 @@ FftTiles fft_default_tiles(int prec, const FftPlan& p) {
   while (t.lpb_c2r > 1 && !fft_smem_bytes(prec, PASS_C2R, p, t.lpb_c2r)) t.lpb_c2r >>= 1;
   while (t.ltx_y > 0 && !fft_smem_bytes(prec, PASS_Y, p, t.ltx_y)) --t.ltx_y;
   while (t.ltx_z > 0 && !fft_smem_bytes(prec, PASS_Z, p, t.ltx_z)) --t.ltx_z;
+  t.engine = fft_reg_engines(p);
   return t;
 }
 

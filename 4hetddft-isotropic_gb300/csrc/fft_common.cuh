@@ -1,0 +1,485 @@
+// fft_common.cuh — device helpers shared by the FFT line passes: complex
+// arithmetic on double2/float2, the radix-2/3/4/5/8 butterflies, the
+// shared-memory Stockham passes of the generic kernels (fft.cu) and the
+// compile-time register DFTs of the specialised kernels (fft_reg.cu).
+#pragma once
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "he4g_internal.cuh"
+
+namespace he4g {
+
+constexpr int kThreads = 256;
+
+template <typename R>
+struct Cx;
+// kTile: kx columns per y/z block (128-byte rows). kPad: shared-memory lines
+// get one padding element per 128 bytes (element i sits at i + (i >> kPad)),
+// which spreads the strided writes of the Stockham passes over all banks.
+template <>
+struct Cx<double> {
+  using T = double2;
+  static constexpr int kTile = 8;
+  static constexpr int kPad = 3;
+};
+template <>
+struct Cx<float> {
+  using T = float2;
+  static constexpr int kTile = 8;
+  static constexpr int kPad = 4;
+};
+template <typename R>
+using C2 = typename Cx<R>::T;
+
+template <typename R>
+__device__ __forceinline__ int pidx(int i) {
+  return i + (i >> Cx<R>::kPad);
+}
+// shared-memory stride of a line holding n elements
+template <typename R>
+__host__ __device__ constexpr int padded_len(int n) {
+  return n + (n >> Cx<R>::kPad) + 1;
+}
+
+template <typename R>
+__device__ __forceinline__ C2<R> mk(R x, R y) {
+  C2<R> c;
+  c.x = x;
+  c.y = y;
+  return c;
+}
+template <typename R>
+__device__ __forceinline__ C2<R> cadd(C2<R> a, C2<R> b) { return mk<R>(a.x + b.x, a.y + b.y); }
+template <typename R>
+__device__ __forceinline__ C2<R> csub(C2<R> a, C2<R> b) { return mk<R>(a.x - b.x, a.y - b.y); }
+template <typename R>
+__device__ __forceinline__ C2<R> cconj(C2<R> a) { return mk<R>(a.x, -a.y); }
+
+// a * w (SIGN < 0) or a * conj(w) (SIGN > 0)
+template <typename R, int SIGN>
+__device__ __forceinline__ C2<R> mulw(C2<R> a, C2<R> w) {
+  if (SIGN < 0) return mk<R>(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
+  return mk<R>(fma(a.x, w.x, a.y * w.y), fma(a.y, w.x, -a.x * w.y));
+}
+// a * (SIGN * i)
+template <typename R, int SIGN>
+__device__ __forceinline__ C2<R> jmul(C2<R> a) {
+  return SIGN < 0 ? mk<R>(a.y, -a.x) : mk<R>(-a.y, a.x);
+}
+
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf2(C2<R>* v) {
+  C2<R> t = v[0];
+  v[0] = cadd<R>(t, v[1]);
+  v[1] = csub<R>(t, v[1]);
+}
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf4(C2<R>& a0, C2<R>& a1, C2<R>& a2, C2<R>& a3) {
+  C2<R> t0 = cadd<R>(a0, a2), t1 = csub<R>(a0, a2);
+  C2<R> t2 = cadd<R>(a1, a3), t3 = jmul<R, SIGN>(csub<R>(a1, a3));
+  a0 = cadd<R>(t0, t2);
+  a2 = csub<R>(t0, t2);
+  a1 = cadd<R>(t1, t3);
+  a3 = csub<R>(t1, t3);
+}
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf8(C2<R>* v) {
+  const R r = (R)0.70710678118654752440;
+  C2<R> a0 = v[0], a1 = v[2], a2 = v[4], a3 = v[6];
+  C2<R> b0 = v[1], b1 = v[3], b2 = v[5], b3 = v[7];
+  bf4<R, SIGN>(a0, a1, a2, a3);
+  bf4<R, SIGN>(b0, b1, b2, b3);
+  if (SIGN < 0) {
+    b1 = mk<R>((b1.x + b1.y) * r, (b1.y - b1.x) * r);
+    b3 = mk<R>((b3.y - b3.x) * r, -(b3.x + b3.y) * r);
+  } else {
+    b1 = mk<R>((b1.x - b1.y) * r, (b1.y + b1.x) * r);
+    b3 = mk<R>(-(b3.x + b3.y) * r, (b3.x - b3.y) * r);
+  }
+  b2 = jmul<R, SIGN>(b2);
+  v[0] = cadd<R>(a0, b0);
+  v[4] = csub<R>(a0, b0);
+  v[1] = cadd<R>(a1, b1);
+  v[5] = csub<R>(a1, b1);
+  v[2] = cadd<R>(a2, b2);
+  v[6] = csub<R>(a2, b2);
+  v[3] = cadd<R>(a3, b3);
+  v[7] = csub<R>(a3, b3);
+}
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf3(C2<R>* v) {
+  const R s3 = (R)0.86602540378443864676;  // sin(2 pi / 3)
+  C2<R> b = cadd<R>(v[1], v[2]);
+  C2<R> d = csub<R>(v[1], v[2]);
+  C2<R> t = mk<R>(fma((R)-0.5, b.x, v[0].x), fma((R)-0.5, b.y, v[0].y));
+  C2<R> s = jmul<R, SIGN>(mk<R>(s3 * d.x, s3 * d.y));
+  v[0] = cadd<R>(v[0], b);
+  v[1] = cadd<R>(t, s);
+  v[2] = csub<R>(t, s);
+}
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf5(C2<R>* v) {
+  const R c1 = (R)0.30901699437494742410, c2 = (R)-0.80901699437494742410;  // cos(2pi/5), cos(4pi/5)
+  const R s1 = (R)0.95105651629515357212, s2 = (R)0.58778525229247312917;   // sin(2pi/5), sin(4pi/5)
+  C2<R> b1 = cadd<R>(v[1], v[4]), b2 = cadd<R>(v[2], v[3]);
+  C2<R> d1 = csub<R>(v[1], v[4]), d2 = csub<R>(v[2], v[3]);
+  C2<R> a0 = v[0];
+  C2<R> t1 = mk<R>(fma(c2, b2.x, fma(c1, b1.x, a0.x)), fma(c2, b2.y, fma(c1, b1.y, a0.y)));
+  C2<R> t2 = mk<R>(fma(c1, b2.x, fma(c2, b1.x, a0.x)), fma(c1, b2.y, fma(c2, b1.y, a0.y)));
+  C2<R> u1 = mk<R>(fma(s2, d2.x, s1 * d1.x), fma(s2, d2.y, s1 * d1.y));
+  C2<R> u2 = mk<R>(fma(-s1, d2.x, s2 * d1.x), fma(-s1, d2.y, s2 * d1.y));
+  u1 = jmul<R, SIGN>(u1);
+  u2 = jmul<R, SIGN>(u2);
+  v[0] = mk<R>(a0.x + b1.x + b2.x, a0.y + b1.y + b2.y);
+  v[1] = cadd<R>(t1, u1);
+  v[4] = csub<R>(t1, u1);
+  v[2] = cadd<R>(t2, u2);
+  v[3] = csub<R>(t2, u2);
+}
+
+template <typename R, int RAD, int SIGN>
+__device__ __forceinline__ void butterfly(C2<R>* v) {
+  if (RAD == 2) bf2<R, SIGN>(v);
+  if (RAD == 3) bf3<R, SIGN>(v);
+  if (RAD == 4) bf4<R, SIGN>(v[0], v[1], v[2], v[3]);
+  if (RAD == 5) bf5<R, SIGN>(v);
+  if (RAD == 8) bf8<R, SIGN>(v);
+}
+
+template <typename R>
+__device__ __forceinline__ const C2<R>* twiddles(const FftAxis& ax);
+template <>
+__device__ __forceinline__ const double2* twiddles<double>(const FftAxis& ax) {
+  return ax.tw;
+}
+template <>
+__device__ __forceinline__ const float2* twiddles<float>(const FftAxis& ax) {
+  return ax.twf;
+}
+
+// One Stockham pass of radix RAD over `nlines` lines of length n held in
+// shared memory at src + l*ld (natural order in, autosorted order out).
+// w / d by multiply-high (mag = ceil(2^32/d); mag == 0 marks d == 1)
+__device__ __forceinline__ int mdiv(int w, unsigned mag) { return mag ? (int)__umulhi((unsigned)w, mag) : w; }
+
+// tw points to the n twiddles of the axis staged in shared memory.
+template <typename R, int RAD, int SIGN>
+__device__ __forceinline__ void stockham_pass(const C2<R>* __restrict__ src, C2<R>* __restrict__ dst, int n,
+                                              int ns, int nlines, int ld, const C2<R>* __restrict__ tw,
+                                              unsigned mag_nr, unsigned mag_ns) {
+  const int nr = n / RAD;
+  const int tstep = n / (ns * RAD);
+  const int total = nlines * nr;
+  for (int w = threadIdx.x; w < total; w += blockDim.x) {
+    const int l = mdiv(w, mag_nr);
+    const int j = w - l * nr;
+    const int q = mdiv(j, mag_ns);
+    const int k = j - q * ns;
+    const C2<R>* s = src + l * ld;
+    C2<R> v[RAD];
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) v[r] = s[pidx<R>(j + r * nr)];
+    if (k > 0) {
+#pragma unroll
+      for (int r = 1; r < RAD; ++r) v[r] = mulw<R, SIGN>(v[r], tw[r * k * tstep]);
+    }
+    butterfly<R, RAD, SIGN>(v);
+    const int idx = q * ns * RAD + k;
+    C2<R>* d = dst + l * ld;
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) d[pidx<R>(idx + r * ns)] = v[r];
+  }
+}
+
+// Copies the axis' n twiddles into shared memory (caller syncs).
+template <typename R>
+__device__ __forceinline__ void stage_twiddles(C2<R>* tws, const FftAxis& ax) {
+  const C2<R>* tw = twiddles<R>(ax);
+  for (int t = threadIdx.x; t < ax.n; t += blockDim.x) tws[t] = __ldg(&tw[t]);
+}
+
+// Full transform of nlines lines; a holds the input, b is scratch, tws the
+// staged twiddles; returns the buffer that holds the result. Ends with a
+// barrier.
+template <typename R, int SIGN>
+__device__ C2<R>* fft_smem(C2<R>* a, C2<R>* b, int nlines, int ld, const FftAxis& ax, const C2<R>* tws) {
+  int ns = 1;
+  for (int f = 0; f < ax.nf; ++f) {
+    const int rad = ax.fac[f];
+    const unsigned mnr = ax.mag_nr[f], mns = ax.mag_ns[f];
+    if (rad == 8)
+      stockham_pass<R, 8, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
+    else if (rad == 4)
+      stockham_pass<R, 4, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
+    else if (rad == 2)
+      stockham_pass<R, 2, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
+    else if (rad == 3)
+      stockham_pass<R, 3, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
+    else
+      stockham_pass<R, 5, SIGN>(a, b, ax.n, ns, nlines, ld, tws, mnr, mns);
+    __syncthreads();
+    C2<R>* t = a;
+    a = b;
+    b = t;
+    ns *= rad;
+  }
+  return a;
+}
+
+template <typename R>
+__device__ __forceinline__ C2<R> ld_pair(const R* p) {
+  return __ldg(reinterpret_cast<const C2<R>*>(p));
+}
+
+// Block-strided loop over w < total that issues the global loads of kStage
+// iterations (ld(w)) before consuming any of them (st(w, value)), so that
+// each thread keeps kStage loads in flight instead of one.
+constexpr int kStage = 8;
+template <typename LD, typename ST>
+__device__ __forceinline__ void staged_loop(int total, LD ld, ST st) {
+  for (int w0 = threadIdx.x; w0 < total; w0 += kStage * blockDim.x) {
+    decltype(ld(0)) v[kStage];
+#pragma unroll
+    for (int u = 0; u < kStage; ++u) {
+      const int w = w0 + u * blockDim.x;
+      if (w < total) v[u] = ld(w);
+    }
+#pragma unroll
+    for (int u = 0; u < kStage; ++u) {
+      const int w = w0 + u * blockDim.x;
+      if (w < total) st(w, v[u]);
+    }
+  }
+}
+
+
+// ------------------------------------------------- compile-time register DFTs
+// cos and sin of 2*pi*e/m at compile time: quadrant reduction with integer
+// arithmetic, a reflection to [0, pi/4], and the Taylor series to the x^26
+// term there (truncation below 1e-24).
+__host__ __device__ constexpr double taylor_cos(double x) {
+  double term = 1.0, sum = 1.0;
+  for (int n = 1; n <= 13; ++n) {
+    term *= -x * x / ((2 * n - 1) * (2 * n));
+    sum += term;
+  }
+  return sum;
+}
+__host__ __device__ constexpr double taylor_sin(double x) {
+  double term = x, sum = x;
+  for (int n = 1; n <= 13; ++n) {
+    term *= -x * x / ((2 * n) * (2 * n + 1));
+    sum += term;
+  }
+  return sum;
+}
+// returns cos (sel 0) or sin (sel 1) of 2 pi e / m
+__host__ __device__ constexpr double cs2pi(int e, int m, int sel) {
+  e %= m;
+  if (e < 0) e += m;
+  const int q = (4 * e) / m;      // quadrant
+  const int r = 4 * e - q * m;    // angle within it: (pi/2) r/m
+  const double half_pi = 1.57079632679489661923;
+  double c = 0.0, s = 0.0;
+  if (2 * r <= m) {
+    c = taylor_cos(half_pi * r / m);
+    s = taylor_sin(half_pi * r / m);
+  } else {
+    c = taylor_sin(half_pi * (m - r) / m);
+    s = taylor_cos(half_pi * (m - r) / m);
+  }
+  double cq = c, sq = s;
+  if (q == 1) {
+    cq = -s;
+    sq = c;
+  } else if (q == 2) {
+    cq = -c;
+    sq = -s;
+  } else if (q == 3) {
+    cq = s;
+    sq = -c;
+  }
+  return sel == 0 ? cq : sq;
+}
+
+// compile-time loop: f(std::integral_constant<int, i>) for i < N
+template <typename F, int... Is>
+__device__ __forceinline__ void sfor_impl(F&& f, std::integer_sequence<int, Is...>) {
+  (f(std::integral_constant<int, Is>{}), ...);
+}
+template <int N, typename F>
+__device__ __forceinline__ void sfor(F&& f) {
+  sfor_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+// a * W_M^E with W_M = exp(-2 pi i / M) (SIGN < 0) or its conjugate
+// (SIGN > 0); multiples of pi/4 cost no general complex product.
+template <typename R, int M, int E, int SIGN>
+__device__ __forceinline__ C2<R> twc(C2<R> a) {
+  constexpr int e = E % M;
+  constexpr R r = (R)0.70710678118654752440;
+  if constexpr (e == 0) {
+    return a;
+  } else if constexpr (2 * e == M) {
+    return mk<R>(-a.x, -a.y);
+  } else if constexpr (4 * e == M) {
+    return jmul<R, SIGN>(a);
+  } else if constexpr (4 * e == 3 * M) {
+    return jmul<R, -SIGN>(a);
+  } else if constexpr (8 * e == M) {  // (1 - i)/sqrt2, conj for SIGN > 0
+    return SIGN < 0 ? mk<R>((a.x + a.y) * r, (a.y - a.x) * r) : mk<R>((a.x - a.y) * r, (a.y + a.x) * r);
+  } else if constexpr (8 * e == 3 * M) {  // (-1 - i)/sqrt2
+    return SIGN < 0 ? mk<R>((a.y - a.x) * r, -(a.x + a.y) * r) : mk<R>(-(a.x + a.y) * r, (a.x - a.y) * r);
+  } else if constexpr (8 * e == 5 * M) {  // (-1 + i)/sqrt2
+    return SIGN < 0 ? mk<R>(-(a.x + a.y) * r, (a.x - a.y) * r) : mk<R>((a.y - a.x) * r, -(a.x + a.y) * r);
+  } else if constexpr (8 * e == 7 * M) {  // (1 + i)/sqrt2
+    return SIGN < 0 ? mk<R>((a.x - a.y) * r, (a.y + a.x) * r) : mk<R>((a.x + a.y) * r, (a.y - a.x) * r);
+  } else {
+    constexpr R c = (R)cs2pi(e, M, 0), s = (R)cs2pi(e, M, 1);
+    return mulw<R, SIGN>(a, mk<R>(c, -s));
+  }
+}
+
+// In-place DFT of M values held in registers, output in natural order.
+// Radices 2, 3, 4, 5 and 8 use the butterflies; composite sizes split
+// M = A*B (Cooley-Tukey, n = B*n1 + n2, k = k1 + A*k2) with compile-time
+// indices and twiddles.
+template <typename R, int M, int SIGN>
+struct RegDft;
+
+template <typename R, int A, int B, int SIGN>
+__device__ __forceinline__ void reg_ct(C2<R>* v) {
+  constexpr int M = A * B;
+  C2<R> y[M];
+  sfor<B>([&](auto n2c) {
+    constexpr int n2 = decltype(n2c)::value;
+    C2<R> t[A];
+    sfor<A>([&](auto n1c) {
+      constexpr int n1 = decltype(n1c)::value;
+      t[n1] = v[B * n1 + n2];
+    });
+    RegDft<R, A, SIGN>::run(t);
+    sfor<A>([&](auto k1c) {
+      constexpr int k1 = decltype(k1c)::value;
+      y[k1 * B + n2] = twc<R, M, n2 * k1, SIGN>(t[k1]);
+    });
+  });
+  sfor<A>([&](auto k1c) {
+    constexpr int k1 = decltype(k1c)::value;
+    C2<R> t[B];
+    sfor<B>([&](auto n2c) {
+      constexpr int n2 = decltype(n2c)::value;
+      t[n2] = y[k1 * B + n2];
+    });
+    RegDft<R, B, SIGN>::run(t);
+    sfor<B>([&](auto k2c) {
+      constexpr int k2 = decltype(k2c)::value;
+      v[k1 + A * k2] = t[k2];
+    });
+  });
+}
+
+template <typename R, int SIGN>
+struct RegDft<R, 1, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>*) {}
+};
+template <typename R, int SIGN>
+struct RegDft<R, 2, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { bf2<R, SIGN>(v); }
+};
+template <typename R, int SIGN>
+struct RegDft<R, 3, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { bf3<R, SIGN>(v); }
+};
+template <typename R, int SIGN>
+struct RegDft<R, 4, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { bf4<R, SIGN>(v[0], v[1], v[2], v[3]); }
+};
+template <typename R, int SIGN>
+struct RegDft<R, 5, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { bf5<R, SIGN>(v); }
+};
+template <typename R, int SIGN>
+struct RegDft<R, 8, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { bf8<R, SIGN>(v); }
+};
+template <typename R, int SIGN>
+struct RegDft<R, 6, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { reg_ct<R, 2, 3, SIGN>(v); }
+};
+template <typename R, int SIGN>
+struct RegDft<R, 10, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { reg_ct<R, 2, 5, SIGN>(v); }
+};
+template <typename R, int SIGN>
+struct RegDft<R, 12, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { reg_ct<R, 4, 3, SIGN>(v); }
+};
+template <typename R, int SIGN>
+struct RegDft<R, 16, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { reg_ct<R, 4, 4, SIGN>(v); }
+};
+template <typename R, int SIGN>
+struct RegDft<R, 20, SIGN> {
+  static __device__ __forceinline__ void run(C2<R>* v) { reg_ct<R, 4, 5, SIGN>(v); }
+};
+
+enum { PRO_PLAIN = 0, PRO_CORR = 1, PRO_PROD = 2 };
+
+enum { EPI_STORE = 0, EPI_POT4 = 1 };
+
+template <typename R>
+struct Pot4Args {
+  const R* dencg;
+  const R* den;
+  Functional fn;
+};
+
+template <typename R>
+struct SpecList {
+  C2<R>* p[4];
+};
+
+template <typename R>
+struct FactorList {
+  const R* f[3];
+  C2<R>* out[3];
+};
+
+// Raises a kernel's dynamic shared-memory limit once per (kernel, device) to
+// the largest size requested so far, so that no attribute call happens
+// while a step is being captured into a graph.
+template <typename K>
+void set_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return;
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = done[{reinterpret_cast<const void*>(kernel), dev}];
+  if (bytes > cur) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cur = bytes;
+  }
+}
+
+// register engine (fft_reg.cu): each returns false when the length has no
+// specialisation, and launches nothing then; launch == false only raises
+// the kernel's shared-memory limit
+template <typename R>
+bool reg_y(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int sign, cudaStream_t s,
+           bool launch = true);
+template <typename R>
+bool reg_z(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors, int nout,
+           double scale, const void* add, cudaStream_t s, bool launch = true);
+template <typename R>
+bool reg_r2c(const Grid& g, const FftPlan& p, const C2<R>* twx, int pro, const R* a, const R* b, R c0, R c1,
+             C2<R>* out, cudaStream_t s, bool launch = true);
+template <typename R>
+bool reg_c2r(const Grid& g, const FftPlan& p, const C2<R>* twx, int epi, const C2<R>* i0, const C2<R>* i1, R* o0,
+             R* o1, int nspec, const Pot4Args<R>& pa, cudaStream_t s, bool launch = true);
+
+}  // namespace he4g

@@ -82,11 +82,15 @@ struct ImpState {
 constexpr int kRingRows = 8192;
 constexpr int kRingCols = 10;
 
-// Tile shapes of the line passes, chosen per run (he4g_autotune):
-// lines per block of the x passes, log2 of the kx columns per y/z block.
+// Tile shapes of the line passes, chosen per run (he4g_autotune): lines per
+// block of the generic x passes, log2 of the kx columns per generic y/z
+// block, and which passes run on the register engine (ENGINE_* bits; only
+// lengths with a specialisation, see fft_reg_supported).
+enum { ENGINE_R2C = 1, ENGINE_C2R = 2, ENGINE_Y = 4, ENGINE_Z = 8 };
 struct FftTiles {
   int lpb_r2c, lpb_c2r;
   int ltx_y, ltx_z;
+  int engine;
 };
 
 struct FftPlan {
@@ -107,6 +111,10 @@ size_t fft_smem_bytes(int prec, int pass, const FftPlan& p, int tile);
 FftTiles fft_default_tiles(int prec, const FftPlan& p);
 // raises the kernels' shared-memory limits for p.tiles (outside any capture)
 void fft_prepare(int prec, const FftPlan& p);
+// true when the register engine has a specialisation for length n
+bool fft_reg_supported(int n);
+// ENGINE_* bits of the passes whose lengths the register engine supports
+int fft_reg_engines(const FftPlan& p);
 
 // ------------------------------------------------- FFT passes (fft.cu)
 // prec: HE4G_PREC_FP64 (double fields, double2 spectra) or HE4G_PREC_MIXED

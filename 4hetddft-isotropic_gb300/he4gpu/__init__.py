@@ -16,6 +16,9 @@ from .initial import (PS_TO_K, KELVIN_PER_PS, woods_saxon_psi, collision_case,  
                       config_for_case, make_meta, state_for, batch_cases, serve_stream)
 
 
+NTILES = 5  # HE4G_NTILES
+
+
 class He4gError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"he4g error {code} ({abi.ERRORS.get(code, '?')}): {msg}")
@@ -144,22 +147,24 @@ class Run:
         self._ck(self.lib.he4g_enable_graphs(self.h, 1 if on else 0))
 
     def autotune(self, reps=5):
-        """Time every FFT tile shape on this run's buffers and keep the fastest.
+        """Time every FFT tile shape and engine on this run's buffers and keep
+        the fastest.
 
-        Returns (lpb_r2c, lpb_c2r, log2 cols y, log2 cols z)."""
-        t = (C.c_int * 4)()
+        Returns (lpb_r2c, lpb_c2r, log2 cols y, log2 cols z, register-engine
+        bits: 1 forward x, 2 inverse x, 4 y, 8 z)."""
+        t = (C.c_int * NTILES)()
         self._ck(self.lib.he4g_autotune(self.h, reps, t))
         return tuple(t)
 
     @property
     def tiles(self):
-        t = (C.c_int * 4)()
+        t = (C.c_int * NTILES)()
         self._ck(self.lib.he4g_get_tiles(self.h, t))
         return tuple(t)
 
     @tiles.setter
     def tiles(self, value):
-        t = (C.c_int * 4)(*[int(v) for v in value])
+        t = (C.c_int * NTILES)(*[int(v) for v in value])
         self._ck(self.lib.he4g_set_tiles(self.h, t))
 
     def energy(self):

@@ -218,20 +218,27 @@ int he4g_enable_graphs(he4g_run* run, int on);
  * Returns the first error of any run. */
 int he4g_step_many(he4g_run** runs, int n, int nsteps);
 
-/* Tile shapes of the FFT line passes: tiles[0] lines per block of the
- * forward x pass, tiles[1] of the inverse x pass, tiles[2] log2 of the kx
- * columns per block of the y pass, tiles[3] of the fused z convolution.
- * No reference counterpart (FFTW picks its own plans in fft.f90:5-153).
+/* Tile shapes of the FFT line passes, HE4G_NTILES ints: tiles[0] lines per
+ * block of the generic forward x pass, tiles[1] of the generic inverse x
+ * pass, tiles[2] log2 of the kx columns per block of the generic y pass,
+ * tiles[3] of the generic fused z convolution, tiles[4] the passes that run
+ * on the register engine instead (bits 1 forward x, 2 inverse x, 4 y, 8 z;
+ * only for lengths it is specialised for: 16, 20, 24, 32, 40, 48, 64, 80, 96,
+ * 128, 160, 192, 256). No reference counterpart (FFTW picks its own plans in
+ * fft.f90:5-153).
  *
- * he4g_autotune times every shape that fits in shared memory for each pass
- * on this run's own buffers (reps timed launches each, 0 = 5) and keeps the
- * fastest; tiles (nullable) receives the choice. Results do not depend on
- * the tiles: every line goes through the same arithmetic. It overwrites the
- * run's scratch spectra only, and drops captured step graphs. Runs on one
- * grid can share one tuning through he4g_get_tiles / he4g_set_tiles. */
-int he4g_autotune(he4g_run* run, int reps, int tiles[4]);
-int he4g_get_tiles(const he4g_run* run, int tiles[4]);
-int he4g_set_tiles(he4g_run* run, const int tiles[4]);
+ * he4g_autotune times, for each pass, every generic shape that fits in
+ * shared memory and the register engine, on this run's own buffers (reps
+ * timed launches each, 0 = 5), and keeps the fastest; tiles (nullable)
+ * receives the choice. Generic shapes change timing only (every line goes
+ * through the same arithmetic); the two engines agree to rounding. It
+ * overwrites the run's scratch spectra only, and drops captured step
+ * graphs. Runs on one grid can share one tuning through he4g_get_tiles /
+ * he4g_set_tiles. */
+#define HE4G_NTILES 5
+int he4g_autotune(he4g_run* run, int reps, int tiles[HE4G_NTILES]);
+int he4g_get_tiles(const he4g_run* run, int tiles[HE4G_NTILES]);
+int he4g_set_tiles(he4g_run* run, const int tiles[HE4G_NTILES]);
 
 /* Kernel launches issued by this run since it was created. */
 long long he4g_launch_count(const he4g_run* run);

@@ -8,7 +8,7 @@ bit: a collision's result is the same alone and in the mix.
 import numpy as np
 import pytest
 
-from helpers import gpu_run, make_case
+from helpers import gpu_run, make_case, rel_field
 
 pytestmark = pytest.mark.gpu
 
@@ -48,28 +48,55 @@ def test_runs_in_the_mix_match_runs_alone(precision):
         assert x.energy() == y.energy()
 
 
+@pytest.mark.parametrize("engine", [0, 15])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_autotuned_tiles_give_identical_results(precision):
-    """Every tile shape transforms each line with the same arithmetic."""
+def test_tile_shapes_give_identical_results(precision, engine):
+    """Every generic tile shape transforms each line with the same arithmetic."""
     cfg, tk, psi, r, v, meta = make_case("he200_xe_40x48x64", precision=precision)
-    a = gpu_run(cfg, tk, psi, r, v)
-    default = a.tiles
-    b = gpu_run(cfg, tk, psi, r, v)
-    tuned = b.autotune(reps=2)
-    assert b.tiles == tuned
-    # force a shape different from the default in every pass
-    c = gpu_run(cfg, tk, psi, r, v)
-    c.tiles = (1 if default[0] != 1 else 2, 3 if default[1] != 3 else 4,
-               0 if default[2] != 0 else 1, 1 if default[3] != 1 else 2)
-    for x in (a, b, c):
+    runs = []
+    for t in [(32, 32, 3, 3), (1, 3, 0, 1), (4, 64, 5, 2)]:
+        x = gpu_run(cfg, tk, psi, r, v)
+        x.tiles = t + (engine,)
         x.enable_graphs(True)
         x.step(8)
+        runs.append(x)
+    a = runs[0]
     ta = a.trajectory()  # rows since the last read: read each run once
     assert len(ta) == 8
-    for x in (b, c):
+    for x in runs[1:]:
         assert np.array_equal(a.psi, x.psi)
         assert np.array_equal(a.den, x.den)
         assert np.array_equal(ta, x.trajectory())
+
+
+@pytest.mark.parametrize("case", ["he100_xe_32", "he300_ar_48", "he200_xe_40x48x64"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_register_engine_matches_generic(case, precision):
+    """The specialised four-step kernels and the generic Stockham kernels
+    compute the same transforms; they differ by rounding only."""
+    cfg, tk, psi, r, v, meta = make_case(case, precision=precision)
+    a = gpu_run(cfg, tk, psi, r, v)
+    b = gpu_run(cfg, tk, psi, r, v)
+    assert a.tiles[4] == 15  # every length of these grids is specialised
+    b.tiles = b.tiles[:4] + (0,)
+    a.step(6)
+    b.step(6)
+    tol = 1e-12 if precision == 0 else 2e-5
+    assert rel_field(a.den, b.den) < tol
+    assert rel_field(a.field("pot4"), b.field("pot4")) < tol
+    assert np.max(np.abs(a.impurity()[0] - b.impurity()[0])) < 1e-9
+
+
+def test_autotune_keeps_a_valid_choice():
+    cfg, tk, psi, r, v, meta = make_case("he200_xe_40x48x64", precision=1)
+    b = gpu_run(cfg, tk, psi, r, v)
+    tuned = b.autotune(reps=2)
+    assert b.tiles == tuned
+    c = gpu_run(cfg, tk, psi, r, v)
+    c.tiles = tuned
+    b.step(5)
+    c.step(5)
+    assert np.array_equal(b.psi, c.psi)
 
 
 def test_set_tiles_rejects_out_of_range_shapes():
@@ -77,7 +104,7 @@ def test_set_tiles_rejects_out_of_range_shapes():
     cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
     a = gpu_run(cfg, tk, psi, r, v)
     before = a.tiles
-    for bad in [(0, 4, 3, 3), (4, 4, -1, 3), (4, 4, 3, 9), (4, 100, 3, 3)]:
+    for bad in [(0, 4, 3, 3, 0), (4, 4, -1, 3, 0), (4, 4, 3, 9, 0), (4, 100, 3, 3, 0), (4, 4, 3, 3, 16)]:
         with pytest.raises(he4gpu.He4gError):
             a.tiles = bad
     assert a.tiles == before
