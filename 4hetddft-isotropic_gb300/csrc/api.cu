@@ -288,7 +288,7 @@ bool radix_ok(int n) {
 // ----------------------------------------------------------------- pieces
 ImpTable imp_table(const he4g_run* r) {
   return ImpTable{r->xsf, r->ysf, r->zsf, static_cast<const float*>(r->potion), r->cfg.npot,
-                  static_cast<float>(1.0 / r->cfg.delinter)};
+                  static_cast<float>(1.0 / r->cfg.delinter), static_cast<float>(r->cfg.npot - 1)};
 }
 
 void potenimp_dev(he4g_run* r, int sel) {
@@ -488,7 +488,7 @@ void force_dev(he4g_run* r, int store_accel, int sel = 1, bool store_uimp = fals
       nb = r->fblocks;
     }
   }
-  Tick t(r, F_SCALAR);
+  Tick t(r, F_SCALAR, 1 + fold_launches(nb));
   launch_imp_force(r->imp, r->partials, nb, r->g.dxyz, r->mass, store_accel, r->s);
 }
 
@@ -628,7 +628,7 @@ void steppc_dev(he4g_run* r, double dt) {
   }
   roles_after_correct(r, psit);
   {
-    Tick t(r, F_SCALAR);
+    Tick t(r, F_SCALAR, 1 + fold_launches(r->pblocks));
     launch_imp_pc_correct(r->imp, r->partials, r->pblocks, dt, c9, static_cast<double>(r->g.n), r->s);
   }
 }

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(kThreads) k_x_r2c(Grid g, FftAxis ax, const C2
   const long long nlines = (long long)g.ny * g.nz;
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
-  staged_loop(
+  staged_loop<R>(
       nl * m,
       [&](int w) {
         const int l = w / m, j = w - l * m;
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
   const long long nlines = (long long)g.ny * g.nz;
   const long long l0 = (long long)blockIdx.x * lpb;
   const int nl = (int)min((long long)lpb, nlines - l0);
-  staged_loop(
+  staged_loop<R>(
       nl * (m + 1),
       [&](int w) {
         const int l = w / (m + 1), k = w - l * (m + 1);
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
   struct Pot4In {
     C2<R> cg, d;
   };
-  staged_loop(
+  staged_loop<R>(
       nl * m,
       [&](int w) {
         Pot4In in{};
@@ -170,10 +170,8 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
       if (fn.lsolid) {
         const C2<R> d = in.d;
         const R beta = (R)fn.beta_solid, dm = (R)fn.den_m, cs = (R)fn.c_solid;
-        const R t0 = tanh(beta * (d.x - dm));
-        const R t1 = tanh(beta * (d.y - dm));
-        p0 += cs * ((R)1 + t0 + beta * d.x * ((R)1 - t0 * t0));
-        p1 += cs * ((R)1 + t1 + beta * d.y * ((R)1 - t1 * t1));
+        p0 += solid_penalty<R>(d.x, beta, dm, cs);
+        p1 += solid_penalty<R>(d.y, beta, dm, cs);
       }
       v = mk<R>(p0, p1);
     }
@@ -197,7 +195,7 @@ __global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> 
   const int kx0 = blockIdx.x * TX;
   const int ncol = min(TX, g.nxh - kx0);
   const long long base = (long long)blockIdx.y * g.ny * g.nxh + kx0;
-  staged_loop(
+  staged_loop<R>(
       TX * n,
       [&](int w) {
         const int c = w & (TX - 1), j = w >> ltx;
@@ -236,7 +234,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   const int ncol = min(TX, g.nxh - kx0);
   const long long plane = (long long)g.ny * g.nxh;
   const long long base = (long long)blockIdx.y * g.nxh + kx0;
-  staged_loop(
+  staged_loop<R>(
       TX * n,
       [&](int w) {
         const int cc = w & (TX - 1), k = w >> ltx;
@@ -253,7 +251,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   C2<R>* s1 = fwd == a ? b : a;
   for (int o = 0; o < nout; ++o) {
     const R* fac = fl.f[o];
-    staged_loop(
+    staged_loop<R>(
         TX * n,
         [&](int w) {
           const int cc = w & (TX - 1), k = w >> ltx;
@@ -271,7 +269,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
     C2<R>* r = fft_smem<R, 1>(s1, c, ncol, ld, ax, tws);
     C2<R>* dst = fl.out[o];
     const C2<R>* addo = o == 0 ? add : nullptr;
-    staged_loop(
+    staged_loop<R>(
         TX * n,
         [&](int w) {
           const int cc = w & (TX - 1), k = w >> ltx;

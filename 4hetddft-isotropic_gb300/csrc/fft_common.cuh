@@ -233,25 +233,30 @@ __device__ __forceinline__ C2<R> ld_pair(const R* p) {
   return __ldg(reinterpret_cast<const C2<R>*>(p));
 }
 
-// Block-strided loop over w < total that issues the global loads of kStage
+// Block-strided loop over w < total that issues the global loads of S
 // iterations (ld(w)) before consuming any of them (st(w, value)), so that
-// each thread keeps kStage loads in flight instead of one.
-constexpr int kStage = 8;
-template <typename LD, typename ST>
-__device__ __forceinline__ void staged_loop(int total, LD ld, ST st) {
-  for (int w0 = threadIdx.x; w0 < total; w0 += kStage * blockDim.x) {
-    decltype(ld(0)) v[kStage];
+// each thread keeps S loads in flight instead of one. FP32 passes use S = 8;
+// the FP64 passes are bound by FP64 issue, and the extra registers of
+// staging cost them occupancy, so they use S = 1.
+template <int S, typename LD, typename ST>
+__device__ __forceinline__ void staged_loop_n(int total, LD ld, ST st) {
+  for (int w0 = threadIdx.x; w0 < total; w0 += S * blockDim.x) {
+    decltype(ld(0)) v[S];
 #pragma unroll
-    for (int u = 0; u < kStage; ++u) {
+    for (int u = 0; u < S; ++u) {
       const int w = w0 + u * blockDim.x;
       if (w < total) v[u] = ld(w);
     }
 #pragma unroll
-    for (int u = 0; u < kStage; ++u) {
+    for (int u = 0; u < S; ++u) {
       const int w = w0 + u * blockDim.x;
       if (w < total) st(w, v[u]);
     }
   }
+}
+template <typename R, typename LD, typename ST>
+__device__ __forceinline__ void staged_loop(int total, LD ld, ST st) {
+  staged_loop_n<sizeof(R) == 8 ? 1 : 8>(total, ld, st);
 }
 
 
@@ -425,6 +430,27 @@ template <typename R, int SIGN>
 struct RegDft<R, 20, SIGN> {
   static __device__ __forceinline__ void run(C2<R>* v) { reg_ct<R, 4, 5, SIGN>(v); }
 };
+
+// Solid penalty C*(1 + t + beta*rho*(1 - t^2)), t = tanh(beta*(rho - rho_m))
+// (poten.f90:110-114). In FP64, where x = beta*(rho - rho_m) < -10 (every
+// rho < 0.12 with the reference's beta = 40, rho_m = 0.37, i.e. the whole
+// droplet), the term is below 1e-3 K and is evaluated in FP32 from
+// E = exp(2x): 1 + t = 2E/(1+E), 1 - t^2 = 4E/(1+E)^2. Its FP32 rounding is
+// below 1e-9 K, far under the FP64 tolerance of pot4, and it replaces an FP64
+// tanh, which costs tens of FP64 instructions on a GPU whose FP64 issue
+// bounds this path.
+template <typename R>
+__device__ __forceinline__ R solid_penalty(R d, R beta, R dm, R cs) {
+  const R x = beta * (d - dm);
+  if (sizeof(R) == 8 && x < (R)-10) {
+    const float e = expf(2.f * (float)x);
+    const float inv = 1.f / (1.f + e);
+    const float bd = (float)(beta * d);
+    return (R)(((float)cs * 2.f * e * inv) * (1.f + 2.f * bd * inv));
+  }
+  const R t = tanh(x);
+  return cs * ((R)1 + t + beta * d * ((R)1 - t * t));
+}
 
 enum { PRO_PLAIN = 0, PRO_CORR = 1, PRO_PROD = 2 };
 

@@ -84,15 +84,19 @@ __global__ void __launch_bounds__(kRegThreads) k_y_reg(Grid g, FftAxis ax, SpecL
 // --------------------------------------------------- fused z convolution
 // Forward z transform of L kx columns of one y plane, product with each
 // factor table (times scale), inverse z transform; output 0 may alias the
-// input, `add` (nullable) is added to output 0.
+// input, `add` (nullable) is added to output 0. The forward spectrum is kept
+// in a second shared buffer (each thread rereads only its own slots), so
+// that registers hold one line segment at a time.
 template <typename R, int P, int Q>
-__global__ void __launch_bounds__(kRegThreads, 1) k_z_conv_reg(Grid g, FftAxis ax, const C2<R>* in, FactorList<R> fl,
-                                                            int nout, R scale, const C2<R>* __restrict__ add) {
+__global__ void __launch_bounds__(kRegThreads, sizeof(R) == 8 ? 1 : 2)
+    k_z_conv_reg(Grid g, FftAxis ax, const C2<R>* in, FactorList<R> fl, int nout, R scale,
+                 const C2<R>* __restrict__ add) {
   constexpr int N = P * Q;
   constexpr int L = reg_lines<P, Q>();
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
-  C2<R>* tws = buf + N * L;
+  C2<R>* xbuf = buf + N * L;
+  C2<R>* tws = xbuf + N * L;
   const int kx0 = blockIdx.x * L;
   const int ncol = min(L, g.nxh - kx0);
   const long long base = (long long)blockIdx.y * g.nxh + kx0;
@@ -104,26 +108,30 @@ __global__ void __launch_bounds__(kRegThreads, 1) k_z_conv_reg(Grid g, FftAxis a
   // layout B: thread (c, k'), k' < P, holds X[k' + P*j]
   const int cb = tid % L, kp = tid / L;
   const bool actB = kp < P && cb < ncol;
-  C2<R> v[P];
-  if (actA) {
+  {
+    C2<R> v[P];
+    if (actA) {
 #pragma unroll
-    for (int p = 0; p < P; ++p) v[p] = in[base + (Q * p + u) * stride + ca];
+      for (int p = 0; p < P; ++p) v[p] = in[base + (Q * p + u) * stride + ca];
+    }
+    stage_tw<R>(tws, twiddles<R>(ax), N);
+    __syncthreads();
+    if (actA) {
+      RegDft<R, P, -1>::run(v);
+#pragma unroll
+      for (int k = 1; k < P; ++k) v[k] = mulw<R, -1>(v[k], tws[u * k]);
+#pragma unroll
+      for (int k = 0; k < P; ++k) buf[(k * Q + u) * L + ca] = v[k];
+    }
   }
-  stage_tw<R>(tws, twiddles<R>(ax), N);
   __syncthreads();
-  if (actA) {
-    RegDft<R, P, -1>::run(v);
-#pragma unroll
-    for (int k = 1; k < P; ++k) v[k] = mulw<R, -1>(v[k], tws[u * k]);
-#pragma unroll
-    for (int k = 0; k < P; ++k) buf[(k * Q + u) * L + ca] = v[k];
-  }
-  __syncthreads();
-  C2<R> X[Q];
   if (actB) {
+    C2<R> X[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) X[q] = buf[(kp * Q + q) * L + cb];
     RegDft<R, Q, -1>::run(X);
+#pragma unroll
+    for (int j = 0; j < Q; ++j) xbuf[(kp * Q + j) * L + cb] = X[j];
   }
   for (int o = 0; o < nout; ++o) {
     C2<R> y[Q];
@@ -132,7 +140,8 @@ __global__ void __launch_bounds__(kRegThreads, 1) k_z_conv_reg(Grid g, FftAxis a
 #pragma unroll
       for (int j = 0; j < Q; ++j) {
         const R f = __ldg(&fac[base + (kp + P * j) * stride + cb]) * scale;
-        y[j] = mk<R>(X[j].x * f, X[j].y * f);
+        const C2<R> x = xbuf[(kp * Q + j) * L + cb];
+        y[j] = mk<R>(x.x * f, x.y * f);
       }
       RegDft<R, Q, 1>::run(y);
 #pragma unroll
@@ -326,10 +335,8 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_reg(Grid g, FftAxis ax, c
         if (fn.lsolid) {
           const C2<R> d = ld_pair<R>(pa.den + e);
           const R beta = (R)fn.beta_solid, dm = (R)fn.den_m, cs = (R)fn.c_solid;
-          const R t0 = tanh(beta * (d.x - dm));
-          const R t1 = tanh(beta * (d.y - dm));
-          p0 += cs * ((R)1 + t0 + beta * d.x * ((R)1 - t0 * t0));
-          p1 += cs * ((R)1 + t1 + beta * d.y * ((R)1 - t1 * t1));
+          p0 += solid_penalty<R>(d.x, beta, dm, cs);
+          p1 += solid_penalty<R>(d.y, beta, dm, cs);
         }
         val = mk<R>(p0, p1);
       }
@@ -353,7 +360,7 @@ template <typename R, int P, int Q>
 void run_z(const Grid& g, const FftPlan& p, const C2<R>* in, const FactorList<R>& fl, int nout, R scale,
            const C2<R>* add, cudaStream_t s, bool launch) {
   constexpr int L = reg_lines<P, Q>();
-  const size_t smem = sizeof(C2<R>) * (P * Q * L + P * Q);
+  const size_t smem = sizeof(C2<R>) * (2 * P * Q * L + P * Q);
   set_smem(k_z_conv_reg<R, P, Q>, smem);
   if (!launch) return;
   dim3 grid((g.nxh + L - 1) / L, g.ny);

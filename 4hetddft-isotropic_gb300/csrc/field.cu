@@ -14,6 +14,7 @@
 // order.
 #include <cstdio>
 
+#include "fpconv.cuh"
 #include "he4g_internal.cuh"
 
 namespace he4g {
@@ -119,6 +120,26 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* partials) {
   }
 }
 
+// FP32 warp sums converted once per warp, FP64 across warps (the |pc| terms
+// of errHe, a printed diagnostic whose relative accuracy 1e-6 is far inside
+// its 1e-10*max|psi| tolerance, while an FP64 sqrt and shuffle tree would add
+// about 15 FP64 instructions per point)
+__device__ __forceinline__ void block_sum_f1(float x, double* partials) {
+  __shared__ double sh[kRedBlock / 32];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  if (lane == 0) sh[wid] = (double)x;
+  __syncthreads();
+  if (tid == 0) {
+    const int nw = (blockDim.x * blockDim.y) >> 5;
+    double sum = 0.0;
+    for (int w = 0; w < nw; ++w) sum += sh[w];
+    partials[block_linear()] = sum;
+  }
+}
+
 // ------------------------------------------------------------ integrators
 // Predictor + modifier (steppc.f90:45-65). p3 holds psi_{n-3} on entry and
 // the modified prediction on exit; h2 holds f_{n-2} on entry and f_n on exit.
@@ -133,7 +154,7 @@ __global__ void __launch_bounds__(256) k_pc_predict(Grid g, Stencil st, Function
   if (!t.ok) return;
   const double2 lap = lap13(psi, t, g, st);
   const double2 ps = ld2(psi + t.p);
-  const double2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), (double)__ldg(timec + t.p), fn.h2o2m4);
+  const double2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), (double)f2d(__ldg(timec + t.p)), fn.h2o2m4);
   const double2 a1 = h1[t.p], a2 = h2[t.p], o3 = p3[t.p], q = pc[t.p];
   // 2 f_n - f_{n-1} + 2 f_{n-2}
   const double tr = fma(2.0, a2.x, fma(2.0, f.x, -a1.x));
@@ -160,11 +181,11 @@ __global__ void __launch_bounds__(256) k_pc_correct(Grid g, Stencil st, Function
                                                      double* den, double* partials, double f3, double c9,
                                                      int* health) {
   const Pt t = point(g);
-  double v[1] = {0.0};
+  float v = 0.f;
   if (t.ok) {
     const double2 lap = lap13(psit, t, g, st);
     const double2 ps = ld2(psit + t.p);
-    const double2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), (double)__ldg(timec + t.p),
+    const double2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), (double)f2d(__ldg(timec + t.p)),
                            fn.h2o2m4);
     const double2 a1 = ld2(h1 + t.p), a2 = ld2(h2 + t.p), o3 = ld2(p3 + t.p), o2 = ld2(p2 + t.p);
     // f* + 2 f_n - f_{n-1}
@@ -179,11 +200,12 @@ __global__ void __launch_bounds__(256) k_pc_correct(Grid g, Stencil st, Function
     psi_out[t.p] = pn;
     const double d = fma(pn.x, pn.x, pn.y * pn.y);
     den[t.p] = d;
-    v[0] = sqrt(fma(q.x, q.x, q.y * q.y));
+    const float qx = d2f(q.x), qy = d2f(q.y);
+    v = sqrtf(fmaf(qx, qx, qy * qy));
     const int h = den_health(d) & 2;
     if (h) atomicOr(health, h);
   }
-  block_sum<1>(v, partials);
+  block_sum_f1(v, partials);
 }
 
 // One Runge–Kutta–Gill stage (steprk.f90:57-92). f_out (stage 1 only)
@@ -199,7 +221,7 @@ __global__ void __launch_bounds__(256) k_rk_stage(Grid g, Stencil st, Functional
   if (!t.ok) return;
   const double2 lap = lap13(psi, t, g, st);
   const double2 ps = ld2(psi + t.p);
-  const double2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), (double)__ldg(timec + t.p), fn.h2o2m4);
+  const double2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), (double)f2d(__ldg(timec + t.p)), fn.h2o2m4);
   double2 qq = q[t.p];
   const double2 s1 = make_double2(ar * fma(-br, qq.x, f.x), ar * fma(-br, qq.y, f.y));
   qq = make_double2(fma(-cr, f.x, fma(3.0, s1.x, qq.x)), fma(-cr, f.y, fma(3.0, s1.y, qq.y)));
@@ -453,6 +475,46 @@ __device__ void reduce_cols(const double* partials, int nblocks, int nvals, doub
 __global__ void __launch_bounds__(kFinalThreads) k_reduce(const double* partials, int nblocks, int nvals,
                                                        double* out) {
   reduce_cols(partials, nblocks, nvals, out);
+}
+
+}  // namespace
+
+int fold_launches(int nblocks) { return nblocks > 4 * 256 ? 1 : 0; }  // 256 = kFold
+
+namespace {
+
+// First level of the per-step sums: block c adds rows [c*kFold, (c+1)*kFold)
+// of partials[nblocks][nvals] in a fixed tree order into folded[c][nvals],
+// so that the single block of the impurity update reads a few hundred rows
+// instead of one per grid block (FP64 adds of one block run at the FP64 rate
+// of one SM).
+constexpr int kFold = 256;
+__global__ void __launch_bounds__(kFold) k_fold(const double* __restrict__ partials, int nblocks, int nvals,
+                                                 double* __restrict__ folded) {
+  __shared__ double sh[kFold];
+  const int b = blockIdx.x * kFold + threadIdx.x;
+  for (int a = 0; a < nvals; ++a) {
+    sh[threadIdx.x] = b < nblocks ? partials[(long long)b * nvals + a] : 0.0;
+    __syncthreads();
+    for (int s = kFold / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) folded[(long long)blockIdx.x * nvals + a] = sh[0];
+    __syncthreads();
+  }
+}
+
+// Folds partials in place when there are many rows: the folded rows go right
+// after the nblocks*nvals values (callers size partials for that); returns
+// the rows the final reduction reads.
+const double* fold_partials(const double* partials, int& nblocks, int nvals, cudaStream_t s) {
+  if (!fold_launches(nblocks)) return partials;
+  double* folded = const_cast<double*>(partials) + (long long)nblocks * nvals;
+  const int nc = (nblocks + kFold - 1) / kFold;
+  k_fold<<<nc, kFold, 0, s>>>(partials, nblocks, nvals, folded);
+  nblocks = nc;
+  return folded;
 }
 
 // ------------------------------------------------- impurity scalar updates
@@ -711,11 +773,13 @@ void launch_imp_pc_predict(ImpState* imp, double c4o3dt, double c112, cudaStream
 }
 void launch_imp_pc_correct(ImpState* imp, const double* err_partials, int nblocks, double dt, double c9,
                            double nxyz, cudaStream_t s) {
-  k_imp_pc_correct<<<1, kFinalThreads, 0, s>>>(imp, err_partials, nblocks, dt, c9, nxyz);
+  const double* p = fold_partials(err_partials, nblocks, 1, s);
+  k_imp_pc_correct<<<1, kFinalThreads, 0, s>>>(imp, p, nblocks, dt, c9, nxyz);
 }
 void launch_imp_force(ImpState* imp, const double* partials, int nblocks, double dxyz, double mass,
                       int store_accel, cudaStream_t s) {
-  k_imp_force<<<1, kFinalThreads, 0, s>>>(imp, partials, nblocks, dxyz, mass, store_accel);
+  const double* p = fold_partials(partials, nblocks, 3, s);
+  k_imp_force<<<1, kFinalThreads, 0, s>>>(imp, p, nblocks, dxyz, mass, store_accel);
 }
 void launch_imp_record(ImpState* imp, double* ring, cudaStream_t s) {
   k_imp_record<<<1, 32, 0, s>>>(imp, ring);

@@ -9,7 +9,12 @@
 // neighbours of each point from FP64 would cost as much as FP64 arithmetic
 // on this GPU, whose FP64 rate is 1/61 of its FP32 rate.
 //
+// Conversions between the FP32 and FP64 values use the integer forms of
+// fpconv.cuh: on GB300 the conversion instructions issue on the FP64 pipe,
+// which bounds these kernels otherwise.
+//
 // Formulas and their reference lines are those of field.cu.
+#include "fpconv.cuh"
 #include "he4g_internal.cuh"
 
 namespace he4g {
@@ -140,12 +145,12 @@ __global__ void __launch_bounds__(256) k_pc_predict_mp(Grid g, StencilF st, Func
   const float tr = fmaf(2.f, a2.x, fmaf(2.f, f.x, -a1.x));
   const float ti = fmaf(2.f, a2.y, fmaf(2.f, f.y, -a1.y));
   const double2 o3 = p3[t.p], q = pc[t.p];
-  const double2 s1 = make_double2(fma(c4o3dt, (double)tr, o3.x), fma(c4o3dt, (double)ti, o3.y));
+  const double2 s1 = make_double2(fma(c4o3dt, f2d(tr), o3.x), fma(c4o3dt, f2d(ti), o3.y));
   const double2 pn = make_double2(fma(-c112, q.x, s1.x), fma(-c112, q.y, s1.y));
   p3[t.p] = pn;
   pc[t.p] = s1;
   h2[t.p] = f;
-  const float2 p32 = make_float2((float)pn.x, (float)pn.y);
+  const float2 p32 = make_float2(d2f(pn.x), d2f(pn.y));
   psi32_out[t.p] = p32;
   den[t.p] = fmaf(p32.x, p32.x, p32.y * p32.y);
 }
@@ -161,7 +166,7 @@ __global__ void __launch_bounds__(256) k_pc_correct_mp(Grid g, StencilF st, Func
                                                         const float* __restrict__ uimp,
                                                         const float* __restrict__ timec, double2* psi_out,
                                                         float2* __restrict__ psi32_out, float* den,
-                                                        double* partials, double f3, double c9, int* health) {
+                                                        double* partials, float f38, double c9, int* health) {
   const Pt t = point(g);
   float v[1] = {0.f};
   if (t.ok) {
@@ -171,19 +176,22 @@ __global__ void __launch_bounds__(256) k_pc_correct_mp(Grid g, StencilF st, Func
     const float2 a1 = ld2f(h1 + t.p), a2 = ld2f(h2 + t.p);
     const float tr = fmaf(2.f, a1.x, f.x) - a2.x;
     const float ti = fmaf(2.f, a1.y, f.y) - a2.y;
+    // s5 = (9 psi_n - psi_{n-2} + 3 dt t)/8 as 1.125 psi_n - 0.125 psi_{n-2}
+    // + (3 dt/8) t: the last product in FP32, where t already carries FP32
+    // error; four FP64 operations per component in all
     const double2 o3 = __ldg(p3 + t.p), o2 = __ldg(p2 + t.p);
-    const double2 s5 = make_double2(0.125 * fma(f3, (double)tr, fma(9.0, o3.x, -o2.x)),
-                                    0.125 * fma(f3, (double)ti, fma(9.0, o3.y, -o2.y)));
+    const double2 s5 = make_double2(fma(1.125, o3.x, fma(-0.125, o2.x, f2d(f38 * tr))),
+                                    fma(1.125, o3.y, fma(-0.125, o2.y, f2d(f38 * ti))));
     double2 q = pc[t.p];
     q = make_double2(q.x - s5.x, q.y - s5.y);
     pc[t.p] = q;
     const double2 pn = make_double2(fma(c9, q.x, s5.x), fma(c9, q.y, s5.y));
     psi_out[t.p] = pn;
-    const float2 p32 = make_float2((float)pn.x, (float)pn.y);
+    const float2 p32 = make_float2(d2f(pn.x), d2f(pn.y));
     psi32_out[t.p] = p32;
     const float d = fmaf(p32.x, p32.x, p32.y * p32.y);
     den[t.p] = d;
-    const float qx = (float)q.x, qy = (float)q.y;
+    const float qx = d2f(q.x), qy = d2f(q.y);
     v[0] = sqrtf(fmaf(qx, qx, qy * qy));
     const int h = den_health(d) & 2;
     if (h) atomicOr(health, h);
@@ -205,7 +213,7 @@ __global__ void __launch_bounds__(256) k_rk_stage_mp(Grid g, StencilF st, Functi
   const float2 lap = lap13f(psi32, t, g, st);
   const float2 ps = ld2f(psi32 + t.p);
   const float2 f = hpsif(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), (float)fn.h2o2m4);
-  const double fx = (double)f.x, fy = (double)f.y;
+  const double fx = f2d(f.x), fy = f2d(f.y);
   double2 qq = q[t.p];
   const double2 s1 = make_double2(ar * fma(-br, qq.x, fx), ar * fma(-br, qq.y, fy));
   qq = make_double2(fma(-cr, fx, fma(3.0, s1.x, qq.x)), fma(-cr, fy, fma(3.0, s1.y, qq.y)));
@@ -214,7 +222,7 @@ __global__ void __launch_bounds__(256) k_rk_stage_mp(Grid g, StencilF st, Functi
   const double2 p0 = __ldg(psi + t.p);
   const double2 pn = make_double2(fma(dt, s1.x, p0.x), fma(dt, s1.y, p0.y));
   psi_out[t.p] = pn;
-  const float2 p32 = make_float2((float)pn.x, (float)pn.y);
+  const float2 p32 = make_float2(d2f(pn.x), d2f(pn.y));
   psi32_out[t.p] = p32;
   den[t.p] = fmaf(p32.x, p32.x, p32.y * p32.y);
   // the steprk.f90:89-92 check on |psi|^2 in FP64: far droplet tails reach
@@ -242,13 +250,19 @@ __global__ void k_split_mp(Grid g, const double2* __restrict__ psi, float2* psi3
 // r = r2 * rsqrt(r2) and r * (1/d) are within a few FP32 ulps, far inside the
 // mixed form's tolerance; the standalone potenimp and the force kernel use
 // this same function, so their uimp agree bit for bit.
+// The node index comes without a conversion instruction: for 0 <= qd < 2^23,
+// qd + 2^23 rounded toward zero is 2^23 + trunc(qd), whose low mantissa
+// bits are the index.
 __device__ __forceinline__ float uimp_at(const ImpTable& t, float dx, float dy, float dz, int* health) {
   const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
   const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
   const float qd = r * t.inv;
-  const int ir = (int)qd;
-  const float w = qd - (float)ir;
-  if (ir >= 0 && ir + 1 < t.npot) return fmaf(__ldg(t.potion + ir), 1.f - w, __ldg(t.potion + ir + 1) * w);
+  if (qd < t.qmax) {  // trunc(qd) + 1 < npot; false for NaN
+    const float big = __fadd_rz(qd, 8388608.f);
+    const int ir = __float_as_int(big) - __float_as_int(8388608.f);
+    const float w = qd - (big - 8388608.f);
+    return fmaf(__ldg(t.potion + ir), 1.f - w, __ldg(t.potion + ir + 1) * w);
+  }
   atomicOr(health, 4);
   return 0.f;
 }
@@ -266,7 +280,7 @@ __device__ __forceinline__ void load_center(ImpState* imp, int center_sel, float
   __syncthreads();
 }
 
-constexpr int kZF = 8;  // z-planes per thread of the impurity kernels
+constexpr int kZF = 16;  // z-planes per thread of the impurity kernels
 
 __global__ void __launch_bounds__(256) k_potenimp_mp(Grid g, ImpTable tab, ImpState* imp, int center_sel,
                                                       float* uimp) {
@@ -331,50 +345,80 @@ __device__ __forceinline__ void block_sum_dw(float (&h)[NV], float (&l)[NV], dou
   }
 }
 
-__global__ void __launch_bounds__(256, 3) k_force_mp(Grid g, StencilF st, const float* __restrict__ den, ImpTable tab,
-                                                      ImpState* imp, int center_sel, float* uimp_out,
-                                                      double* partials) {
+// Blocks of kFX x kFY columns march kZF planes. Each plane's den tile with
+// its 6-point halo (kTW x kTH) is staged in shared memory, so the 24 x/y
+// neighbours are shared-memory reads at fixed offsets; the z neighbours stay
+// in a per-column register window. The loads of a plane are issued before
+// the barrier that frees the tile, so they overlap the previous plane.
+constexpr int kFX = 32, kFY = 8;
+constexpr int kTW = kFX + 2 * kStencilHalf, kTH = kFY + 2 * kStencilHalf;
+constexpr int kTileSlots = (kTW * kTH + kFX * kFY - 1) / (kFX * kFY);
+
+__global__ void __launch_bounds__(kFX * kFY) k_force_mp(Grid g, StencilF st, const float* __restrict__ den,
+                                                         ImpTable tab, ImpState* imp, int center_sel,
+                                                         float* uimp_out, double* partials) {
   __shared__ float cf[3];
+  __shared__ float tile[kTH * kTW];
   load_center(imp, center_sel, cf);
-  const int i = blockIdx.x * kBX + threadIdx.x;
-  const int j = blockIdx.y * kBY + threadIdx.y;
-  const int k0 = blockIdx.z * kZF;
+  const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * kFX + lx;
+  const int x0 = blockIdx.x * kFX, y0 = blockIdx.y * kFY, k0 = blockIdx.z * kZF;
+  const int i = x0 + lx, j = y0 + ly;
+  const bool own = i < g.nx && j < g.ny;
+  const long long sz = (long long)g.nx * g.ny;
+  // this thread's slots of the tile: in-plane offset and whether in the grid
+  int toff[kTileSlots];
+  bool tok[kTileSlots];
+#pragma unroll
+  for (int s = 0; s < kTileSlots; ++s) {
+    const int idx = tid + s * kFX * kFY;
+    const int ty = idx / kTW, tx = idx - ty * kTW;
+    const int gx = x0 - kStencilHalf + tx, gy = y0 - kStencilHalf + ty;
+    tok[s] = idx < kTW * kTH && gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
+    toff[s] = tok[s] ? gy * g.nx + gx : 0;
+  }
+  float dx = 0.f, dy = 0.f;
+  constexpr int W = kZF + 2 * kStencilHalf;
+  float wz[W];  // den at planes k0-6 .. k0+kZF+5 of this column
+  const long long colo = (long long)j * g.nx + i;
+#pragma unroll
+  for (int m = 0; m < W; ++m) {
+    const int k = k0 - kStencilHalf + m;
+    wz[m] = (own && k >= 0 && k < g.nz) ? __ldg(den + colo + k * sz) : 0.f;
+  }
+  if (own) {
+    dx = __ldg(tab.xs + i) - cf[0];
+    dy = __ldg(tab.ys + j) - cf[1];
+  }
   float s[3] = {0.f, 0.f, 0.f}, cc[3] = {0.f, 0.f, 0.f};
-  if (i < g.nx && j < g.ny) {
-    const int sy = g.nx, sz = g.nx * g.ny;
-    const long long colo = (long long)j * g.nx + i;
-    const float* col = den + colo;
-    const float dx = __ldg(tab.xs + i) - cf[0];
-    const float dy = __ldg(tab.ys + j) - cf[1];
-    constexpr int W = kZF + 2 * kStencilHalf;
-    float wz[W];  // den at planes k0-6 .. k0+kZF+5 of this column
+  const float* t0 = tile + (ly + kStencilHalf) * kTW + lx + kStencilHalf;  // this point in the tile
 #pragma unroll
-    for (int m = 0; m < W; ++m) {
-      const int k = k0 - kStencilHalf + m;
-      wz[m] = (k >= 0 && k < g.nz) ? __ldg(col + (long long)k * sz) : 0.f;
+  for (int m = 0; m < kZF; ++m) {
+    const int k = k0 + m;
+    if (k >= g.nz) break;  // uniform over the block
+    const float* plane = den + k * sz;
+    float tv[kTileSlots];
+#pragma unroll
+    for (int q = 0; q < kTileSlots; ++q) tv[q] = tok[q] ? __ldg(plane + toff[q]) : 0.f;
+    __syncthreads();  // the previous plane's reads of the tile are done
+#pragma unroll
+    for (int q = 0; q < kTileSlots; ++q) {
+      const int idx = tid + q * kFX * kFY;
+      if (idx < kTW * kTH) tile[idx] = tv[q];
     }
+    __syncthreads();
+    if (own) {
+      float gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
-    for (int m = 0; m < kZF; ++m) {
-      const int k = k0 + m;
-      if (k < g.nz) {
-        const float* q = col + (long long)k * sz;
-        float gx = 0.f, gy = 0.f, gz = 0.f;
-#pragma unroll
-        for (int o = 1; o <= kStencilHalf; ++o) {
-          float a = i - o >= 0 ? __ldg(q - o) : 0.f;
-          float b = i + o < g.nx ? __ldg(q + o) : 0.f;
-          gx = fmaf(st.d1[0][o], b - a, gx);
-          a = j - o >= 0 ? __ldg(q - o * sy) : 0.f;
-          b = j + o < g.ny ? __ldg(q + o * sy) : 0.f;
-          gy = fmaf(st.d1[1][o], b - a, gy);
-          gz = fmaf(st.d1[2][o], wz[m + kStencilHalf + o] - wz[m + kStencilHalf - o], gz);
-        }
-        const float u = uimp_at(tab, dx, dy, __ldg(tab.zs + k) - cf[2], &imp->health);
-        if (uimp_out) uimp_out[colo + (long long)k * sz] = u;
-        kahan_add(s[0], cc[0], gx * u);
-        kahan_add(s[1], cc[1], gy * u);
-        kahan_add(s[2], cc[2], gz * u);
+      for (int o = 1; o <= kStencilHalf; ++o) {
+        gx = fmaf(st.d1[0][o], t0[o] - t0[-o], gx);
+        gy = fmaf(st.d1[1][o], t0[o * kTW] - t0[-o * kTW], gy);
+        gz = fmaf(st.d1[2][o], wz[m + kStencilHalf + o] - wz[m + kStencilHalf - o], gz);
       }
+      const float u = uimp_at(tab, dx, dy, __ldg(tab.zs + k) - cf[2], &imp->health);
+      if (uimp_out) uimp_out[colo + k * sz] = u;
+      kahan_add(s[0], cc[0], gx * u);
+      kahan_add(s[1], cc[1], gy * u);
+      kahan_add(s[2], cc[2], gz * u);
     }
   }
   float lo[3] = {-cc[0], -cc[1], -cc[2]};
@@ -467,7 +511,7 @@ __global__ void __launch_bounds__(256) k_energy_point_mp(Grid g, Functional fn, 
 }  // namespace
 
 int force_blocks_mp(const Grid& g) {
-  return ((g.nx + kBX - 1) / kBX) * ((g.ny + kBY - 1) / kBY) * ((g.nz + kZF - 1) / kZF);
+  return ((g.nx + kFX - 1) / kFX) * ((g.ny + kFY - 1) / kFY) * ((g.nz + kZF - 1) / kZF);
 }
 
 void launch_pc_predict_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
@@ -482,8 +526,9 @@ void launch_pc_correct_mp(const Grid& g, const StencilF& st, const Functional& f
                           const float* pot4, const float* uimp, const float* timec, double2* psi_out,
                           float2* psi32_out, float* den, double* partials, double f3, double c9, int* health,
                           cudaStream_t s) {
+  const float f38 = (float)(0.125 * f3);
   k_pc_correct_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, fn, psit32, p3, p2, h1, h2, pc, pot4, uimp,
-                                                           timec, psi_out, psi32_out, den, partials, f3, c9,
+                                                           timec, psi_out, psi32_out, den, partials, f38, c9,
                                                            health);
 }
 void launch_rk_stage_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
@@ -503,8 +548,8 @@ void launch_potenimp_mp(const Grid& g, const ImpTable& tab, ImpState* imp, int c
 }
 void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const ImpTable& tab, ImpState* imp,
                      int center_sel, float* uimp_out, double* partials, cudaStream_t s) {
-  dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZF - 1) / kZF);
-  k_force_mp<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, tab, imp, center_sel, uimp_out, partials);
+  dim3 grid((g.nx + kFX - 1) / kFX, (g.ny + kFY - 1) / kFY, (g.nz + kZF - 1) / kZF);
+  k_force_mp<<<grid, dim3(kFX, kFY), 0, s>>>(g, st, den, tab, imp, center_sel, uimp_out, partials);
 }
 void launch_grad1_f(const Grid& g, const StencilF& st, int axis, const float* in, float* out, cudaStream_t s) {
   k_grad1_f<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, axis, in, out);

@@ -183,13 +183,18 @@ void launch_ualphas_a(const Grid& g, const double* falfs, const double* ix, cons
 void launch_ualphas_b(const Grid& g, double* u, const double* s4, const double* s5, const double* s6,
                       double h2o2m4, double alphas, double* pot4, cudaStream_t s);
 
-// impurity scalar kernels (field.cu)
+// impurity scalar kernels (field.cu). The partial arrays of
+// launch_imp_pc_correct / launch_imp_force need room for
+// ceil(nblocks/256)*nvals more values after their nblocks*nvals (first-level
+// sums); the run's partial buffer holds 12 values per point block.
 void launch_imp_rk(ImpState* imp, int stage, double ar, double br, double cr, double dt, cudaStream_t s);
 void launch_imp_pc_predict(ImpState* imp, double c4o3dt, double c112, cudaStream_t s);
 void launch_imp_pc_correct(ImpState* imp, const double* err_partials, int nblocks, double dt,
                            double c9, double nxyz, cudaStream_t s);
 void launch_imp_force(ImpState* imp, const double* partials, int nblocks, double dxyz, double mass,
                       int store_accel, cudaStream_t s);
+// extra launches (first-level sums) the two calls above make for nblocks rows
+int fold_launches(int nblocks);
 void launch_imp_record(ImpState* imp, double* ring, cudaStream_t s);
 
 // ------------------------- mixed-precision field kernels (fieldmp.cu)
@@ -212,7 +217,8 @@ struct ImpTable {
   const float *xs, *ys, *zs;
   const float* potion;
   int npot;
-  float inv;  // 1 / delinter
+  float inv;   // 1 / delinter
+  float qmax;  // npot - 1: r/delinter below it has both interpolation nodes
 };
 void launch_potenimp_mp(const Grid& g, const ImpTable& tab, ImpState* imp, int center_sel, float* uimp,
                         cudaStream_t s);

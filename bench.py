@@ -69,7 +69,9 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64):
     return {
         "pc_predict": pred,
         "pc_correct": corr,
-        "potenimp": ev * r * n,
+        # FP64: its own pass writing uimp; mixed: uimp is evaluated in the
+        # force kernel, whose bytes below include the uimp write
+        "potenimp": ev * r * n if prec == FP64 else 0,
         # den -> spectrum; den, dencg -> spectrum (correlation prologue)
         "fft_x_r2c": ev * ((r * n + c * nh) + (2 * r * n + c * nh)),
         # fwd 1, inv 1, fwd 1, inv 1 spectrum: read + write each
@@ -80,10 +82,23 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64):
         "fft_x_c2r": ev * (c * nh + r * n),
         # spectrum + dencg + den -> pot4
         "fft_x_c2r_pot4": ev * (c * nh + 3 * r * n),
-        # R den + uimp
+        # FP64: R den + uimp; mixed: R den, W uimp
         "force": ev * 2 * r * n,
         "impurity_scalar": 0,
     }
+
+
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of each
+# kernel family at 256^3, mean over the captured launches; from the ncu
+# captures summarised in profiles/fp64_step_he5000_xe_256_kernels.md and
+# profiles/mixed_step_he5000_xe_256_kernels.md.
+TRAFFIC_256 = {
+    FP64: {"potenimp": 71.7e6, "fft_x_r2c": 293.2e6, "fft_y": 216.6e6, "fft_z_conv": 470.7e6,
+           "fft_x_c2r": 218.4e6, "fft_x_c2r_pot4": 511.3e6, "force": 268.8e6, "pc_predict": 2581.7e6,
+           "pc_correct": 2600.8e6},
+    MIXED: {"fft_x_r2c": 126.0e6, "fft_y": 81.5e6, "fft_z_conv": 212.1e6, "fft_x_c2r": 85.9e6,
+            "fft_x_c2r_pot4": 244.2e6, "force": 97.1e6, "pc_predict": 1961.1e6, "pc_correct": 2114.0e6},
+}
 
 
 def read_peaks():
@@ -301,7 +316,10 @@ def timed_steps(run, cfg, prec, steps, barrier, clock_gpu):
     step_gbs = step_bytes / (ms / steps * 1e-3) / 1e9
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-        "peak_source": peak_kind, "kernel": top["family"], "traffic": None,
+        "peak_source": peak_kind, "kernel": top["family"],
+        "traffic": (TRAFFIC_256[prec].get(top["family"])
+                    if (cfg.nx, cfg.ny, cfg.nz) == (256, 256, 256) else None),
+        "traffic_source": "ncu dram bytes per launch (profiles/, 256^3 capture)",
         "step_algorithmic_bytes": step_bytes, "step_gbs": step_gbs, "step_frac": step_gbs / peak,
         "families": rows,
     }
@@ -372,7 +390,8 @@ def ours(args):
             "hbm_gbs": rf["step_gbs"],
             "roofline": rf,
             "fp64_note": ("FP64 issue bounds the FP64 form (GB300: 1.2 TFLOP/s FP64, 1/61 of FP32); ncu shows "
-                          "77-88% FP64-pipe activity in every kernel" if prec == FP64 else None),
+                          "83-85% FP64-pipe activity in every kernel of the step" if prec == FP64 else None),
+            "fp64_pipe_busy_ncu": 0.84 if prec == FP64 else None,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val * ws if e2e_val else None, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
