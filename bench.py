@@ -47,10 +47,13 @@ def set_case(name):
     CASE = name
 
 
-def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64):
+def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64, fused_corr=False):
     """Compulsory HBM bytes of one predictor-corrector step per kernel family:
     reads + writes of each launch's inputs and outputs, stencil neighbours
-    counted once, spectra as (nx/2+1)*ny*nz complex. Returns {family: bytes}."""
+    counted once, spectra as (nx/2+1)*ny*nz complex. fused_corr: the inverse
+    x pass of the coarse-grained density and the forward x pass of the
+    correlation prologue run as one kernel (family fft_x_c2r_corr).
+    Returns {family: bytes}."""
     n = nx * ny * nz
     nh = (nx // 2 + 1) * ny * nz
     ev = 2  # potential evaluations per step
@@ -66,7 +69,7 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64):
         pred = 120 * n
         # R psit32 8 pot4 4 uimp 4 timec 4 p3 16 p2 16 h1 8 h2 8 pc 16 | W pc 16 psi 16 psi32 8 den 4
         corr = 128 * n
-    return {
+    fam = {
         "pc_predict": pred,
         "pc_correct": corr,
         # FP64: its own pass writing uimp; mixed: uimp is evaluated in the
@@ -85,7 +88,14 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64):
         # FP64: R den + uimp; mixed: R den, W uimp
         "force": ev * 2 * r * n,
         "impurity_scalar": 0,
+        "fft_x_c2r_corr": 0,
     }
+    if fused_corr:
+        # R spectrum, W dencg, R den, W spectrum; the r2c family keeps the plain pass only
+        fam["fft_x_c2r_corr"] = ev * (2 * c * nh + 2 * r * n)
+        fam["fft_x_c2r"] = 0
+        fam["fft_x_r2c"] = ev * (r * n + c * nh)
+    return fam
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of each
@@ -242,7 +252,7 @@ def cpu_sample(kind_steps):
 def run_cpu_sample(warm, steps):
     env = dict(os.environ)
     env.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
-    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-sample", str(warm), str(steps)],
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-sample", str(warm), str(steps), CASE],
                        capture_output=True, text=True, env=env, timeout=1800)
     if r.returncode != 0:
         raise RuntimeError("cpu sample failed: " + r.stderr[-2000:])
@@ -252,6 +262,28 @@ def run_cpu_sample(warm, steps):
 def dist_env():
     return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
             int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def max_over_ranks(ms, dist, device):
+    """The slowest replica's time: the job is done when the last rank is."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ws, steps, ms):
+    """Whole-job steps/s: every rank advances its own run by `steps`."""
+    return ws * steps / (ms * 1e-3)
+
+
+def case_grid(case):
+    import he4gpu
+    c = he4gpu.initial.CASES[case]
+    n = c["n"]
+    return list(n) if not isinstance(n, int) else [n, n, n]
 
 
 def reference_arm(args):
@@ -264,16 +296,19 @@ def reference_arm(args):
     steps = max(1, min(args.steps, 8))
     s = run_cpu_sample(warm, steps)
     val = 1.0 / s["sec_per_step"]
+    import he4gpu
+    c = he4gpu.initial.CASES[CASE]
+    grid = case_grid(CASE)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * s["sec_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Woods-Saxon droplet + Xe)",
-        "config": {"workload": CASE, "grid": [256, 256, 256], "h": 0.4, "n4": 5000, "impurity": "Xe",
+        "config": {"workload": CASE, "grid": grid, "h": c["h"], "n4": c["n4"], "impurity": c["imp"],
                    "steps_timed": steps},
         "cpu_baseline": {"value": val, "unit": "steps/s", "cores": s["cores"], "kind": "port",
-                         "sample": f"{steps} predictor-corrector steps of the FP64 C oracle at 256^3 "
-                                   f"(median), OpenMP over {s['cores']} cores"},
+                         "sample": f"{steps} predictor-corrector steps of the FP64 C oracle at "
+                                   f"{'x'.join(map(str, grid))} (median), OpenMP over {s['cores']} cores"},
         "e2e": {"value": val, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -299,7 +334,8 @@ def timed_steps(run, cfg, prec, steps, barrier, clock_gpu):
     dev_ms_clean = run.step_timed(steps)
     barrier()
     ms = min(dev_ms, dev_ms_clean)
-    bytes_fam = algorithmic_bytes_per_step(cfg.nx, cfg.ny, cfg.nz, prec)
+    fused = fam.get("fft_x_c2r_corr", (0.0, 0))[1] > 0
+    bytes_fam = algorithmic_bytes_per_step(cfg.nx, cfg.ny, cfg.nz, prec, fused)
     tot = sum(v[0] for v in fam.values()) or 1.0
     rows = []
     for name, (fms, nl) in sorted(fam.items(), key=lambda x: -x[1][0]):
@@ -349,12 +385,8 @@ def ours(args):
     warm = max(args.warmup, 3)
     run.step(warm)
     res = timed_steps(run, cfg, prec, args.steps, barrier, local)
-    ms = res["ms"]
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(res["ms"], dist, "cuda")
+    value = replica_value(ws, args.steps, ms)
     line = None
     if rank == 0:
         if args.no_e2e:
@@ -448,6 +480,8 @@ def mixed_measure(args, run64, barrier, gpu):
 
 def main():
     if len(sys.argv) >= 2 and sys.argv[1] == "--cpu-sample":
+        if len(sys.argv) > 4:
+            set_case(sys.argv[4])
         cpu_sample((int(sys.argv[2]), int(sys.argv[3])))
         return 0
     ap = argparse.ArgumentParser()
