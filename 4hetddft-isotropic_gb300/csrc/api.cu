@@ -46,11 +46,13 @@ enum Fam {
   F_FORCE,
   F_SCALAR,
   F_ALPHA_S,
+  F_FFT_X_C2R_CORR,
   F_COUNT
 };
 const char* kFamName[F_COUNT] = {"pc_predict", "pc_correct", "rk_stage",        "potenimp",
                                  "fft_x_r2c",  "fft_y",      "fft_z_conv",      "fft_x_c2r",
-                                 "fft_x_c2r_pot4", "force",  "impurity_scalar", "alpha_s_pointwise"};
+                                 "fft_x_c2r_pot4", "force",  "impurity_scalar", "alpha_s_pointwise",
+                                 "fft_x_c2r_corr"};
 
 // history roles a captured step graph was recorded with
 struct GraphKey {
@@ -169,15 +171,26 @@ cudaEvent_t take_event(he4g_run* r) {
 struct Tick {
   he4g_run* r;
   int fam;
+  int n;
+  bool live = true;
   cudaEvent_t a = nullptr;
-  Tick(he4g_run* run, int f, int nlaunch = 1) : r(run), fam(f) {
+  Tick(he4g_run* run, int f, int nlaunch = 1) : r(run), fam(f), n(nlaunch) {
     r->launches += nlaunch;
     if (r->timing) {
       a = take_event(r);
       cudaEventRecord(a, r->s);
     }
   }
+  // the guarded launch did not happen
+  void cancel() {
+    live = false;
+    r->launches -= n;
+  }
   ~Tick() {
+    if (!live) {
+      if (a) r->pool.push_back(a);
+      return;
+    }
     if (r->timing) {
       cudaEvent_t b = take_event(r);
       cudaEventRecord(b, r->s);
@@ -424,15 +437,25 @@ void poten_dev(he4g_run* r) {
     void* sp[2] = {r->spec0, r->spec2};
     fft_y(g, r->plan, prec, sp, otc ? 2 : 1, +1, r->s);
   }
-  {
-    Tick t(r, F_FFT_X_C2R);
-    const void* in[2] = {r->spec0, r->spec2};
-    void* o[2] = {r->dencg, r->denalf};
-    fft_x_c2r(g, r->plan, prec, in, o, otc ? 2 : 1, r->s);
+  // dencg and the correlation prologue: one fused row pass on the register
+  // engine (OT core), else c2r then r2c
+  bool fused = false;
+  if (!otc) {
+    Tick t(r, F_FFT_X_C2R_CORR);
+    fused = fft_x_c2r_corr(g, r->plan, prec, r->spec0, r->dencg, r->den, r->cfg.cp4, r->cfg.cpp4, r->s);
+    if (!fused) t.cancel();
   }
-  {
-    Tick t(r, F_FFT_X_R2C);
-    fft_x_r2c_corr(g, r->plan, prec, r->den, r->dencg, r->cfg.cp4, r->cfg.cpp4, r->spec0, r->s);
+  if (!fused) {
+    {
+      Tick t(r, F_FFT_X_C2R);
+      const void* in[2] = {r->spec0, r->spec2};
+      void* o[2] = {r->dencg, r->denalf};
+      fft_x_c2r(g, r->plan, prec, in, o, otc ? 2 : 1, r->s);
+    }
+    {
+      Tick t(r, F_FFT_X_R2C);
+      fft_x_r2c_corr(g, r->plan, prec, r->den, r->dencg, r->cfg.cp4, r->cfg.cpp4, r->spec0, r->s);
+    }
   }
   {
     Tick t(r, F_FFT_Y);
@@ -628,8 +651,9 @@ void steppc_dev(he4g_run* r, double dt) {
   }
   roles_after_correct(r, psit);
   {
-    Tick t(r, F_SCALAR, 1 + fold_launches(r->pblocks));
-    launch_imp_pc_correct(r->imp, r->partials, r->pblocks, dt, c9, static_cast<double>(r->g.n), r->s);
+    const int nb = mp ? pc_blocks_mp(r->g) : r->pblocks;
+    Tick t(r, F_SCALAR, 1 + fold_launches(nb));
+    launch_imp_pc_correct(r->imp, r->partials, nb, dt, c9, static_cast<double>(r->g.n), r->s);
   }
 }
 

@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   C2<R>* fwd = fft_smem<R, -1>(a, b, ncol, ld, ax, tws);
   C2<R>* s1 = fwd == a ? b : a;
   for (int o = 0; o < nout; ++o) {
-    const R* fac = fl.f[o];
+    const R* fac = o == 0 ? fl.f[0] : (o == 1 ? fl.f[1] : fl.f[2]);  // selected: no local copy
     staged_loop<R>(
         TX * n,
         [&](int w) {
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
         });
     __syncthreads();
     C2<R>* r = fft_smem<R, 1>(s1, c, ncol, ld, ax, tws);
-    C2<R>* dst = fl.out[o];
+    C2<R>* dst = o == 0 ? fl.out[0] : (o == 1 ? fl.out[1] : fl.out[2]);
     const C2<R>* addo = o == 0 ? add : nullptr;
     staged_loop<R>(
         TX * n,
@@ -448,6 +448,16 @@ void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv,
     pot4_impl<float>(g, p, conv, dencg, den, fn, pot4, s);
 }
 
+bool fft_x_c2r_corr(const Grid& g, const FftPlan& p, int prec, void* spec, void* dencg, const void* den, double cp4,
+                    double cpp4, cudaStream_t s) {
+  if ((p.tiles.engine & (ENGINE_R2C | ENGINE_C2R)) != (ENGINE_R2C | ENGINE_C2R)) return false;
+  if (prec == HE4G_PREC_FP64)
+    return reg_c2r_corr<double>(g, p, twx_of<double>(p), static_cast<double2*>(spec), static_cast<double*>(dencg),
+                                static_cast<const double*>(den), cp4, cpp4, s);
+  return reg_c2r_corr<float>(g, p, twx_of<float>(p), static_cast<float2*>(spec), static_cast<float*>(dencg),
+                             static_cast<const float*>(den), (float)cp4, (float)cpp4, s);
+}
+
 size_t fft_smem_bytes(int prec, int pass, const FftPlan& p, int tile) {
   const size_t b = prec == HE4G_PREC_FP64 ? smem_of<double>(pass, p, tile) : smem_of<float>(pass, p, tile);
   return b <= kMaxSmemPerBlock ? b : 0;
@@ -477,6 +487,7 @@ void prepare_impl(const FftPlan& p) {
   for (int sign : {-1, 1}) reg_y<R>(g, p, sp, 1, sign, nullptr, false);
   reg_z<R>(g, p, nullptr, sp, f, 1, 1.0, nullptr, nullptr, false);
   for (int epi : {EPI_STORE, EPI_POT4}) reg_c2r<R>(g, p, nullptr, epi, nullptr, nullptr, nullptr, nullptr, 1, pa, nullptr, false);
+  reg_c2r_corr<R>(g, p, nullptr, nullptr, nullptr, nullptr, (R)0, (R)0, nullptr, false);
 }
 }  // namespace
 

@@ -439,17 +439,31 @@ struct RegDft<R, 20, SIGN> {
 // below 1e-9 K, far under the FP64 tolerance of pot4, and it replaces an FP64
 // tanh, which costs tens of FP64 instructions on a GPU whose FP64 issue
 // bounds this path.
+// In FP32 (the mixed form) the same closed form serves every density; x is
+// clamped at 20, where 1 + t = 2 and 1 - t^2 = 0 to FP32 rounding, so E
+// stays finite and no branch is taken. It avoids tanhf, whose range
+// reduction issues conversion instructions on the FP64 pipe.
+__device__ __forceinline__ float penalty_f32(float x, float bd, float cs) {
+  const float e = __expf(2.f * fminf(x, 20.f));
+  const float inv = __fdividef(1.f, 1.f + e);
+  return (cs * 2.f * e * inv) * (1.f + 2.f * bd * inv);
+}
+
 template <typename R>
 __device__ __forceinline__ R solid_penalty(R d, R beta, R dm, R cs) {
   const R x = beta * (d - dm);
-  if (sizeof(R) == 8 && x < (R)-10) {
-    const float e = expf(2.f * (float)x);
-    const float inv = 1.f / (1.f + e);
-    const float bd = (float)(beta * d);
-    return (R)(((float)cs * 2.f * e * inv) * (1.f + 2.f * bd * inv));
+  if constexpr (sizeof(R) == 4) {
+    return penalty_f32(x, beta * d, cs);
+  } else {
+    if (x < -10.0) {
+      const float e = expf(2.f * (float)x);
+      const float inv = 1.f / (1.f + e);
+      const float bd = (float)(beta * d);
+      return (R)(((float)cs * 2.f * e * inv) * (1.f + 2.f * bd * inv));
+    }
+    const R t = tanh(x);
+    return cs * ((R)1 + t + beta * d * ((R)1 - t * t));
   }
-  const R t = tanh(x);
-  return cs * ((R)1 + t + beta * d * ((R)1 - t * t));
 }
 
 enum { PRO_PLAIN = 0, PRO_CORR = 1, PRO_PROD = 2 };
@@ -507,5 +521,8 @@ bool reg_r2c(const Grid& g, const FftPlan& p, const C2<R>* twx, int pro, const R
 template <typename R>
 bool reg_c2r(const Grid& g, const FftPlan& p, const C2<R>* twx, int epi, const C2<R>* i0, const C2<R>* i1, R* o0,
              R* o1, int nspec, const Pot4Args<R>& pa, cudaStream_t s, bool launch = true);
+template <typename R>
+bool reg_c2r_corr(const Grid& g, const FftPlan& p, const C2<R>* twx, C2<R>* spec, R* dencg, const R* den, R c0,
+                  R c1, cudaStream_t s, bool launch = true);
 
 }  // namespace he4g

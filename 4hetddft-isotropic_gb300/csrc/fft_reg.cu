@@ -136,7 +136,9 @@ __global__ void __launch_bounds__(kRegThreads, sizeof(R) == 8 ? 1 : 2)
   for (int o = 0; o < nout; ++o) {
     C2<R> y[Q];
     if (actB) {
-      const R* fac = fl.f[o];
+      // selected, not indexed: a runtime index into the parameter struct
+      // would copy it to local memory
+      const R* fac = o == 0 ? fl.f[0] : (o == 1 ? fl.f[1] : fl.f[2]);
 #pragma unroll
       for (int j = 0; j < Q; ++j) {
         const R f = __ldg(&fac[base + (kp + P * j) * stride + cb]) * scale;
@@ -155,7 +157,7 @@ __global__ void __launch_bounds__(kRegThreads, sizeof(R) == 8 ? 1 : 2)
     __syncthreads();
     if (actA) {
       const C2<R>* addo = o == 0 ? add : nullptr;
-      C2<R>* dst = fl.out[o];
+      C2<R>* dst = o == 0 ? fl.out[0] : (o == 1 ? fl.out[1] : fl.out[2]);
       C2<R> w[P];
 #pragma unroll
       for (int q = 0; q < P; ++q) w[q] = buf[(u * P + q) * L + ca];
@@ -345,6 +347,122 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_reg(Grid g, FftAxis ax, c
   }
 }
 
+// Inverse x transform of the coarse-grained density spectrum fused with the
+// forward x transform of the correlation prologue g = den*dencg*(cp4 +
+// cpp4*dencg) (poten.f90:62-64) on the same rows: dencg is stored once and
+// never read back. The inverse pass ends with thread k' < P holding the
+// packed row at k' + P*j, which is the input layout of the forward pass with
+// P and Q swapped; the forward spectrum is untangled as in k_x_r2c_reg. The
+// spectrum rows are read and then overwritten by the same block.
+template <typename R, int P, int Q>
+__global__ void __launch_bounds__(kRegThreads) k_x_c2r_corr_reg(Grid g, FftAxis ax, const C2<R>* __restrict__ twx,
+                                                                C2<R>* spec, R* __restrict__ dencg,
+                                                                const R* __restrict__ den, R c0, R c1) {
+  constexpr int M = P * Q;
+  constexpr int L = reg_lines<P, Q>();
+  constexpr int LD = M + (P > Q ? P : Q) + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
+  C2<R>* tws = buf + L * LD;
+  const long long nlines = (long long)g.ny * g.nz;
+  const long long row0 = (long long)blockIdx.x * L;
+  const int nrows = (int)min((long long)L, nlines - row0);
+  const int tid = threadIdx.x;
+  // inverse pass, first half: thread (ra, u), u < Q, tangles X[k], X[M-k]
+  const int ra = tid / Q, u = tid % Q;
+  const bool actA = ra < nrows;
+  {
+    C2<R> v[P];
+    if (actA) {
+      const C2<R>* x = spec + (row0 + ra) * g.nxh;
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const int k = Q * p + u;
+        const C2<R> xk = x[k];
+        const C2<R> xm = x[M - k];
+        if (k == 0) {
+          v[p] = mk<R>(xk.x + xm.x, xk.x - xm.x);
+        } else {
+          const C2<R> fe = cadd<R>(xk, cconj<R>(xm));
+          const C2<R> fo = mulw<R, 1>(csub<R>(xk, cconj<R>(xm)), __ldg(&twx[k]));
+          v[p] = cadd<R>(fe, jmul<R, 1>(fo));
+        }
+      }
+    }
+    stage_tw<R>(tws, twiddles<R>(ax), M);
+    __syncthreads();
+    if (actA) {
+      RegDft<R, P, 1>::run(v);
+#pragma unroll
+      for (int k = 1; k < P; ++k) v[k] = mulw<R, 1>(v[k], tws[u * k]);
+#pragma unroll
+      for (int k = 0; k < P; ++k) buf[ra * LD + xpad<Q>(k * Q + u)] = v[k];
+    }
+  }
+  __syncthreads();
+  // inverse pass, second half, then the prologue and the forward pass's
+  // first half: thread (rb, k'), k' < P
+  const int rb = tid / P, kp = tid % P;
+  const bool actB = rb < L && rb < nrows;
+  C2<R> w[Q];
+  if (actB) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) w[q] = buf[rb * LD + xpad<Q>(kp * Q + q)];
+    RegDft<R, Q, 1>::run(w);
+    const long long rowe = (row0 + rb) * g.nx;
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+      const long long e = rowe + 2 * (kp + P * j);
+      const C2<R> cg = w[j];
+      *reinterpret_cast<C2<R>*>(dencg + e) = cg;
+      const C2<R> d = ld_pair<R>(den + e);
+      w[j] = mk<R>(d.x * cg.x * fma(c1, cg.x, c0), d.y * cg.y * fma(c1, cg.y, c0));
+    }
+    RegDft<R, Q, -1>::run(w);
+#pragma unroll
+    for (int k = 1; k < Q; ++k) w[k] = mulw<R, -1>(w[k], tws[kp * k]);
+  }
+  __syncthreads();  // the exchange buffer is free again
+  if (actB) {
+#pragma unroll
+    for (int k = 0; k < Q; ++k) buf[rb * LD + xpad<P>(k * P + kp)] = w[k];
+  }
+  __syncthreads();
+  // forward pass, second half: thread (rc, kq), kq < Q, holds Z[kq + Q*jj]
+  const int rc = tid / Q, kq = tid % Q;
+  const bool actC = rc < L && rc < nrows;
+  C2<R> z[P];
+  if (actC) {
+#pragma unroll
+    for (int pp = 0; pp < P; ++pp) z[pp] = buf[rc * LD + xpad<P>(kq * P + pp)];
+    RegDft<R, P, -1>::run(z);
+  }
+  __syncthreads();
+  if (actC) {
+#pragma unroll
+    for (int jj = 0; jj < P; ++jj) buf[rc * LD + kq + Q * jj] = z[jj];
+  }
+  __syncthreads();
+  // untangle into the half spectrum (2*DFT convention), over the same rows
+  constexpr int H = M / 2 + 1;
+  for (int it = tid; it < nrows * H; it += kRegThreads) {
+    const int l = it / H, k = it - l * H;
+    const C2<R> zk = buf[l * LD + k];
+    const C2<R> zm = buf[l * LD + (k == 0 ? 0 : M - k)];
+    C2<R>* o = spec + (row0 + l) * g.nxh;
+    if (k == 0) {
+      o[0] = mk<R>((R)2 * (zk.x + zk.y), (R)0);
+      o[M] = mk<R>((R)2 * (zk.x - zk.y), (R)0);
+      continue;
+    }
+    const C2<R> fe = cadd<R>(zk, cconj<R>(zm));
+    const C2<R> fo = jmul<R, -1>(csub<R>(zk, cconj<R>(zm)));
+    const C2<R> t = mulw<R, -1>(fo, __ldg(&twx[k]));
+    o[k] = cadd<R>(fe, t);
+    o[M - k] = cconj<R>(csub<R>(fe, t));
+  }
+}
+
 // ------------------------------------------------------------ launchers
 template <typename R, int P, int Q, int SIGN>
 void run_y(const Grid& g, const FftPlan& p, const SpecList<R>& sl, int nspec, cudaStream_t s, bool launch) {
@@ -391,6 +509,19 @@ void run_c2r(const Grid& g, const FftPlan& p, const C2<R>* twx, const C2<R>* i0,
   const long long nlines = (long long)g.ny * g.nz;
   dim3 grid((unsigned)((nlines + L - 1) / L), nspec);
   k_x_c2r_reg<R, P, Q, EPI><<<grid, kRegThreads, smem, s>>>(g, p.xh, twx, i0, i1, o0, o1, pa);
+}
+
+template <typename R, int P, int Q>
+void run_c2r_corr(const Grid& g, const FftPlan& p, const C2<R>* twx, C2<R>* spec, R* dencg, const R* den, R c0,
+                  R c1, cudaStream_t s, bool launch) {
+  constexpr int L = reg_lines<P, Q>();
+  constexpr int LD = P * Q + (P > Q ? P : Q) + 1;
+  const size_t smem = sizeof(C2<R>) * (L * LD + P * Q);
+  set_smem(k_x_c2r_corr_reg<R, P, Q>, smem);
+  if (!launch) return;
+  const long long nlines = (long long)g.ny * g.nz;
+  dim3 grid((unsigned)((nlines + L - 1) / L));
+  k_x_c2r_corr_reg<R, P, Q><<<grid, kRegThreads, smem, s>>>(g, p.xh, twx, spec, dencg, den, c0, c1);
 }
 
 // Transform lengths with a register split N = P*Q (P, Q <= 16).
@@ -496,6 +627,24 @@ bool reg_c2r(const Grid& g, const FftPlan& p, const C2<R>* twx, int epi, const C
   return false;
 }
 
+template <typename R>
+bool reg_c2r_corr(const Grid& g, const FftPlan& p, const C2<R>* twx, C2<R>* spec, R* dencg, const R* den, R c0,
+                  R c1, cudaStream_t s, bool launch) {
+  switch (p.xh.n) {
+#define HE4G_CASE(N, P, Q)                                                  \
+  case N:                                                                   \
+    run_c2r_corr<R, P, Q>(g, p, twx, spec, dencg, den, c0, c1, s, launch);   \
+    return true;
+    HE4G_REG_SIZES(HE4G_CASE)
+#undef HE4G_CASE
+  }
+  return false;
+}
+
+template bool reg_c2r_corr<double>(const Grid&, const FftPlan&, const double2*, double2*, double*, const double*,
+                                   double, double, cudaStream_t, bool);
+template bool reg_c2r_corr<float>(const Grid&, const FftPlan&, const float2*, float2*, float*, const float*, float,
+                                  float, cudaStream_t, bool);
 template bool reg_y<double>(const Grid&, const FftPlan&, void* const*, int, int, cudaStream_t, bool);
 template bool reg_y<float>(const Grid&, const FftPlan&, void* const*, int, int, cudaStream_t, bool);
 template bool reg_z<double>(const Grid&, const FftPlan&, const void*, void* const*, const void* const*, int, double,

@@ -346,34 +346,50 @@ __device__ __forceinline__ void block_sum_dw(float (&h)[NV], float (&l)[NV], dou
 }
 
 // Blocks of kFX x kFY columns march kZF planes. Each plane's den tile with
-// its 6-point halo (kTW x kTH) is staged in shared memory, so the 24 x/y
-// neighbours are shared-memory reads at fixed offsets; the z neighbours stay
-// in a per-column register window. The loads of a plane are issued before
-// the barrier that frees the tile, so they overlap the previous plane.
+// its halo (6 points in y; in x from 8 left, so that it starts on a 16-byte
+// boundary, to 8 right) is staged in shared memory, so the 24 x/y neighbours
+// are shared-memory reads at fixed offsets; the z neighbours stay in a
+// per-column register window. When nx is a multiple of 4 a plane's tile is
+// 240 aligned 16-byte loads (one per thread), each wholly inside or outside
+// the grid; otherwise it is loaded point by point. The loads of a plane are
+// issued before the barrier that frees the tile, so they overlap the
+// previous plane.
 constexpr int kFX = 32, kFY = 8;
-constexpr int kTW = kFX + 2 * kStencilHalf, kTH = kFY + 2 * kStencilHalf;
+constexpr int kTX0 = 8;                            // tile column 0 is x0 - 8
+constexpr int kTW = kFX + 2 * kTX0;                // 48
+constexpr int kTH = kFY + 2 * kStencilHalf;        // 20
+constexpr int kTileVec = (kTW / 4) * kTH;          // 240 float4 per plane
 constexpr int kTileSlots = (kTW * kTH + kFX * kFY - 1) / (kFX * kFY);
 
 __global__ void __launch_bounds__(kFX * kFY) k_force_mp(Grid g, StencilF st, const float* __restrict__ den,
                                                          ImpTable tab, ImpState* imp, int center_sel,
                                                          float* uimp_out, double* partials) {
   __shared__ float cf[3];
-  __shared__ float tile[kTH * kTW];
+  __shared__ __align__(16) float tile[kTH * kTW];
   load_center(imp, center_sel, cf);
   const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * kFX + lx;
   const int x0 = blockIdx.x * kFX, y0 = blockIdx.y * kFY, k0 = blockIdx.z * kZF;
   const int i = x0 + lx, j = y0 + ly;
   const bool own = i < g.nx && j < g.ny;
   const long long sz = (long long)g.nx * g.ny;
-  // this thread's slots of the tile: in-plane offset and whether in the grid
+  const bool vec = (g.nx & 3) == 0;  // uniform over the grid
+  // this thread's tile slots: in-plane offset and whether in the grid
+  int voff = 0;
+  bool vok = false;
+  if (tid < kTileVec) {
+    const int ty = tid / (kTW / 4), c4 = tid - ty * (kTW / 4);
+    const int gx = x0 - kTX0 + 4 * c4, gy = y0 - kStencilHalf + ty;
+    vok = gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
+    voff = vok ? gy * g.nx + gx : 0;
+  }
   int toff[kTileSlots];
   bool tok[kTileSlots];
 #pragma unroll
   for (int s = 0; s < kTileSlots; ++s) {
     const int idx = tid + s * kFX * kFY;
     const int ty = idx / kTW, tx = idx - ty * kTW;
-    const int gx = x0 - kStencilHalf + tx, gy = y0 - kStencilHalf + ty;
-    tok[s] = idx < kTW * kTH && gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
+    const int gx = x0 - kTX0 + tx, gy = y0 - kStencilHalf + ty;
+    tok[s] = !vec && idx < kTW * kTH && gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
     toff[s] = tok[s] ? gy * g.nx + gx : 0;
   }
   float dx = 0.f, dy = 0.f;
@@ -390,20 +406,26 @@ __global__ void __launch_bounds__(kFX * kFY) k_force_mp(Grid g, StencilF st, con
     dy = __ldg(tab.ys + j) - cf[1];
   }
   float s[3] = {0.f, 0.f, 0.f}, cc[3] = {0.f, 0.f, 0.f};
-  const float* t0 = tile + (ly + kStencilHalf) * kTW + lx + kStencilHalf;  // this point in the tile
+  const float* t0 = tile + (ly + kStencilHalf) * kTW + lx + kTX0;  // this point in the tile
 #pragma unroll
   for (int m = 0; m < kZF; ++m) {
     const int k = k0 + m;
     if (k >= g.nz) break;  // uniform over the block
     const float* plane = den + k * sz;
-    float tv[kTileSlots];
+    if (vec) {
+      const float4 v = vok ? __ldg(reinterpret_cast<const float4*>(plane + voff)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      __syncthreads();  // the previous plane's reads of the tile are done
+      if (tid < kTileVec) reinterpret_cast<float4*>(tile)[tid] = v;
+    } else {
+      float tv[kTileSlots];
 #pragma unroll
-    for (int q = 0; q < kTileSlots; ++q) tv[q] = tok[q] ? __ldg(plane + toff[q]) : 0.f;
-    __syncthreads();  // the previous plane's reads of the tile are done
+      for (int q = 0; q < kTileSlots; ++q) tv[q] = tok[q] ? __ldg(plane + toff[q]) : 0.f;
+      __syncthreads();
 #pragma unroll
-    for (int q = 0; q < kTileSlots; ++q) {
-      const int idx = tid + q * kFX * kFY;
-      if (idx < kTW * kTH) tile[idx] = tv[q];
+      for (int q = 0; q < kTileSlots; ++q) {
+        const int idx = tid + q * kFX * kFY;
+        if (idx < kTW * kTH) tile[idx] = tv[q];
+      }
     }
     __syncthreads();
     if (own) {
@@ -509,6 +531,11 @@ __global__ void __launch_bounds__(256) k_energy_point_mp(Grid g, Functional fn, 
 }
 
 }  // namespace
+
+int pc_blocks_mp(const Grid& g) {
+  const dim3 d = point_grid(g);
+  return (int)(d.x * d.y * d.z);
+}
 
 int force_blocks_mp(const Grid& g) {
   return ((g.nx + kFX - 1) / kFX) * ((g.ny + kFY - 1) / kFY) * ((g.nz + kZF - 1) / kZF);

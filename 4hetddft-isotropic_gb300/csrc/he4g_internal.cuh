@@ -133,6 +133,12 @@ void fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void*
                 const void* const* factors, int nout, double scale, const void* add, cudaStream_t s);
 void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins, void* const* outs, int nspec,
                cudaStream_t s);
+// c2r of the coarse-grained density spectrum (stored to dencg) fused with the
+// r2c of g = den*dencg*(cp4 + cpp4*dencg) back into spec; register engine
+// only (both x-pass engine bits set and a specialised length), else returns
+// false and launches nothing
+bool fft_x_c2r_corr(const Grid& g, const FftPlan& p, int prec, void* spec, void* dencg, const void* den, double cp4,
+                    double cpp4, cudaStream_t s);
 // c2r of delj4 + correlation convolution fused with the rest of pot4
 // (poten.f90:80-94,110-114)
 void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv, const void* dencg,
@@ -223,6 +229,8 @@ struct ImpTable {
 void launch_potenimp_mp(const Grid& g, const ImpTable& tab, ImpState* imp, int center_sel, float* uimp,
                         cudaStream_t s);
 int force_blocks_mp(const Grid& g);
+// partial-sum blocks of launch_pc_correct_mp
+int pc_blocks_mp(const Grid& g);
 // potenimp fused into the force sum: uimp is evaluated in place from the
 // centre (stored to uimp_out when not null)
 void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const ImpTable& tab, ImpState* imp,
