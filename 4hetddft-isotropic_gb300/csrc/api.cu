@@ -109,6 +109,7 @@ struct he4g_run {
   float *xsf = nullptr, *ysf = nullptr, *zsf = nullptr;
 
   double* partials = nullptr;
+  unsigned* counters = nullptr;  // completion counters of the finishing kernels (zero between kernels)
   double* small = nullptr;  // reduction outputs / cm
   ImpState* imp = nullptr;
   double* ring = nullptr;
@@ -180,6 +181,11 @@ struct Tick {
       a = take_event(r);
       cudaEventRecord(a, r->s);
     }
+  }
+  // the guarded call launched k kernels in all
+  void launched(int k) {
+    r->launches += k - n;
+    n = k;
   }
   // the guarded launch did not happen
   void cancel() {
@@ -497,33 +503,29 @@ void delj4_dev(he4g_run* r) {
 // The mixed form evaluates uimp inside the force kernel about centre `sel`
 // (potenimp_dev's selector) and stores it when `store_uimp` is set, which
 // replaces a separate potenimp launch; the FP64 form reads the stored uimp.
-void force_dev(he4g_run* r, int store_accel, int sel = 1, bool store_uimp = false) {
-  int nb;
-  {
-    Tick t(r, F_FORCE);
-    if (mixed(r)) {
-      launch_force_mp(r->g, r->stf, static_cast<const float*>(r->den), imp_table(r), r->imp, sel,
-                      store_uimp ? static_cast<float*>(r->uimp) : nullptr, r->partials, r->s);
-      nb = r->fblocks;
-    } else {
-      launch_force(r->g, r->st, static_cast<const double*>(r->den), static_cast<const double*>(r->uimp), nullptr,
-                   nullptr, nullptr, r->partials, r->s);
-      nb = r->fblocks;
-    }
-  }
-  Tick t(r, F_SCALAR, 1 + fold_launches(nb));
-  launch_imp_force(r->imp, r->partials, nb, r->g.dxyz, r->mass, store_accel, r->s);
+// The kernel's last block applies F (and, with `record`, writes the step's
+// trajectory row).
+void force_dev(he4g_run* r, int store_accel, int sel = 1, bool store_uimp = false, bool record = false) {
+  const ForceFinish fin{r->imp, r->counters, record ? r->ring : nullptr, r->g.dxyz, r->mass, store_accel};
+  Tick t(r, F_FORCE);
+  if (mixed(r))
+    t.launched(launch_force_mp(r->g, r->stf, static_cast<const float*>(r->den), imp_table(r), r->imp, sel,
+                               store_uimp ? static_cast<float*>(r->uimp) : nullptr, r->partials, fin, r->s));
+  else
+    t.launched(launch_force(r->g, r->st, static_cast<const double*>(r->den), static_cast<const double*>(r->uimp),
+                            nullptr, nullptr, nullptr, r->partials, fin, r->s));
 }
 
-// potenimp(centre sel); poten(); forceimp(rimp, aimp); aimp /= m
-void evaluate_at(he4g_run* r, int sel) {
+// potenimp(centre sel); poten(); forceimp(rimp, aimp); aimp /= m;
+// record: the step's trajectory row after the force
+void evaluate_at(he4g_run* r, int sel, bool record = false) {
   if (mixed(r)) {
     poten_dev(r);  // does not read uimp
-    force_dev(r, 1, sel, true);
+    force_dev(r, 1, sel, true, record);
   } else {
     potenimp_dev(r, sel);
     poten_dev(r);
-    force_dev(r, 1);
+    force_dev(r, 1, sel, false, record);
   }
 }
 void evaluate_dev(he4g_run* r) { evaluate_at(r, 0); }
@@ -620,41 +622,33 @@ void steppc_dev(he4g_run* r, double dt) {
       launch_pc_predict_mp(r->g, r->stf, r->fn, r->psi32[r->cur32], r->old[2], r->psi32[1 - r->cur32],
                            static_cast<const float2*>(r->h[0]), static_cast<float2*>(r->h[1]), r->pc,
                            static_cast<const float*>(r->pot4), static_cast<const float*>(r->uimp), r->timec,
-                           static_cast<float*>(r->den), c4o3 * dt, c112, r->s);
+                           static_cast<float*>(r->den), c4o3 * dt, c112, r->imp, r->s);
     } else {
       launch_pc_predict(r->g, r->st, r->fn, r->psi, r->old[2], static_cast<double2*>(r->h[0]),
                         static_cast<double2*>(r->h[1]), r->pc, static_cast<const double*>(r->pot4),
                         static_cast<const double*>(r->uimp), r->timec, static_cast<double*>(r->den), c4o3 * dt, c112,
-                        r->s);
+                        r->imp, r->s);
     }
   }
   double2* psit = roles_after_predict(r);
-  {
-    Tick t(r, F_SCALAR);
-    launch_imp_pc_predict(r->imp, c4o3 * dt, c112, r->s);
-  }
   evaluate_at(r, 1);
+  const PcFinish fin{r->imp, r->counters, dt, c9, static_cast<double>(r->g.n)};
   {
     Tick t(r, F_PC_CORRECT);
     if (mp) {
-      launch_pc_correct_mp(r->g, r->stf, r->fn, r->psi32[r->cur32], r->old[2], r->old[1],
+      t.launched(launch_pc_correct_mp(r->g, r->stf, r->fn, r->psi32[r->cur32], r->old[2], r->old[1],
                            static_cast<const float2*>(r->h[0]), static_cast<const float2*>(r->h[1]), r->pc,
                            static_cast<const float*>(r->pot4), static_cast<const float*>(r->uimp), r->timec,
                            r->scratch, r->psi32[1 - r->cur32], static_cast<float*>(r->den), r->partials, 3.0 * dt, c9,
-                           &r->imp->health, r->s);
+                           &r->imp->health, fin, r->s));
     } else {
-      launch_pc_correct(r->g, r->st, r->fn, psit, r->old[2], r->old[1], static_cast<const double2*>(r->h[0]),
+      t.launched(launch_pc_correct(r->g, r->st, r->fn, psit, r->old[2], r->old[1], static_cast<const double2*>(r->h[0]),
                         static_cast<const double2*>(r->h[1]), r->pc, static_cast<const double*>(r->pot4),
                         static_cast<const double*>(r->uimp), r->timec, r->scratch, static_cast<double*>(r->den),
-                        r->partials, 3.0 * dt, c9, &r->imp->health, r->s);
+                        r->partials, 3.0 * dt, c9, &r->imp->health, fin, r->s));
     }
   }
   roles_after_correct(r, psit);
-  {
-    const int nb = mp ? pc_blocks_mp(r->g) : r->pblocks;
-    Tick t(r, F_SCALAR, 1 + fold_launches(nb));
-    launch_imp_pc_correct(r->imp, r->partials, nb, dt, c9, static_cast<double>(r->g.n), r->s);
-  }
 }
 
 int step_impl(he4g_run* r, int nsteps, cudaEvent_t stop);
@@ -674,9 +668,7 @@ int sync_err(he4g_run* r, const char* where) {
 // the launches of one predictor-corrector step and the trailing evaluation
 void pc_step_launches(he4g_run* r) {
   steppc_dev(r, r->cfg.deltat);
-  evaluate_dev(r);
-  Tick t(r, F_SCALAR);
-  launch_imp_record(r->imp, r->ring, r->s);
+  evaluate_at(r, 0, true);
 }
 
 GraphKey current_key(const he4g_run* r) {
@@ -797,6 +789,7 @@ int he4g_footprint(const he4g_config* c, uint64_t* bytes) {
   }
   const uint64_t pblocks = (uint64_t)((c->nx + 63) / 64) * ((c->ny + 3) / 4) * c->nz;
   add(pblocks * 12 * 8);
+  add(he4g::kFinishCounters * 4);
   add(64 * 8);
   add(sizeof(ImpState));
   add((uint64_t)kRingRows * kRingCols * 8);
@@ -915,6 +908,7 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   r->pblocks = pc_blocks(g);
   r->fblocks = r->prec == HE4G_PREC_MIXED ? force_blocks_mp(g) : force_blocks(g);
   chk(r->partials = dalloc<double>(r, (size_t)r->pblocks * 12));
+  chk(r->counters = dalloc<unsigned>(r, kFinishCounters, true));
   chk(r->small = dalloc<double>(r, 64));
   chk(r->imp = dalloc<ImpState>(r, 1));
   chk(r->ring = dalloc<double>(r, (size_t)kRingRows * kRingCols));

@@ -16,6 +16,7 @@
 
 #include "fpconv.cuh"
 #include "he4g_internal.cuh"
+#include "impurity.cuh"
 
 namespace he4g {
 
@@ -149,8 +150,10 @@ __global__ void __launch_bounds__(256) k_pc_predict(Grid g, Stencil st, Function
                                                      double2* pc, const double* __restrict__ pot4,
                                                      const double* __restrict__ uimp,
                                                      const float* __restrict__ timec, double* den,
-                                                     double c4o3dt, double c112) {
+                                                     double c4o3dt, double c112, ImpState* imp) {
   const Pt t = point(g);
+  if (imp && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    imp_pc_predict_body(imp, c4o3dt, c112);
   if (!t.ok) return;
   const double2 lap = lap13(psi, t, g, st);
   const double2 ps = ld2(psi + t.p);
@@ -179,7 +182,7 @@ __global__ void __launch_bounds__(256) k_pc_correct(Grid g, Stencil st, Function
                                                      const double* __restrict__ uimp,
                                                      const float* __restrict__ timec, double2* psi_out,
                                                      double* den, double* partials, double f3, double c9,
-                                                     int* health) {
+                                                     int* health, PcFinish fin) {
   const Pt t = point(g);
   float v = 0.f;
   if (t.ok) {
@@ -206,6 +209,11 @@ __global__ void __launch_bounds__(256) k_pc_correct(Grid g, Stencil st, Function
     if (h) atomicOr(health, h);
   }
   block_sum_f1(v, partials);
+  if (threadIdx.y * blockDim.x + threadIdx.x >= 32) return;  // warp 0 finishes (when fin.cnt is set)
+  double tot[1];
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  if (fin.cnt && finish_sum<1>(partials, nb, fin.cnt, tot) && threadIdx.x == 0 && threadIdx.y == 0)
+    imp_pc_correct_body(fin.imp, tot[0], fin.dt, fin.c9, fin.nxyz);
 }
 
 // One Runge–Kutta–Gill stage (steprk.f90:57-92). f_out (stage 1 only)
@@ -297,7 +305,7 @@ constexpr int kZD = 8;
 
 __global__ void __launch_bounds__(256) k_force(Grid g, Stencil st, const double* __restrict__ den,
                                                 const double* __restrict__ uimp, double* dx, double* dy,
-                                                double* dz, double* partials) {
+                                                double* dz, double* partials, ForceFinish fin) {
   const int i = blockIdx.x * kBX + threadIdx.x;
   const int j = blockIdx.y * kBY + threadIdx.y;
   const int k0 = blockIdx.z * kZD;
@@ -341,6 +349,13 @@ __global__ void __launch_bounds__(256) k_force(Grid g, Stencil st, const double*
     }
   }
   block_sum<3>(v, partials);
+  if (threadIdx.y * blockDim.x + threadIdx.x >= 32) return;  // warp 0 finishes (when fin.cnt is set)
+  double tot[3];
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  if (fin.cnt && finish_sum<3>(partials, nb, fin.cnt, tot) && threadIdx.x == 0 && threadIdx.y == 0) {
+    imp_force_body(fin.imp, tot, fin.dxyz, fin.mass, fin.store_accel);
+    if (fin.ring) imp_record_body(fin.imp, fin.ring);
+  }
 }
 
 // one-axis first derivative of a real field (Deriv3D_p, id = 1)
@@ -477,17 +492,9 @@ __global__ void __launch_bounds__(kFinalThreads) k_reduce(const double* partials
   reduce_cols(partials, nblocks, nvals, out);
 }
 
-}  // namespace
-
-int fold_launches(int nblocks) { return nblocks > 4 * 256 ? 1 : 0; }  // 256 = kFold
-
-namespace {
-
-// First level of the per-step sums: block c adds rows [c*kFold, (c+1)*kFold)
-// of partials[nblocks][nvals] in a fixed tree order into folded[c][nvals],
-// so that the single block of the impurity update reads a few hundred rows
-// instead of one per grid block (FP64 adds of one block run at the FP64 rate
-// of one SM).
+// ---------------------------------- separate finish of large grids' sums
+// First level: block c adds rows [c*kFold, (c+1)*kFold) of
+// partials[nblocks][nvals] in a fixed tree order into folded[c][nvals].
 constexpr int kFold = 256;
 __global__ void __launch_bounds__(kFold) k_fold(const double* __restrict__ partials, int nblocks, int nvals,
                                                  double* __restrict__ folded) {
@@ -505,16 +512,31 @@ __global__ void __launch_bounds__(kFold) k_fold(const double* __restrict__ parti
   }
 }
 
-// Folds partials in place when there are many rows: the folded rows go right
-// after the nblocks*nvals values (callers size partials for that); returns
-// the rows the final reduction reads.
-const double* fold_partials(const double* partials, int& nblocks, int nvals, cudaStream_t s) {
-  if (!fold_launches(nblocks)) return partials;
+// folds in place when there are many rows (the folded rows go right after
+// the nblocks*nvals values); returns the rows left and counts the launch
+const double* fold_partials(const double* partials, int& nblocks, int nvals, int& launches, cudaStream_t s) {
+  if (nblocks <= 4 * kFold) return partials;
   double* folded = const_cast<double*>(partials) + (long long)nblocks * nvals;
   const int nc = (nblocks + kFold - 1) / kFold;
   k_fold<<<nc, kFold, 0, s>>>(partials, nblocks, nvals, folded);
+  ++launches;
   nblocks = nc;
   return folded;
+}
+
+__global__ void __launch_bounds__(kFinalThreads) k_finish_force(const double* partials, int nblocks,
+                                                             ForceFinish fin) {
+  __shared__ double tot[3];
+  reduce_cols(partials, nblocks, 3, tot);
+  if (threadIdx.x == 0) {
+    imp_force_body(fin.imp, tot, fin.dxyz, fin.mass, fin.store_accel);
+    if (fin.ring) imp_record_body(fin.imp, fin.ring);
+  }
+}
+__global__ void __launch_bounds__(kFinalThreads) k_finish_pc(const double* partials, int nblocks, PcFinish fin) {
+  __shared__ double tot[1];
+  reduce_cols(partials, nblocks, 1, tot);
+  if (threadIdx.x == 0) imp_pc_correct_body(fin.imp, tot[0], fin.dt, fin.c9, fin.nxyz);
 }
 
 // ------------------------------------------------- impurity scalar updates
@@ -552,101 +574,9 @@ __global__ void k_imp_rk(ImpState* s, int stage, double ar, double br, double cr
   }
 }
 
-// predictor + modifier of (r, v) (steppc.f90:77-100); sets the potential
-// centre to the predicted position
-__global__ void k_imp_pc_predict(ImpState* s, double f, double c112) {
-  if (threadIdx.x != 0) return;
-  double aux[3];
-  int* ir = s->ioldr;
-  int* iv = s->ioldv;
-  int* ia = s->iolda;
-  for (int a = 0; a < 3; ++a)
-    aux[a] = s->rimpold[ir[2]][a] + f * (2.0 * s->vimp[a] - s->vimpold[iv[0]][a] + 2.0 * s->vimpold[iv[1]][a]);
-  for (int a = 0; a < 3; ++a) {
-    s->rimpold[ir[2]][a] = aux[a] - c112 * s->pcr[a];
-    s->pcr[a] = aux[a];
-  }
-  for (int a = 0; a < 3; ++a)
-    aux[a] = s->vimpold[iv[2]][a] + f * (2.0 * s->aimp[a] - s->aimpold[ia[0]][a] + 2.0 * s->aimpold[ia[1]][a]);
-  for (int a = 0; a < 3; ++a) {
-    s->vimpold[iv[2]][a] = aux[a] - c112 * s->pcv[a];
-    s->pcv[a] = aux[a];
-  }
-  for (int a = 0; a < 3; ++a) s->aimpold[ia[1]][a] = s->aimp[a];
-  const int t = ia[1];
-  ia[1] = ia[0];
-  ia[0] = t;
-  for (int a = 0; a < 3; ++a) s->center[a] = s->rimpold[ir[2]][a];
-}
-
-// errHe reduction + corrector of (r, v) (steppc.f90:131-174)
-__global__ void __launch_bounds__(kFinalThreads) k_imp_pc_correct(ImpState* s, const double* partials, int nblocks,
-                                                               double dt, double c9, double nxyz) {
-  __shared__ double tot[1];
-  reduce_cols(partials, nblocks, 1, tot);
-  if (threadIdx.x != 0) return;
-  s->errHe = (c9 * tot[0]) / nxyz;
-  double aux[3];
-  int* ir = s->ioldr;
-  int* iv = s->ioldv;
-  int* ia = s->iolda;
-  const double f3 = 3.0 * dt;
-  for (int a = 0; a < 3; ++a)
-    aux[a] = 0.125 * (9.0 * s->rimp[a] - s->rimpold[ir[1]][a] +
-                      f3 * (s->vimpold[iv[2]][a] + 2.0 * s->vimp[a] - s->vimpold[iv[0]][a]));
-  double ei = 0.0;
-  for (int a = 0; a < 3; ++a) {
-    s->pcr[a] = s->pcr[a] - aux[a];
-    s->rimpold[ir[2]][a] = s->rimp[a];
-    s->rimp[a] = aux[a] + c9 * s->pcr[a];
-    ei += fabs(c9 * s->pcr[a]);
-  }
-  s->errimp = ei * 0.3333333333;
-  int t = ir[2];
-  ir[2] = ir[1];
-  ir[1] = ir[0];
-  ir[0] = t;
-  for (int a = 0; a < 3; ++a)
-    aux[a] = 0.125 * (9.0 * s->vimp[a] - s->vimpold[iv[1]][a] +
-                      f3 * (s->aimp[a] + 2.0 * s->aimpold[ia[0]][a] - s->aimpold[ia[1]][a]));
-  for (int a = 0; a < 3; ++a) {
-    s->pcv[a] = s->pcv[a] - aux[a];
-    s->vimpold[iv[2]][a] = s->vimp[a];
-    s->vimp[a] = aux[a] + c9 * s->pcv[a];
-  }
-  t = iv[2];
-  iv[2] = iv[1];
-  iv[1] = iv[0];
-  iv[0] = t;
-}
-
-// F = -sum(grad den * uimp) * dxyz; aimp = F / m when store_accel
-__global__ void __launch_bounds__(kFinalThreads) k_imp_force(ImpState* s, const double* partials, int nblocks,
-                                                          double dxyz, double mass, int store_accel) {
-  __shared__ double tot[3];
-  reduce_cols(partials, nblocks, 3, tot);
-  if (threadIdx.x != 0) return;
-  for (int a = 0; a < 3; ++a) {
-    const double F = -tot[a] * dxyz;
-    s->force[a] = F;
-    if (store_accel) s->aimp[a] = F / mass;
-  }
-}
-
-// one trajectory row per step; the step number is the count of rows written
-// since set_state, kept on the device so that a captured step graph records
-// the right number on every replay
+// one trajectory row (impurity.cuh)
 __global__ void k_imp_record(ImpState* s, double* ring) {
-  if (threadIdx.x != 0) return;
-  const long long row = s->ring_head % kRingRows;
-  double* r = ring + row * kRingCols;
-  r[0] = (double)(s->ring_head + 1);
-  for (int a = 0; a < 3; ++a) {
-    r[1 + a] = s->rimp[a];
-    r[4 + a] = s->vimp[a];
-    r[7 + a] = s->aimp[a];
-  }
-  s->ring_head += 1;
+  if (threadIdx.x == 0) imp_record_body(s, ring);
 }
 
 // den = |psi|^2 (DFT4He3d.f90:637)
@@ -696,17 +626,33 @@ int energy_blocks(const Grid& g) { return point_blocks(g); }
 void launch_pc_predict(const Grid& g, const Stencil& st, const Functional& fn, const double2* psi,
                        double2* p3_out, double2* h1, double2* h2_out, double2* pc, const double* pot4,
                        const double* uimp, const float* timec, double* den, double c4o3dt, double c112,
-                       cudaStream_t s) {
+                       ImpState* imp, cudaStream_t s) {
   k_pc_predict<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, fn, psi, p3_out, h1, h2_out, pc, pot4, uimp,
-                                                        timec, den, c4o3dt, c112);
+                                                        timec, den, c4o3dt, c112, imp);
 }
-void launch_pc_correct(const Grid& g, const Stencil& st, const Functional& fn, const double2* psit,
-                       const double2* p3, const double2* p2, const double2* h1, const double2* h2,
-                       double2* pc, const double* pot4, const double* uimp, const float* timec,
-                       double2* psi_out, double* den, double* partials, double f3, double c9, int* health,
-                       cudaStream_t s) {
+int launch_pc_correct(const Grid& g, const Stencil& st, const Functional& fn, const double2* psit,
+                      const double2* p3, const double2* p2, const double2* h1, const double2* h2,
+                      double2* pc, const double* pot4, const double* uimp, const float* timec,
+                      double2* psi_out, double* den, double* partials, double f3, double c9, int* health,
+                      const PcFinish& fin, cudaStream_t s) {
+  const int nb = point_blocks(g);
+  PcFinish f = fin;
+  if (nb > kFinishInKernelMax) f.cnt = nullptr;
   k_pc_correct<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, fn, psit, p3, p2, h1, h2, pc, pot4, uimp,
-                                                        timec, psi_out, den, partials, f3, c9, health);
+                                                        timec, psi_out, den, partials, f3, c9, health, f);
+  return 1 + (f.cnt ? 0 : launch_finish_pc(partials, nb, fin, s));
+}
+int launch_finish_pc(const double* partials, int nblocks, const PcFinish& fin, cudaStream_t s) {
+  int launches = 1;
+  const double* p = fold_partials(partials, nblocks, 1, launches, s);
+  k_finish_pc<<<1, kFinalThreads, 0, s>>>(p, nblocks, fin);
+  return launches;
+}
+int launch_finish_force(const double* partials, int nblocks, const ForceFinish& fin, cudaStream_t s) {
+  int launches = 1;
+  const double* p = fold_partials(partials, nblocks, 3, launches, s);
+  k_finish_force<<<1, kFinalThreads, 0, s>>>(p, nblocks, fin);
+  return launches;
 }
 void launch_rk_stage(const Grid& g, const Stencil& st, const Functional& fn, const double2* psi,
                      double2* psi_out, double2* q, double2* f_out, const double* pot4, const double* uimp,
@@ -722,10 +668,14 @@ void launch_potenimp(const Grid& g, const double* x, const double* y, const doub
   k_potenimp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, x, y, z, potion, npot, delinter, inv,
                                                       const_cast<ImpState*>(imp), center_sel, uimp);
 }
-void launch_force(const Grid& g, const Stencil& st, const double* den, const double* uimp, double* dx,
-                  double* dy, double* dz, double* partials, cudaStream_t s) {
+int launch_force(const Grid& g, const Stencil& st, const double* den, const double* uimp, double* dx,
+                 double* dy, double* dz, double* partials, const ForceFinish& fin, cudaStream_t s) {
   dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZD - 1) / kZD);
-  k_force<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, uimp, dx, dy, dz, partials);
+  const int nb = (int)(grid.x * grid.y * grid.z);
+  ForceFinish f = fin;
+  if (nb > kFinishInKernelMax) f.cnt = nullptr;
+  k_force<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, uimp, dx, dy, dz, partials, f);
+  return 1 + (f.cnt ? 0 : launch_finish_force(partials, nb, fin, s));
 }
 void launch_grad1(const Grid& g, const Stencil& st, int axis, const double* in, double* out, cudaStream_t s) {
   k_grad1<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, axis, in, out);
@@ -767,19 +717,6 @@ void launch_ualphas_b(const Grid& g, double* u, const double* s4, const double* 
 }
 void launch_imp_rk(ImpState* imp, int stage, double ar, double br, double cr, double dt, cudaStream_t s) {
   k_imp_rk<<<1, 32, 0, s>>>(imp, stage, ar, br, cr, dt);
-}
-void launch_imp_pc_predict(ImpState* imp, double c4o3dt, double c112, cudaStream_t s) {
-  k_imp_pc_predict<<<1, 32, 0, s>>>(imp, c4o3dt, c112);
-}
-void launch_imp_pc_correct(ImpState* imp, const double* err_partials, int nblocks, double dt, double c9,
-                           double nxyz, cudaStream_t s) {
-  const double* p = fold_partials(err_partials, nblocks, 1, s);
-  k_imp_pc_correct<<<1, kFinalThreads, 0, s>>>(imp, p, nblocks, dt, c9, nxyz);
-}
-void launch_imp_force(ImpState* imp, const double* partials, int nblocks, double dxyz, double mass,
-                      int store_accel, cudaStream_t s) {
-  const double* p = fold_partials(partials, nblocks, 3, s);
-  k_imp_force<<<1, kFinalThreads, 0, s>>>(imp, p, nblocks, dxyz, mass, store_accel);
 }
 void launch_imp_record(ImpState* imp, double* ring, cudaStream_t s) {
   k_imp_record<<<1, 32, 0, s>>>(imp, ring);

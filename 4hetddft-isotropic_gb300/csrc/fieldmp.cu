@@ -16,6 +16,7 @@
 // Formulas and their reference lines are those of field.cu.
 #include "fpconv.cuh"
 #include "he4g_internal.cuh"
+#include "impurity.cuh"
 
 namespace he4g {
 
@@ -135,8 +136,10 @@ __global__ void __launch_bounds__(256) k_pc_predict_mp(Grid g, StencilF st, Func
                                                         const float* __restrict__ pot4,
                                                         const float* __restrict__ uimp,
                                                         const float* __restrict__ timec, float* den,
-                                                        double c4o3dt, double c112) {
+                                                        double c4o3dt, double c112, ImpState* imp) {
   const Pt t = point(g);
+  if (imp && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    imp_pc_predict_body(imp, c4o3dt, c112);
   if (!t.ok) return;
   const float2 lap = lap13f(psi32, t, g, st);
   const float2 ps = ld2f(psi32 + t.p);
@@ -166,7 +169,8 @@ __global__ void __launch_bounds__(256) k_pc_correct_mp(Grid g, StencilF st, Func
                                                         const float* __restrict__ uimp,
                                                         const float* __restrict__ timec, double2* psi_out,
                                                         float2* __restrict__ psi32_out, float* den,
-                                                        double* partials, float f38, double c9, int* health) {
+                                                        double* partials, float f38, double c9, int* health,
+                                                        PcFinish fin) {
   const Pt t = point(g);
   float v[1] = {0.f};
   if (t.ok) {
@@ -197,6 +201,11 @@ __global__ void __launch_bounds__(256) k_pc_correct_mp(Grid g, StencilF st, Func
     if (h) atomicOr(health, h);
   }
   block_sum_f<1>(v, partials);
+  if (threadIdx.y * blockDim.x + threadIdx.x >= 32) return;  // warp 0 finishes (when fin.cnt is set)
+  double tot[1];
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  if (fin.cnt && finish_sum<1>(partials, nb, fin.cnt, tot) && threadIdx.x == 0 && threadIdx.y == 0)
+    imp_pc_correct_body(fin.imp, tot[0], fin.dt, fin.c9, fin.nxyz);
 }
 
 // Runge–Kutta–Gill stage (steprk.f90:57-92) with FP64 psi and q
@@ -363,7 +372,7 @@ constexpr int kTileSlots = (kTW * kTH + kFX * kFY - 1) / (kFX * kFY);
 
 __global__ void __launch_bounds__(kFX * kFY) k_force_mp(Grid g, StencilF st, const float* __restrict__ den,
                                                          ImpTable tab, ImpState* imp, int center_sel,
-                                                         float* uimp_out, double* partials) {
+                                                         float* uimp_out, double* partials, ForceFinish fin) {
   __shared__ float cf[3];
   __shared__ __align__(16) float tile[kTH * kTW];
   load_center(imp, center_sel, cf);
@@ -445,6 +454,13 @@ __global__ void __launch_bounds__(kFX * kFY) k_force_mp(Grid g, StencilF st, con
   }
   float lo[3] = {-cc[0], -cc[1], -cc[2]};
   block_sum_dw<3>(s, lo, partials);
+  if (tid >= 32) return;  // warp 0 finishes (when fin.cnt is set)
+  double tot[3];
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  if (fin.cnt && finish_sum<3>(partials, nb, fin.cnt, tot) && tid == 0) {
+    imp_force_body(fin.imp, tot, fin.dxyz, fin.mass, fin.store_accel);
+    if (fin.ring) imp_record_body(fin.imp, fin.ring);
+  }
 }
 
 __global__ void __launch_bounds__(256) k_grad1_f(Grid g, StencilF st, int axis, const float* __restrict__ in,
@@ -532,11 +548,6 @@ __global__ void __launch_bounds__(256) k_energy_point_mp(Grid g, Functional fn, 
 
 }  // namespace
 
-int pc_blocks_mp(const Grid& g) {
-  const dim3 d = point_grid(g);
-  return (int)(d.x * d.y * d.z);
-}
-
 int force_blocks_mp(const Grid& g) {
   return ((g.nx + kFX - 1) / kFX) * ((g.ny + kFY - 1) / kFY) * ((g.nz + kZF - 1) / kZF);
 }
@@ -544,19 +555,23 @@ int force_blocks_mp(const Grid& g) {
 void launch_pc_predict_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
                           double2* p3, float2* psi32_out, const float2* h1, float2* h2, double2* pc,
                           const float* pot4, const float* uimp, const float* timec, float* den, double c4o3dt,
-                          double c112, cudaStream_t s) {
+                          double c112, ImpState* imp, cudaStream_t s) {
   k_pc_predict_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, fn, psi32, p3, psi32_out, h1, h2, pc, pot4, uimp,
-                                                           timec, den, c4o3dt, c112);
+                                                           timec, den, c4o3dt, c112, imp);
 }
-void launch_pc_correct_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psit32,
+int launch_pc_correct_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psit32,
                           const double2* p3, const double2* p2, const float2* h1, const float2* h2, double2* pc,
                           const float* pot4, const float* uimp, const float* timec, double2* psi_out,
                           float2* psi32_out, float* den, double* partials, double f3, double c9, int* health,
-                          cudaStream_t s) {
+                          const PcFinish& fin, cudaStream_t s) {
   const float f38 = (float)(0.125 * f3);
+  const int nb = (int)(point_grid(g).x * point_grid(g).y * point_grid(g).z);
+  PcFinish f = fin;
+  if (nb > kFinishInKernelMax) f.cnt = nullptr;
   k_pc_correct_mp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, fn, psit32, p3, p2, h1, h2, pc, pot4, uimp,
                                                            timec, psi_out, psi32_out, den, partials, f38, c9,
-                                                           health);
+                                                           health, f);
+  return 1 + (f.cnt ? 0 : launch_finish_pc(partials, nb, fin, s));
 }
 void launch_rk_stage_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
                         const double2* psi, double2* psi_out, float2* psi32_out, double2* q, float2* f_out,
@@ -573,10 +588,14 @@ void launch_potenimp_mp(const Grid& g, const ImpTable& tab, ImpState* imp, int c
   dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZF - 1) / kZF);
   k_potenimp_mp<<<grid, dim3(kBX, kBY), 0, s>>>(g, tab, imp, center_sel, uimp);
 }
-void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const ImpTable& tab, ImpState* imp,
-                     int center_sel, float* uimp_out, double* partials, cudaStream_t s) {
+int launch_force_mp(const Grid& g, const StencilF& st, const float* den, const ImpTable& tab, ImpState* imp,
+                     int center_sel, float* uimp_out, double* partials, const ForceFinish& fin, cudaStream_t s) {
   dim3 grid((g.nx + kFX - 1) / kFX, (g.ny + kFY - 1) / kFY, (g.nz + kZF - 1) / kZF);
-  k_force_mp<<<grid, dim3(kFX, kFY), 0, s>>>(g, st, den, tab, imp, center_sel, uimp_out, partials);
+  const int nb = (int)(grid.x * grid.y * grid.z);
+  ForceFinish f = fin;
+  if (nb > kFinishInKernelMax) f.cnt = nullptr;
+  k_force_mp<<<grid, dim3(kFX, kFY), 0, s>>>(g, st, den, tab, imp, center_sel, uimp_out, partials, f);
+  return 1 + (f.cnt ? 0 : launch_finish_force(partials, nb, fin, s));
 }
 void launch_grad1_f(const Grid& g, const StencilF& st, int axis, const float* in, float* out, cudaStream_t s) {
   k_grad1_f<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, axis, in, out);

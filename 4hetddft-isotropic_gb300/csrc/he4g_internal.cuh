@@ -82,6 +82,28 @@ struct ImpState {
 constexpr int kRingRows = 8192;
 constexpr int kRingCols = 10;
 
+// How a kernel's grid-wide sum continues into the impurity update in its last
+// block (impurity.cuh): cnt are the run's completion counters, ring (nullable)
+// receives a trajectory row after the force.
+struct ForceFinish {
+  ImpState* imp;
+  unsigned* cnt;
+  double* ring;
+  double dxyz, mass;
+  int store_accel;
+};
+struct PcFinish {
+  ImpState* imp;
+  unsigned* cnt;
+  double dt, c9, nxyz;
+};
+constexpr int kFinishCounters = 4097;  // 1 + groups of 256 blocks (grids up to 2^20 blocks)
+// The launchers of the corrector and force kernels return how many kernels
+// they launched: grids of more than kFinishInKernelMax (impurity.cuh) blocks
+// finish in separate kernels (field.cu), which these launch themselves.
+int launch_finish_pc(const double* partials, int nblocks, const PcFinish& fin, cudaStream_t s);
+int launch_finish_force(const double* partials, int nblocks, const ForceFinish& fin, cudaStream_t s);
+
 // Tile shapes of the line passes, chosen per run (he4g_autotune): lines per
 // block of the generic x passes, log2 of the kx columns per generic y/z
 // block, and which passes run on the register engine (ENGINE_* bits; only
@@ -145,15 +167,17 @@ void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv,
                     const void* den, const Functional& fn, void* pot4, cudaStream_t s);
 
 // ---------------------------------------- FP64 field kernels (field.cu)
+// the predictors also run the impurity predictor (steppc.f90:77-100) in one
+// thread when imp is not null
 void launch_pc_predict(const Grid& g, const Stencil& st, const Functional& fn, const double2* psi,
                        double2* p3_out, double2* h1, double2* h2_out, double2* pc, const double* pot4,
                        const double* uimp, const float* timec, double* den, double c4o3dt, double c112,
-                       cudaStream_t s);
-void launch_pc_correct(const Grid& g, const Stencil& st, const Functional& fn, const double2* psit,
+                       ImpState* imp, cudaStream_t s);
+int launch_pc_correct(const Grid& g, const Stencil& st, const Functional& fn, const double2* psit,
                        const double2* p3, const double2* p2, const double2* h1, const double2* h2,
                        double2* pc, const double* pot4, const double* uimp, const float* timec,
                        double2* psi_out, double* den, double* partials, double f3, double c9,
-                       int* health, cudaStream_t s);
+                       int* health, const PcFinish& fin, cudaStream_t s);
 void launch_rk_stage(const Grid& g, const Stencil& st, const Functional& fn, const double2* psi,
                      double2* psi_out, double2* q, double2* f_out, const double* pot4,
                      const double* uimp, const float* timec, double* den, double ar, double br,
@@ -162,8 +186,8 @@ void launch_potenimp(const Grid& g, const double* x, const double* y, const doub
                      const double* potion, int npot, double delinter, const ImpState* imp,
                      int center_sel, double* uimp, cudaStream_t s);
 int force_blocks(const Grid& g);
-void launch_force(const Grid& g, const Stencil& st, const double* den, const double* uimp,
-                  double* dx, double* dy, double* dz, double* partials, cudaStream_t s);
+int launch_force(const Grid& g, const Stencil& st, const double* den, const double* uimp,
+                  double* dx, double* dy, double* dz, double* partials, const ForceFinish& fin, cudaStream_t s);
 void launch_grad1(const Grid& g, const Stencil& st, int axis, const double* in, double* out,
                   cudaStream_t s);
 int energy_blocks(const Grid& g);
@@ -189,30 +213,23 @@ void launch_ualphas_a(const Grid& g, const double* falfs, const double* ix, cons
 void launch_ualphas_b(const Grid& g, double* u, const double* s4, const double* s5, const double* s6,
                       double h2o2m4, double alphas, double* pot4, cudaStream_t s);
 
-// impurity scalar kernels (field.cu). The partial arrays of
-// launch_imp_pc_correct / launch_imp_force need room for
-// ceil(nblocks/256)*nvals more values after their nblocks*nvals (first-level
-// sums); the run's partial buffer holds 12 values per point block.
+// impurity scalar kernels (field.cu); the predictor-corrector and force
+// kernels finish their own sums into the impurity update (impurity.cuh),
+// which needs ceil(nblocks/256)*nvals values after the nblocks*nvals partials
+// (the run's partial buffer holds 12 values per point block)
 void launch_imp_rk(ImpState* imp, int stage, double ar, double br, double cr, double dt, cudaStream_t s);
-void launch_imp_pc_predict(ImpState* imp, double c4o3dt, double c112, cudaStream_t s);
-void launch_imp_pc_correct(ImpState* imp, const double* err_partials, int nblocks, double dt,
-                           double c9, double nxyz, cudaStream_t s);
-void launch_imp_force(ImpState* imp, const double* partials, int nblocks, double dxyz, double mass,
-                      int store_accel, cudaStream_t s);
-// extra launches (first-level sums) the two calls above make for nblocks rows
-int fold_launches(int nblocks);
 void launch_imp_record(ImpState* imp, double* ring, cudaStream_t s);
 
 // ------------------------- mixed-precision field kernels (fieldmp.cu)
 void launch_pc_predict_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
                           double2* p3, float2* psi32_out, const float2* h1, float2* h2, double2* pc,
                           const float* pot4, const float* uimp, const float* timec, float* den, double c4o3dt,
-                          double c112, cudaStream_t s);
-void launch_pc_correct_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psit32,
+                          double c112, ImpState* imp, cudaStream_t s);
+int launch_pc_correct_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psit32,
                           const double2* p3, const double2* p2, const float2* h1, const float2* h2, double2* pc,
                           const float* pot4, const float* uimp, const float* timec, double2* psi_out,
                           float2* psi32_out, float* den, double* partials, double f3, double c9, int* health,
-                          cudaStream_t s);
+                          const PcFinish& fin, cudaStream_t s);
 void launch_rk_stage_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
                         const double2* psi, double2* psi_out, float2* psi32_out, double2* q, float2* f_out,
                         const float* pot4, const float* uimp, const float* timec, float* den, double ar, double br,
@@ -229,12 +246,10 @@ struct ImpTable {
 void launch_potenimp_mp(const Grid& g, const ImpTable& tab, ImpState* imp, int center_sel, float* uimp,
                         cudaStream_t s);
 int force_blocks_mp(const Grid& g);
-// partial-sum blocks of launch_pc_correct_mp
-int pc_blocks_mp(const Grid& g);
 // potenimp fused into the force sum: uimp is evaluated in place from the
 // centre (stored to uimp_out when not null)
-void launch_force_mp(const Grid& g, const StencilF& st, const float* den, const ImpTable& tab, ImpState* imp,
-                     int center_sel, float* uimp_out, double* partials, cudaStream_t s);
+int launch_force_mp(const Grid& g, const StencilF& st, const float* den, const ImpTable& tab, ImpState* imp,
+                     int center_sel, float* uimp_out, double* partials, const ForceFinish& fin, cudaStream_t s);
 void launch_grad1_f(const Grid& g, const StencilF& st, int axis, const float* in, float* out, cudaStream_t s);
 void launch_falfs_f(const Grid& g, const float* denalf, float den0s, float* falfs, cudaStream_t s);
 void launch_dot3_f(const Grid& g, const float* ax, const float* ay, const float* az, const float* bx,
