@@ -204,6 +204,29 @@ class Run:
         self._ck(self.lib.he4g_get_field(self.h, self.FIELDS[name], abi.dptr(out)))
         return out
 
+    def write_density(self, path, n4, time_ps=0.0, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463):
+        """The reference's restart/output file (printoutc.f90) of the current
+        state: energies, observables, rimp, vimp and psi; readenc mode 2
+        (and he4gpu.formats.read_density) read it back."""
+        from . import formats
+        e, o = self.energy(), self.observables(n4)
+        r, v, _ = self.impurity()
+        formats.write_density(path, self.psi, r, v, self.cfg.xmax, self.cfg.ymax, self.cfg.zmax,
+                              iteration=self.steps_taken, dtps=self.cfg.deltat * formats.PS_PER_KELVIN_UNIT,
+                              time=time_ps, selec=selec, r_cutoff=r_cutoff, umax=umax, cm=o["cm"],
+                              npart=o["npart"], energies=e, ang=o["ang"], r2=o["r2"])
+
+    def read_state(self, path, mode=2):
+        """set_state from a reference density / wave-function file (readenc
+        modes 0, 2, 3); mode 0 densities become psi = sqrt(den)."""
+        from . import formats
+        d = formats.read_density(path, mode)
+        if (d["nx"], d["ny"], d["nz"]) != (self.cfg.nx, self.cfg.ny, self.cfg.nz):
+            raise He4gError(-1, f"{path}: grid {d['nx']}x{d['ny']}x{d['nz']} does not match the run")
+        psi = d["psi"] if "psi" in d else np.sqrt(np.maximum(d["den"], 0.0)).astype(np.complex128)
+        self.set_state(psi, d["rimp"], d.get("vimp", np.zeros(3)))
+        return d
+
     def impurity(self):
         r, v, a = np.zeros(3), np.zeros(3), np.zeros(3)
         self._ck(self.lib.he4g_get_impurity(self.h, abi.dptr(r), abi.dptr(v), abi.dptr(a)))

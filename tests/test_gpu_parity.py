@@ -199,3 +199,18 @@ def test_config1_short_run():
     eg, eo = g.energy(), o.energy()
     for k in eo:
         assert abs(eg[k] - eo[k]) <= STEP_TOL * max(abs(eo[k]), 1e-3), k
+
+
+def test_restart_through_the_reference_file_format(tmp_path):
+    """A state written in printoutc's format and read back as readenc mode 2
+    reads it restores psi and the impurity's position and velocity bit for
+    bit."""
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    a = gpu_run(cfg, tk, psi, r, v)
+    a.step(4)
+    path = tmp_path / "den.out"
+    a.write_density(path, meta["n4"])
+    b = gpu_run(cfg, tk, psi, r, v)
+    b.read_state(path, mode=2)
+    assert np.array_equal(a.psi, b.psi)
+    assert all(np.array_equal(x, y) for x, y in zip(a.impurity()[:2], b.impurity()[:2]))
