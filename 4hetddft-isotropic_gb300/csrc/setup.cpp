@@ -100,10 +100,85 @@ double tang_toennies(double r, double AA, double BB, double C6, double C8, doubl
   return aux * hartree_to_k;
 }
 
+// He-He, HFD-B form of Aziz et al. (V_impur.f90:967-988): eps*[A exp(-alpha x
+// + beta x^2) - F(x)(C6/x^6 + C8/x^8 + C10/x^10)], x = r/rm, F = exp(-(D/x-1)^2)
+// for x <= D
+double aziz_he(double rr) {
+  const double eps = 10.948, A = 1.8443101e5, alpha = 10.43329537, beta = -2.27965105, D = 1.4826;
+  const double C6 = 1.36745214, C8 = 0.42123807, C10 = 0.17473318, rm = 2.963;
+  const double x = rr / rm;
+  if (x == 0.0) return A * eps;
+  const double f = x <= D ? std::exp(-(D / x - 1.0) * (D / x - 1.0)) : 1.0;
+  const double x2 = x * x, x6 = x2 * x2 * x2, x8 = x6 * x2, x10 = x8 * x2;
+  return (A * std::exp(-alpha * x + beta * x2) - f * (C6 / x6 + C8 / x8 + C10 / x10)) * eps;
+}
+
+// Lennard-Jones cored the Orsay-Trento way (V_impur.f90:1009-1034): a
+// constant inside rcutoff, sum_k pg_k x^-(k+5) outside (only k = 1 and 7
+// non-zero)
+double lj_ot(double x) {
+  const double rcutoff = 2.190323254008688, fcutoff = 1.574659520268255e2;
+  const double pg[7] = {-1.139924227407542e4, 0.0, 0.0, 0.0, 0.0, 0.0, 3.178638072971337e6};
+  if (x <= rcutoff) return fcutoff;
+  const double xq = 1.0 / x;
+  double sto = 0.0, xk = xq * xq * xq * xq * xq;  // xq^5
+  for (int k = 0; k < 7; ++k) {
+    xk *= xq;  // xq^(k+6)
+    sto += pg[k] * xk;
+  }
+  return sto;
+}
+
+// Alkali-He pseudopotentials of V_alka (V_impur.f90:1094-1189): the
+// electron-density overlap term and damped C6/C8 dispersion, in atomic units
+// converted to K. elem: 0 Li, 1 Na, 2 K, 3 Rb, 4 Cs.
+double alkali_he(double dist, int elem) {
+  const double evk = 11604.448, bohr = 0.529177249, hartree = 27.211608;
+  const double av[5] = {1.588, 1.627, 1.771, 1.805, 1.869};
+  const double c6v[5] = {22.5, 24.7, 38.9, 44.6, 51.2};
+  const double c8v[5] = {1.06e3, 1.29e3, 2.66e3, 3.18e3, 4.34e3};
+  const double agranv[5] = {0.0519, 0.0450, 0.0259, 0.0226, 0.0173};
+  const double b = 0.744, r2 = 2.37, r4 = 7.78, r6 = 50.5;
+  const double a = av[elem], c6 = c6v[elem], c8 = c8v[elem], agran = agranv[elem];
+  const double d = dist / bohr;
+  const double abar = (a + b) / 4.0, u = a - 1.0, v = -0.5 * a * a * u;
+  const double roa = agran * std::pow(d, 2.0 * u) * (1.0 + v / d) * (1.0 + v / d) * std::exp(-2.0 * d / a);
+  double f[2];
+  for (int l = 1; l <= 2; ++l) {
+    double s = 0.0, term = 1.0;  // (d/abar)^n / n!
+    for (int n = 0; n <= 2 * l + 7; ++n) {
+      if (n > 0) term *= (d / abar) / n;
+      s += term;
+    }
+    f[l - 1] = 1.0 - s * std::exp(-d / abar);
+  }
+  const double pi = 4.0 * std::atan(1.0);
+  const double d2 = d * d, d6 = d2 * d2 * d2, d8 = d6 * d2;
+  const double vimp = 4.0 * pi / 3.0 * roa * (r2 + 37.0 / 90.0 * r4 / (a * a) + 28.0 / 525.0 * r6 / (a * a * a * a)) -
+                      c6 * f[0] / d6 - c8 * f[1] / d8;
+  return vimp * evk * hartree;
+}
+
+// Select_pot (V_impur.f90): the radial potential named selec, umax inside
+// r_cutoff; -1 when the name is not implemented
+int pot_kind(const char* selec) {
+  static const char* names[] = {"Xe_He", "Ar_He", "Aziz_He", "LJ_OT", "LI", "NA", "K", "RB", "CS", "null"};
+  for (int k = 0; k < 10; ++k)
+    if (std::strcmp(selec, names[k]) == 0) return k;
+  return -1;
+}
+
 double v_pair(const char* selec, double r, double r_cutoff, double umax) {
+  const int kind = pot_kind(selec);
+  if (kind == 9) return 0.0;  // null: V_null everywhere
   if (r < r_cutoff) return umax;
-  if (std::strcmp(selec, "Ar_He") == 0) return tang_toennies(r, 75.8953, 2.0589, 9.7697, 152.8468, 3249.728);
-  return tang_toennies(r, 74.9002, 1.8175, 21.5674, 430.148, 10610.21);
+  switch (kind) {
+    case 1: return tang_toennies(r, 75.8953, 2.0589, 9.7697, 152.8468, 3249.728);
+    case 2: return aziz_he(r);
+    case 3: return lj_ot(r);
+    case 4: case 5: case 6: case 7: case 8: return alkali_he(r, kind - 4);
+    default: return tang_toennies(r, 74.9002, 1.8175, 21.5674, 430.148, 10610.21);
+  }
 }
 
 // pi/2 - Si(a x) (fforma.f90 sinint, a > 0)
@@ -197,7 +272,7 @@ extern "C" void he4g_default_config(he4g_config* c, int nx, int ny, int nz, doub
 extern "C" int he4g_build_tables(const he4g_config* c, const char* selec, double r_cutoff, double umax,
                                  double* fvlj4, double* wcgk, double* kalfs, double* potion) {
   if (!c || c->nx <= 0 || c->ny <= 0 || c->nz <= 0) return HE4G_EINVAL;
-  if (selec && std::strcmp(selec, "Xe_He") != 0 && std::strcmp(selec, "Ar_He") != 0) return HE4G_EINVAL;
+  if (selec && pot_kind(selec) < 0) return HE4G_EINVAL;
   const int nx = c->nx, ny = c->ny, nz = c->nz, nxh = nx / 2 + 1;
   const double hx = 2.0 * std::fabs(c->xmax) / nx, hy = 2.0 * std::fabs(c->ymax) / ny,
                hz = 2.0 * std::fabs(c->zmax) / nz;

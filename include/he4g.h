@@ -113,7 +113,9 @@ void he4g_default_config(he4g_config* cfg, int nx, int ny, int nz, double xmax, 
  * cored LJ potential, p = 0 from bforce :256-280), initcg.f90:32-49 (coarse
  * graining kernel), DFT4He3d.f90:592-596 (alpha_s Gaussian kalfs) and
  * potenimpini.f90:11-27 + V_impur.f90 Select_Pot (radial impurity table).
- * selec: "Xe_He" or "Ar_He". Output half-grid arrays hold (nx/2+1)*ny*nz
+ * selec (Select_pot names of V_impur.f90): "Xe_He", "Ar_He", "Aziz_He",
+ * "LJ_OT", "LI", "NA", "K", "RB", "CS" or "null"; others give HE4G_EINVAL.
+ * Output half-grid arrays hold (nx/2+1)*ny*nz
  * doubles; potion holds cfg->npot doubles; kalfs may be NULL. */
 int he4g_build_tables(const he4g_config* cfg, const char* selec, double r_cutoff, double umax,
                       double* fvlj4, double* wcgk, double* kalfs, double* potion);

@@ -331,10 +331,72 @@ static double sinx5(double a, double x) {
   return res1 + res2;
 }
 
-static double select_pot(const char* selec, double r, double r_cutoff, double umax) {
+/* He-He HFD-B (V_impur.f90:967-988) */
+double orc_v_aziz_he(double rr) {
+  const double eps = 10.948, A = 1.8443101e5, alpha = 10.43329537, beta = -2.27965105, D = 1.4826;
+  const double C6 = 1.36745214, C8 = 0.42123807, C10 = 0.17473318, rm = 2.963;
+  double x = rr / rm;
+  if (x == 0.0) return A * eps;
+  double f = x <= D ? exp(-(D / x - 1.0) * (D / x - 1.0)) : 1.0;
+  double x2 = x * x, x6 = x2 * x2 * x2, x8 = x6 * x2, x10 = x8 * x2;
+  return (A * exp(-alpha * x + beta * x2) - f * (C6 / x6 + C8 / x8 + C10 / x10)) * eps;
+}
+
+/* Orsay-Trento cored Lennard-Jones (V_impur.f90:1009-1034) */
+double orc_v_lj_ot(double x) {
+  const double rcutoff = 2.190323254008688, fcutoff = 1.574659520268255e2;
+  const double pg[7] = {-1.139924227407542e4, 0.0, 0.0, 0.0, 0.0, 0.0, 3.178638072971337e6};
+  if (x <= rcutoff) return fcutoff;
+  double xq = 1.0 / x, sto = 0.0, xk = xq * xq * xq * xq * xq;
+  for (int k = 0; k < 7; ++k) {
+    xk *= xq;
+    sto += pg[k] * xk;
+  }
+  return sto;
+}
+
+/* alkali-He (V_impur.f90:1094-1189); elem 0 Li, 1 Na, 2 K, 3 Rb, 4 Cs */
+double orc_v_alkali_he(double dist, int elem) {
+  const double evk = 11604.448, bohr = 0.529177249, hartree = 27.211608;
+  const double av[5] = {1.588, 1.627, 1.771, 1.805, 1.869};
+  const double c6v[5] = {22.5, 24.7, 38.9, 44.6, 51.2};
+  const double c8v[5] = {1.06e3, 1.29e3, 2.66e3, 3.18e3, 4.34e3};
+  const double agranv[5] = {0.0519, 0.0450, 0.0259, 0.0226, 0.0173};
+  const double b = 0.744, r2 = 2.37, r4 = 7.78, r6 = 50.5;
+  double a = av[elem], c6 = c6v[elem], c8 = c8v[elem], agran = agranv[elem];
+  double d = dist / bohr;
+  double abar = (a + b) / 4.0, u = a - 1.0, v = -0.5 * a * a * u;
+  double roa = agran * pow(d, 2.0 * u) * (1.0 + v / d) * (1.0 + v / d) * exp(-2.0 * d / a);
+  double f[2];
+  for (int l = 1; l <= 2; ++l) {
+    double sum = 0.0, term = 1.0;
+    for (int n = 0; n <= 2 * l + 7; ++n) {
+      if (n > 0) term *= (d / abar) / n;
+      sum += term;
+    }
+    f[l - 1] = 1.0 - sum * exp(-d / abar);
+  }
+  double pi = 4.0 * atan(1.0);
+  double d2 = d * d, d6 = d2 * d2 * d2, d8 = d6 * d2;
+  double vimp = 4.0 * pi / 3.0 * roa * (r2 + 37.0 / 90.0 * r4 / (a * a) + 28.0 / 525.0 * r6 / (a * a * a * a)) -
+                c6 * f[0] / d6 - c8 * f[1] / d8;
+  return vimp * evk * hartree;
+}
+
+/* Select_pot (V_impur.f90): umax inside r_cutoff; 'null' is zero everywhere */
+double orc_select_pot(const char* selec, double r, double r_cutoff, double umax) {
+  if (strcmp(selec, "null") == 0) return 0.0;
   if (r < r_cutoff) return umax;
   if (strcmp(selec, "Ar_He") == 0) return orc_v_ar_he(r);
+  if (strcmp(selec, "Aziz_He") == 0) return orc_v_aziz_he(r);
+  if (strcmp(selec, "LJ_OT") == 0) return orc_v_lj_ot(r);
+  static const char* alk[5] = {"LI", "NA", "K", "RB", "CS"};
+  for (int k = 0; k < 5; ++k)
+    if (strcmp(selec, alk[k]) == 0) return orc_v_alkali_he(r, k);
   return orc_v_xe_he(r);
+}
+static double select_pot(const char* selec, double r, double r_cutoff, double umax) {
+  return orc_select_pot(selec, r, r_cutoff, umax);
 }
 
 /* momentum grid modulus (DFT4He3d.f90:314-361) */

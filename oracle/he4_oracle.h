@@ -27,6 +27,10 @@ int orc_build_tables(const he4g_config* cfg, const char* selec, double r_cutoff,
 double orc_si(double x);
 double orc_v_xe_he(double r);
 double orc_v_ar_he(double r);
+double orc_v_aziz_he(double r);
+double orc_v_lj_ot(double r);
+double orc_v_alkali_he(double r, int elem);
+double orc_select_pot(const char* selec, double r, double r_cutoff, double umax);
 double orc_bforce(double eps, double sigma, double hc);
 
 orc_run* orc_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,

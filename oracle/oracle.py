@@ -43,6 +43,10 @@ def load():
         "orc_si": (C.c_double, [C.c_double]),
         "orc_v_xe_he": (C.c_double, [C.c_double]),
         "orc_v_ar_he": (C.c_double, [C.c_double]),
+        "orc_v_aziz_he": (C.c_double, [C.c_double]),
+        "orc_v_lj_ot": (C.c_double, [C.c_double]),
+        "orc_v_alkali_he": (C.c_double, [C.c_double, C.c_int]),
+        "orc_select_pot": (C.c_double, [C.c_char_p, C.c_double, C.c_double, C.c_double]),
         "orc_bforce": (C.c_double, [C.c_double, C.c_double, C.c_double]),
         "orc_create": (P, [P, _D, _D, _D, _D]),
         "orc_destroy": (None, [P]),
