@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -47,12 +48,15 @@ enum Fam {
   F_SCALAR,
   F_ALPHA_S,
   F_FFT_X_C2R_CORR,
+  F_FFT_XY_FWD,
+  F_FFT_XY_MID,
+  F_FFT_XY_INV_POT4,
   F_COUNT
 };
 const char* kFamName[F_COUNT] = {"pc_predict", "pc_correct", "rk_stage",        "potenimp",
                                  "fft_x_r2c",  "fft_y",      "fft_z_conv",      "fft_x_c2r",
                                  "fft_x_c2r_pot4", "force",  "impurity_scalar", "alpha_s_pointwise",
-                                 "fft_x_c2r_corr"};
+                                 "fft_x_c2r_corr", "fft_xy_fwd", "fft_xy_mid", "fft_xy_inv_pot4"};
 
 // history roles a captured step graph was recorded with
 struct GraphKey {
@@ -118,6 +122,8 @@ struct he4g_run {
 
   int iter = 0;
   bool have_state = false;
+  int device = 0;        // the device current at he4g_create
+  bool l2_window = false;  // a persisting L2 window is set on the stream
   bool delj4_valid = false;
   long long ring_read = 0;
 
@@ -421,15 +427,26 @@ void poten_dev(he4g_run* r) {
   const Grid& g = r->g;
   const bool otc = r->fn.otc;
   const int prec = r->prec;
+  // fused plane kernels (mixed form): the y passes run inside the x passes'
+  // kernels, one z plane per cluster
+  const bool xy = mixed(r) && (r->plan.tiles.engine & ENGINE_XY);
   r->delj4_valid = false;
-  {
-    Tick t(r, F_FFT_X_R2C);
-    fft_x_r2c(g, r->plan, prec, r->den, r->spec0, r->s);
+  bool fwd = false;
+  if (xy) {
+    Tick t(r, F_FFT_XY_FWD);
+    fwd = xy_fwd(g, r->plan, r->den, r->spec0, r->s);
+    if (!fwd) t.cancel();
   }
   void* sp0[1] = {r->spec0};
-  {
-    Tick t(r, F_FFT_Y);
-    fft_y(g, r->plan, prec, sp0, 1, -1, r->s);
+  if (!fwd) {
+    {
+      Tick t(r, F_FFT_X_R2C);
+      fft_x_r2c(g, r->plan, prec, r->den, r->spec0, r->s);
+    }
+    {
+      Tick t(r, F_FFT_Y);
+      fft_y(g, r->plan, prec, sp0, 1, -1, r->s);
+    }
   }
   {
     // rho-hat -> coarse-grained density (spec0), Lennard-Jones (spec1), alpha_s density (spec2)
@@ -438,34 +455,43 @@ void poten_dev(he4g_run* r) {
     const void* facs[3] = {r->wcgk, r->fvlj4, r->kalfs};
     fft_z_conv(g, r->plan, prec, r->spec0, outs, facs, otc ? 3 : 2, 0.5 * g.renor, nullptr, r->s);
   }
-  {
-    Tick t(r, F_FFT_Y);
-    void* sp[2] = {r->spec0, r->spec2};
-    fft_y(g, r->plan, prec, sp, otc ? 2 : 1, +1, r->s);
+  // inverse y, dencg and the correlation prologue, forward y: one fused
+  // plane kernel, else the y passes around one fused row pass on the
+  // register engine (OT core), else around c2r then r2c
+  bool mid = false;
+  if (xy && !otc) {
+    Tick t(r, F_FFT_XY_MID);
+    mid = xy_mid(g, r->plan, r->spec0, r->dencg, r->den, r->cfg.cp4, r->cfg.cpp4, r->s);
+    if (!mid) t.cancel();
   }
-  // dencg and the correlation prologue: one fused row pass on the register
-  // engine (OT core), else c2r then r2c
-  bool fused = false;
-  if (!otc) {
-    Tick t(r, F_FFT_X_C2R_CORR);
-    fused = fft_x_c2r_corr(g, r->plan, prec, r->spec0, r->dencg, r->den, r->cfg.cp4, r->cfg.cpp4, r->s);
-    if (!fused) t.cancel();
-  }
-  if (!fused) {
+  if (!mid) {
     {
-      Tick t(r, F_FFT_X_C2R);
-      const void* in[2] = {r->spec0, r->spec2};
-      void* o[2] = {r->dencg, r->denalf};
-      fft_x_c2r(g, r->plan, prec, in, o, otc ? 2 : 1, r->s);
+      Tick t(r, F_FFT_Y);
+      void* sp[2] = {r->spec0, r->spec2};
+      fft_y(g, r->plan, prec, sp, otc ? 2 : 1, +1, r->s);
+    }
+    bool fused = false;
+    if (!otc) {
+      Tick t(r, F_FFT_X_C2R_CORR);
+      fused = fft_x_c2r_corr(g, r->plan, prec, r->spec0, r->dencg, r->den, r->cfg.cp4, r->cfg.cpp4, r->s);
+      if (!fused) t.cancel();
+    }
+    if (!fused) {
+      {
+        Tick t(r, F_FFT_X_C2R);
+        const void* in[2] = {r->spec0, r->spec2};
+        void* o[2] = {r->dencg, r->denalf};
+        fft_x_c2r(g, r->plan, prec, in, o, otc ? 2 : 1, r->s);
+      }
+      {
+        Tick t(r, F_FFT_X_R2C);
+        fft_x_r2c_corr(g, r->plan, prec, r->den, r->dencg, r->cfg.cp4, r->cfg.cpp4, r->spec0, r->s);
+      }
     }
     {
-      Tick t(r, F_FFT_X_R2C);
-      fft_x_r2c_corr(g, r->plan, prec, r->den, r->dencg, r->cfg.cp4, r->cfg.cpp4, r->spec0, r->s);
+      Tick t(r, F_FFT_Y);
+      fft_y(g, r->plan, prec, sp0, 1, -1, r->s);
     }
-  }
-  {
-    Tick t(r, F_FFT_Y);
-    fft_y(g, r->plan, prec, sp0, 1, -1, r->s);
   }
   {
     // correlation convolution, plus the Lennard-Jones field already in spec1
@@ -473,13 +499,21 @@ void poten_dev(he4g_run* r) {
     const void* f1[1] = {r->wcgk};
     fft_z_conv(g, r->plan, prec, r->spec0, sp0, f1, 1, 0.5 * g.renor, r->spec1, r->s);
   }
-  {
-    Tick t(r, F_FFT_Y);
-    fft_y(g, r->plan, prec, sp0, 1, +1, r->s);
+  bool inv = false;
+  if (xy) {
+    Tick t(r, F_FFT_XY_INV_POT4);
+    inv = xy_inv_pot4(g, r->plan, r->spec0, r->dencg, r->den, r->fn, r->pot4, r->s);
+    if (!inv) t.cancel();
   }
-  {
-    Tick t(r, F_FFT_X_C2R_POT4);
-    fft_x_c2r_pot4(g, r->plan, prec, r->spec0, r->dencg, r->den, r->fn, r->pot4, r->s);
+  if (!inv) {
+    {
+      Tick t(r, F_FFT_Y);
+      fft_y(g, r->plan, prec, sp0, 1, +1, r->s);
+    }
+    {
+      Tick t(r, F_FFT_X_C2R_POT4);
+      fft_x_c2r_pot4(g, r->plan, prec, r->spec0, r->dencg, r->den, r->fn, r->pot4, r->s);
+    }
   }
   if (otc) {
     {
@@ -822,6 +856,7 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   if (c.precision != HE4G_PREC_FP64 && c.precision != HE4G_PREC_MIXED) return bad("unsupported precision");
   r->prec = c.precision;
   r->rs = mixed(r) ? 4 : 8;
+  cudaGetDevice(&r->device);
   if (cudaStreamCreateWithFlags(&r->s, cudaStreamNonBlocking) != cudaSuccess) return bad("no CUDA device");
 
   Grid& g = r->g;
@@ -988,9 +1023,59 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   return HE4G_OK;
 }
 
+extern "C++" {
+namespace {
+// Runs with an L2 window share their context's persisting L2 limit: the
+// first raises it (remembering the value it found), the last to drop its
+// window restores that value, so that runs without a window get the whole
+// L2 again. Per device; the calls come from the host thread(s) driving runs.
+struct L2Share {
+  int users = 0;
+  size_t orig = 0;
+};
+std::mutex g_l2_mu;
+L2Share g_l2[64];
+
+// L2 residency of the spectrum scratch spec0, which every line pass of an
+// evaluation reads or writes: a persisting access-policy window on the run's
+// stream over spec0 (its first l2_window_bytes() when larger), with the
+// context's persisting L2 limit raised to cover it; off: no window.
+void set_l2_window(he4g_run* r, bool on) {
+  cudaStreamAttrValue v{};
+  const size_t bytes = 2 * r->rs * (size_t)r->g.nh;
+  const size_t win = on ? std::min(bytes, l2_window_bytes()) : 0;
+  {
+    std::lock_guard<std::mutex> lock(g_l2_mu);
+    L2Share& sh = g_l2[r->device & 63];
+    if (win && !r->l2_window) {
+      if (sh.users++ == 0) cudaDeviceGetLimit(&sh.orig, cudaLimitPersistingL2CacheSize);
+      r->l2_window = true;
+    } else if (!win && r->l2_window) {
+      r->l2_window = false;
+      if (--sh.users == 0) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, sh.orig);
+    }
+    if (win) {
+      size_t cur = 0;
+      cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+      if (cur < win) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, win);
+    }
+  }
+  if (win) {
+    v.accessPolicyWindow.base_ptr = r->spec0;
+    v.accessPolicyWindow.num_bytes = win;
+    v.accessPolicyWindow.hitRatio = 1.f;
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+  }
+  if (r->s) cudaStreamSetAttribute(r->s, cudaStreamAttributeAccessPolicyWindow, &v);
+}
+}  // namespace
+}  // extern "C++"
+
 void he4g_destroy(he4g_run* r) {
   if (!r) return;
   if (r->s) cudaStreamSynchronize(r->s);
+  if (r->l2_window) set_l2_window(r, false);
   for (auto& p : r->pending) {
     cudaEventDestroy(p.second.first);
     cudaEventDestroy(p.second.second);
@@ -1130,17 +1215,19 @@ constexpr int kMaxLpb = 64;
 constexpr int kMaxLtx = 5;
 
 bool tiles_fit(const he4g_run* r, const FftTiles& t) {
-  if (t.engine & ~fft_reg_engines(r->plan)) return false;
+  if (t.engine & ~fft_reg_engines(r->prec, r->plan)) return false;
   if (t.lpb_r2c < 1 || t.lpb_r2c > kMaxLpb || t.lpb_c2r < 1 || t.lpb_c2r > kMaxLpb) return false;
   if (t.ltx_y < 0 || t.ltx_y > kMaxLtx || t.ltx_z < 0 || t.ltx_z > kMaxLtx) return false;
   return fft_smem_bytes(r->prec, PASS_R2C, r->plan, t.lpb_r2c) && fft_smem_bytes(r->prec, PASS_C2R, r->plan, t.lpb_c2r) &&
          fft_smem_bytes(r->prec, PASS_Y, r->plan, t.ltx_y) && fft_smem_bytes(r->prec, PASS_Z, r->plan, t.ltx_z);
 }
 
-// Captured graphs hold the launch shapes they were captured with.
+// Captured graphs hold the launch shapes (and the access policy) they were
+// captured with.
 void apply_tiles(he4g_run* r, const FftTiles& t) {
   r->plan.tiles = t;
   fft_prepare(r->prec, r->plan);
+  set_l2_window(r, (t.engine & ENGINE_L2RES) != 0);
   for (auto& e : r->graphs) cudaGraphExecDestroy(e.exec);
   r->graphs.clear();
 }
@@ -1191,7 +1278,7 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
   const void* zf[1] = {r->fvlj4};
   const void* ci[1] = {r->spec0};
   void* co[1] = {r->spec1};
-  const int engines = fft_reg_engines(r->plan);
+  const int engines = fft_reg_engines(prec, r->plan);
   auto sweep = [&](int pass, int lo, int hi, bool pow2, int FftTiles::*field, int bit) {
     float best_ms = 0.f;
     int best_tile = best.*field;
@@ -1235,6 +1322,56 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
   sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y, ENGINE_Y);
   sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z, ENGINE_Z);
   sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r, ENGINE_C2R);
+  // Execution options (fused plane kernels, L2 residency of the spectrum):
+  // every combination the device and plane allow, timed over an
+  // evaluation's line passes with the tiles chosen above. dencg and pot4 go
+  // to delj4, which is rebuilt on demand, so the run's fields stay as they are.
+  const int options = engines & (ENGINE_XY | ENGINE_L2RES);
+  if (options) {
+    const bool otc = r->fn.otc;
+    const double cp4 = r->cfg.cp4, cpp4 = r->cfg.cpp4;
+    void* out = r->delj4;
+    const void* cin[1] = {r->spec0};
+    void* cout[1] = {out};
+    void* zouts[2] = {r->spec0, r->spec1};
+    const void* zfacs[2] = {r->wcgk, r->fvlj4};
+    const void* zf1[1] = {r->wcgk};
+    float best_ms = 0.f;
+    int best_opt = 0;
+    for (int opt = 0; opt <= options; ++opt) {
+      if (opt & ~options) continue;
+      trial = best;
+      trial.engine = (trial.engine & ~(ENGINE_XY | ENGINE_L2RES)) | opt;
+      apply_tiles(r, trial);
+      const bool xy = (opt & ENGINE_XY) != 0;
+      const float ms = per_launch_ms(r, a, b, reps, [&] {
+        if (!(xy && xy_fwd(g, r->plan, r->den, r->spec0, r->s))) {
+          fft_x_r2c(g, r->plan, prec, r->den, r->spec0, r->s);
+          fft_y(g, r->plan, prec, sp, 1, -1, r->s);
+        }
+        fft_z_conv(g, r->plan, prec, r->spec0, zouts, zfacs, 2, 0.5 * g.renor, nullptr, r->s);
+        if (!(xy && !otc && xy_mid(g, r->plan, r->spec0, out, r->den, cp4, cpp4, r->s))) {
+          fft_y(g, r->plan, prec, sp, 1, +1, r->s);
+          if (!fft_x_c2r_corr(g, r->plan, prec, r->spec0, out, r->den, cp4, cpp4, r->s)) {
+            fft_x_c2r(g, r->plan, prec, cin, cout, 1, r->s);
+            fft_x_r2c_corr(g, r->plan, prec, r->den, out, cp4, cpp4, r->spec0, r->s);
+          }
+          fft_y(g, r->plan, prec, sp, 1, -1, r->s);
+        }
+        fft_z_conv(g, r->plan, prec, r->spec0, sp, zf1, 1, 0.5 * g.renor, r->spec1, r->s);
+        if (!(xy && xy_inv_pot4(g, r->plan, r->spec0, r->dencg, r->den, r->fn, out, r->s))) {
+          fft_y(g, r->plan, prec, sp, 1, +1, r->s);
+          fft_x_c2r_pot4(g, r->plan, prec, r->spec0, r->dencg, r->den, r->fn, out, r->s);
+        }
+      });
+      if (best_ms == 0.f || ms < best_ms) {
+        best_ms = ms;
+        best_opt = opt;
+      }
+    }
+    best.engine = (best.engine & ~(ENGINE_XY | ENGINE_L2RES)) | best_opt;
+    r->delj4_valid = false;
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   apply_tiles(r, best);

@@ -228,6 +228,14 @@ __device__ C2<R>* fft_smem(C2<R>* a, C2<R>* b, int nlines, int ld, const FftAxis
   return a;
 }
 
+// Starts moving `bytes` of global memory at p into L2 without waiting (a
+// bulk prefetch; p 16-byte aligned, bytes a multiple of 16). Kernels issue it
+// at their start for rows their epilogue reads after the transform work, so
+// that those loads hit L2.
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 template <typename R>
 __device__ __forceinline__ C2<R> ld_pair(const R* p) {
   return __ldg(reinterpret_cast<const C2<R>*>(p));

@@ -286,6 +286,11 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_reg(Grid g, FftAxis ax, c
   const long long row0 = (long long)blockIdx.x * L;
   const int nrows = (int)min((long long)L, nlines - row0);
   const int tid = threadIdx.x;
+  if (EPI == EPI_POT4 && tid == 0 && (g.nx * sizeof(R)) % 16 == 0) {
+    const unsigned bytes = (unsigned)(nrows * g.nx * sizeof(R));
+    prefetch_l2(pa.dencg + row0 * g.nx, bytes);
+    if (pa.fn.lsolid) prefetch_l2(pa.den + row0 * g.nx, bytes);
+  }
   const int ra = tid / Q, u = tid % Q;
   const bool actA = ra < nrows;
   C2<R> v[P];
@@ -368,6 +373,7 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_corr_reg(Grid g, FftAxis 
   const long long row0 = (long long)blockIdx.x * L;
   const int nrows = (int)min((long long)L, nlines - row0);
   const int tid = threadIdx.x;
+  if (tid == 0 && (g.nx * sizeof(R)) % 16 == 0) prefetch_l2(den + row0 * g.nx, (unsigned)(nrows * g.nx * sizeof(R)));
   // inverse pass, first half: thread (ra, u), u < Q, tangles X[k], X[M-k]
   const int ra = tid / Q, u = tid % Q;
   const bool actA = ra < nrows;

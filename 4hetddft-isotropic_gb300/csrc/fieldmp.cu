@@ -262,8 +262,7 @@ __global__ void k_split_mp(Grid g, const double2* __restrict__ psi, float2* psi3
 // The node index comes without a conversion instruction: for 0 <= qd < 2^23,
 // qd + 2^23 rounded toward zero is 2^23 + trunc(qd), whose low mantissa
 // bits are the index.
-__device__ __forceinline__ float uimp_at(const ImpTable& t, float dx, float dy, float dz, int* health) {
-  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+__device__ __forceinline__ float uimp_r2(const ImpTable& t, float r2, int* health) {
   const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
   const float qd = r * t.inv;
   if (qd < t.qmax) {  // trunc(qd) + 1 < npot; false for NaN
@@ -274,6 +273,9 @@ __device__ __forceinline__ float uimp_at(const ImpTable& t, float dx, float dy, 
   }
   atomicOr(health, 4);
   return 0.f;
+}
+__device__ __forceinline__ float uimp_at(const ImpTable& t, float dx, float dy, float dz, int* health) {
+  return uimp_r2(t, fmaf(dx, dx, fmaf(dy, dy, dz * dz)), health);
 }
 
 // The block's centre in FP32 (conversions from FP64 issue at the FP64 rate,
@@ -463,6 +465,174 @@ __global__ void __launch_bounds__(kFX * kFY) k_force_mp(Grid g, StencilF st, con
   }
 }
 
+// The same sum with two x-adjacent points per thread in packed FP32
+// arithmetic (FFMA2/FADD2/FMUL2: two lanes per instruction, each rounded as
+// the scalar operation), for grids with nx a multiple of 4. Per point the
+// operations and their order are those of k_force_mp; the x neighbours are
+// seven aligned 8-byte shared-memory reads, the y neighbours twelve, the z
+// neighbours a register window of float2. Blocks of 16 x 16 threads cover
+// 32 x 16 columns and march kP2Z planes; the plane tiles are double-buffered
+// (one barrier per plane), the next plane's loads issued before the current
+// plane's arithmetic.
+constexpr int kP2X = 16, kP2Y = 16, kP2Z = 8;
+constexpr int kP2CX = 2 * kP2X;                  // 32 columns
+constexpr int kP2TW = kP2CX + 2 * kTX0;          // 48
+constexpr int kP2TH = kP2Y + 2 * kStencilHalf;   // 28
+constexpr int kP2Vec = (kP2TW / 4) * kP2TH;      // 336 float4 per plane
+constexpr int kP2Slots = (kP2Vec + kP2X * kP2Y - 1) / (kP2X * kP2Y);
+
+// a - b in each lane as fma(b, -1, a): the product is exact, so the one
+// rounding is that of the subtraction
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+
+__device__ __forceinline__ void kahan_add2(float2& s, float2& c, float2 x) {
+  const float2 y = sub2(x, c);
+  const float2 t = __fadd2_rn(s, y);
+  c = sub2(sub2(t, s), y);
+  s = t;
+}
+
+// uimp_r2 of two points without a branch: a point beyond the table (or NaN)
+// gets 0 and sets `bad`; its table index is clamped to 0 so the loads stay
+// in bounds. In-table points take the operations of uimp_r2.
+__device__ __forceinline__ float2 uimp_r2_pair(const ImpTable& t, float2 r2, bool& bad) {
+  float qd[2], u[2];
+  const float rr[2] = {r2.x, r2.y};
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float r = rr[h] > 0.f ? rr[h] * rsqrtf(rr[h]) : 0.f;
+    qd[h] = r * t.inv;
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const bool in = qd[h] < t.qmax;  // false for NaN
+    bad |= !in;
+    const float q = in ? qd[h] : 0.f;
+    const float big = __fadd_rz(q, 8388608.f);
+    const int ir = __float_as_int(big) - __float_as_int(8388608.f);
+    const float w = q - (big - 8388608.f);
+    const float v = fmaf(__ldg(t.potion + ir), 1.f - w, __ldg(t.potion + ir + 1) * w);
+    u[h] = in ? v : 0.f;
+  }
+  return make_float2(u[0], u[1]);
+}
+
+// first-derivative coefficients as (c, c) pairs, the packed operand
+struct StencilP2 {
+  float2 c[3][kStencilHalf + 1];
+};
+
+__global__ void __launch_bounds__(kP2X * kP2Y, 3) k_force_mp2(Grid g, StencilP2 st, const float* __restrict__ den,
+                                                              ImpTable tab, ImpState* imp, int center_sel,
+                                                              float* uimp_out, double* partials, ForceFinish fin) {
+  __shared__ float cf[3];
+  __shared__ __align__(16) float tile[2][kP2TH * kP2TW];
+  load_center(imp, center_sel, cf);
+  const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * kP2X + lx;
+  const int x0 = blockIdx.x * kP2CX, y0 = blockIdx.y * kP2Y, k0 = blockIdx.z * kP2Z;
+  const int i = x0 + 2 * lx, j = y0 + ly;
+  const bool own = i < g.nx && j < g.ny;  // nx even: i + 1 < nx as well
+  const long long sz = (long long)g.nx * g.ny;
+  int voff[kP2Slots];
+  bool vok[kP2Slots];
+#pragma unroll
+  for (int q = 0; q < kP2Slots; ++q) {
+    const int idx = tid + q * kP2X * kP2Y;
+    const int ty = idx / (kP2TW / 4), c4 = idx - ty * (kP2TW / 4);
+    const int gx = x0 - kTX0 + 4 * c4, gy = y0 - kStencilHalf + ty;
+    vok[q] = idx < kP2Vec && gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
+    voff[q] = vok[q] ? gy * g.nx + gx : 0;
+  }
+  constexpr int W = kP2Z + 2 * kStencilHalf;
+  float2 wz[W];  // den at planes k0-6 .. k0+kP2Z+5 of this thread's two columns
+  const long long colo = (long long)j * g.nx + i;
+#pragma unroll
+  for (int m = 0; m < W; ++m) {
+    const int k = k0 - kStencilHalf + m;
+    wz[m] = (own && k >= 0 && k < g.nz) ? __ldg(reinterpret_cast<const float2*>(den + colo + k * sz))
+                                        : make_float2(0.f, 0.f);
+  }
+  float2 dx = make_float2(0.f, 0.f);
+  float dy = 0.f;
+  if (own) {
+    dx = make_float2(__ldg(tab.xs + i) - cf[0], __ldg(tab.xs + i + 1) - cf[0]);
+    dy = __ldg(tab.ys + j) - cf[1];
+  }
+  bool bad = false;
+  float2 s[3], cc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) s[a] = cc[a] = make_float2(0.f, 0.f);
+  float4 nv[kP2Slots];
+#pragma unroll
+  for (int q = 0; q < kP2Slots; ++q)
+    nv[q] = vok[q] ? __ldg(reinterpret_cast<const float4*>(den + k0 * sz + voff[q])) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int m = 0; m < kP2Z; ++m) {
+    const int k = k0 + m;
+    if (k >= g.nz) break;  // uniform over the block
+    float* tb = tile[m & 1];
+#pragma unroll
+    for (int q = 0; q < kP2Slots; ++q) {
+      const int idx = tid + q * kP2X * kP2Y;
+      if (idx < kP2Vec) reinterpret_cast<float4*>(tb)[idx] = nv[q];
+    }
+    __syncthreads();  // the tile of plane k is complete; the other buffer is free
+    if (m + 1 < kP2Z && k + 1 < g.nz) {
+#pragma unroll
+      for (int q = 0; q < kP2Slots; ++q)
+        nv[q] = vok[q] ? __ldg(reinterpret_cast<const float4*>(den + (k + 1) * sz + voff[q]))
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (own) {
+      const float* t0 = tb + (ly + kStencilHalf) * kP2TW + 2 * lx + kTX0;  // 8-byte aligned
+      float2 P[7];  // t0[-6 .. 7] as pairs
+#pragma unroll
+      for (int q = 0; q < 7; ++q) P[q] = *reinterpret_cast<const float2*>(t0 + 2 * (q - 3));
+      float2 gx = make_float2(0.f, 0.f), gy = gx, gz = gx;
+#pragma unroll
+      for (int o = 1; o <= kStencilHalf; ++o) {
+        if (o & 1) {
+          // (t0[o], t0[o+1]) - (t0[-o], t0[1-o]) straddle the pairs: lane by lane
+          const float c = st.c[0][o].x;
+          gx.x = fmaf(c, P[3 + (o - 1) / 2].y - P[3 - (o + 1) / 2].y, gx.x);
+          gx.y = fmaf(c, P[3 + (o + 1) / 2].x - P[3 - (o - 1) / 2].x, gx.y);
+        } else {
+          gx = __ffma2_rn(st.c[0][o], sub2(P[3 + o / 2], P[3 - o / 2]), gx);
+        }
+        const float2 ay = *reinterpret_cast<const float2*>(t0 + o * kP2TW);
+        const float2 by = *reinterpret_cast<const float2*>(t0 - o * kP2TW);
+        gy = __ffma2_rn(st.c[1][o], sub2(ay, by), gy);
+        gz = __ffma2_rn(st.c[2][o], sub2(wz[m + kStencilHalf + o], wz[m + kStencilHalf - o]), gz);
+      }
+      const float dz = __ldg(tab.zs + k) - cf[2];
+      const float yz = fmaf(dy, dy, dz * dz);
+      const float2 u = uimp_r2_pair(tab, __ffma2_rn(dx, dx, make_float2(yz, yz)), bad);
+      if (uimp_out) *reinterpret_cast<float2*>(uimp_out + colo + k * sz) = u;
+      kahan_add2(s[0], cc[0], __fmul2_rn(gx, u));
+      kahan_add2(s[1], cc[1], __fmul2_rn(gy, u));
+      kahan_add2(s[2], cc[2], __fmul2_rn(gz, u));
+    }
+  }
+  if (__syncthreads_or(bad) && tid == 0) atomicOr(&imp->health, 4);
+  float h[3], lo[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    h[a] = s[a].x;
+    lo[a] = -cc[a].x;
+    dw_add(h[a], lo[a], s[a].y, -cc[a].y);
+  }
+  block_sum_dw<3>(h, lo, partials);
+  if (tid >= 32) return;  // warp 0 finishes (when fin.cnt is set)
+  double tot[3];
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  if (fin.cnt && finish_sum<3>(partials, nb, fin.cnt, tot) && tid == 0) {
+    imp_force_body(fin.imp, tot, fin.dxyz, fin.mass, fin.store_accel);
+    if (fin.ring) imp_record_body(fin.imp, fin.ring);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_grad1_f(Grid g, StencilF st, int axis, const float* __restrict__ in,
                                                   float* out) {
   const Pt t = point(g);
@@ -549,7 +719,9 @@ __global__ void __launch_bounds__(256) k_energy_point_mp(Grid g, Functional fn, 
 }  // namespace
 
 int force_blocks_mp(const Grid& g) {
-  return ((g.nx + kFX - 1) / kFX) * ((g.ny + kFY - 1) / kFY) * ((g.nz + kZF - 1) / kZF);
+  const int a = ((g.nx + kFX - 1) / kFX) * ((g.ny + kFY - 1) / kFY) * ((g.nz + kZF - 1) / kZF);
+  const int b = ((g.nx + kP2CX - 1) / kP2CX) * ((g.ny + kP2Y - 1) / kP2Y) * ((g.nz + kP2Z - 1) / kP2Z);
+  return a > b ? a : b;
 }
 
 void launch_pc_predict_mp(const Grid& g, const StencilF& st, const Functional& fn, const float2* psi32,
@@ -590,11 +762,20 @@ void launch_potenimp_mp(const Grid& g, const ImpTable& tab, ImpState* imp, int c
 }
 int launch_force_mp(const Grid& g, const StencilF& st, const float* den, const ImpTable& tab, ImpState* imp,
                      int center_sel, float* uimp_out, double* partials, const ForceFinish& fin, cudaStream_t s) {
-  dim3 grid((g.nx + kFX - 1) / kFX, (g.ny + kFY - 1) / kFY, (g.nz + kZF - 1) / kZF);
+  const bool packed = (g.nx & 3) == 0;
+  const dim3 grid = packed ? dim3((g.nx + kP2CX - 1) / kP2CX, (g.ny + kP2Y - 1) / kP2Y, (g.nz + kP2Z - 1) / kP2Z)
+                           : dim3((g.nx + kFX - 1) / kFX, (g.ny + kFY - 1) / kFY, (g.nz + kZF - 1) / kZF);
   const int nb = (int)(grid.x * grid.y * grid.z);
   ForceFinish f = fin;
   if (nb > kFinishInKernelMax) f.cnt = nullptr;
-  k_force_mp<<<grid, dim3(kFX, kFY), 0, s>>>(g, st, den, tab, imp, center_sel, uimp_out, partials, f);
+  if (packed) {
+    StencilP2 sp;
+    for (int a = 0; a < 3; ++a)
+      for (int o = 0; o <= kStencilHalf; ++o) sp.c[a][o] = make_float2(st.d1[a][o], st.d1[a][o]);
+    k_force_mp2<<<grid, dim3(kP2X, kP2Y), 0, s>>>(g, sp, den, tab, imp, center_sel, uimp_out, partials, f);
+  }
+  else
+    k_force_mp<<<grid, dim3(kFX, kFY), 0, s>>>(g, st, den, tab, imp, center_sel, uimp_out, partials, f);
   return 1 + (f.cnt ? 0 : launch_finish_force(partials, nb, fin, s));
 }
 void launch_grad1_f(const Grid& g, const StencilF& st, int axis, const float* in, float* out, cudaStream_t s) {

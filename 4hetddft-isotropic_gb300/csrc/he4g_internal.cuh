@@ -107,8 +107,11 @@ int launch_finish_force(const double* partials, int nblocks, const ForceFinish& 
 // Tile shapes of the line passes, chosen per run (he4g_autotune): lines per
 // block of the generic x passes, log2 of the kx columns per generic y/z
 // block, and which passes run on the register engine (ENGINE_* bits; only
-// lengths with a specialisation, see fft_reg_supported).
-enum { ENGINE_R2C = 1, ENGINE_C2R = 2, ENGINE_Y = 4, ENGINE_Z = 8 };
+// lengths with a specialisation, see fft_reg_supported). ENGINE_XY fuses the
+// y pass with the neighbouring x passes per z plane (fft_xy.cu; mixed form,
+// planes with a specialisation, see fft_xy_supported). ENGINE_L2RES keeps
+// the spectrum scratch resident in L2 (l2_window_bytes).
+enum { ENGINE_R2C = 1, ENGINE_C2R = 2, ENGINE_Y = 4, ENGINE_Z = 8, ENGINE_XY = 16, ENGINE_L2RES = 32 };
 struct FftTiles {
   int lpb_r2c, lpb_c2r;
   int ltx_y, ltx_z;
@@ -136,7 +139,25 @@ void fft_prepare(int prec, const FftPlan& p);
 // true when the register engine has a specialisation for length n
 bool fft_reg_supported(int n);
 // ENGINE_* bits of the passes whose lengths the register engine supports
-int fft_reg_engines(const FftPlan& p);
+int fft_reg_engines(int prec, const FftPlan& p);
+// bytes of L2 the device lets a stream keep resident for an address window
+// (the smaller of its largest access-policy window and its persisting L2
+// capacity; 0 when it has none)
+size_t l2_window_bytes();
+// true when the fused plane kernels (fft_xy.cu) cover nx/2 = m, ny = n
+bool fft_xy_supported(int m, int n);
+// Fused plane kernels on FP32 fields; each returns false (and launches
+// nothing) when the plane has no fused kernel; launch=false only raises the
+// kernel's shared-memory limit.
+// x r2c of den + forward y pass into spec
+bool xy_fwd(const Grid& g, const FftPlan& p, const void* den, void* spec, cudaStream_t s, bool launch = true);
+// inverse y pass + x c2r into dencg + correlation prologue + x r2c + forward
+// y pass, spec in place
+bool xy_mid(const Grid& g, const FftPlan& p, void* spec, void* dencg, const void* den, double cp4, double cpp4,
+            cudaStream_t s, bool launch = true);
+// inverse y pass + inverse x pass with the pot4 epilogue
+bool xy_inv_pot4(const Grid& g, const FftPlan& p, const void* spec, const void* dencg, const void* den,
+                 const Functional& fn, void* pot4, cudaStream_t s, bool launch = true);
 
 // ------------------------------------------------- FFT passes (fft.cu)
 // prec: HE4G_PREC_FP64 (double fields, double2 spectra) or HE4G_PREC_MIXED

@@ -87,6 +87,41 @@ def test_register_engine_matches_generic(case, precision):
     assert np.max(np.abs(a.impurity()[0] - b.impurity()[0])) < 1e-9
 
 
+@pytest.mark.parametrize("case", ["he1000_xe_128", "he5000_xe_256"])
+def test_fused_plane_kernels_match_separate_passes(case):
+    """The cluster kernels that fuse the y pass with the x passes of each z
+    plane (mixed form) transform every line with the register engine's
+    arithmetic; they agree with the separate passes to FP32 rounding."""
+    cfg, tk, psi, r, v, meta = make_case(case, precision=1)
+    a = gpu_run(cfg, tk, psi, r, v)
+    b = gpu_run(cfg, tk, psi, r, v)
+    assert a.tiles[4] & 16 == 0  # not a default choice
+    b.tiles = a.tiles[:4] + (a.tiles[4] | 16,)
+    b.enable_timing(True)
+    a.step(4)
+    b.step(4)
+    fams = {k for k, (ms, n) in b.kernel_times().items() if n > 0}
+    assert {"fft_xy_fwd", "fft_xy_mid", "fft_xy_inv_pot4"} <= fams
+    assert not fams & {"fft_y", "fft_x_c2r_pot4", "fft_x_c2r_corr"}
+    assert rel_field(b.den, a.den) < 2e-5
+    assert rel_field(b.field("pot4"), a.field("pot4")) < 2e-5
+    assert rel_field(b.field("dencg"), a.field("dencg")) < 2e-5
+    assert np.max(np.abs(a.impurity()[0] - b.impurity()[0])) < 1e-9
+
+
+def test_fused_plane_kernels_replay_in_graphs():
+    cfg, tk, psi, r, v, meta = make_case("he1000_xe_128", precision=1)
+    runs = []
+    for graphs in (False, True):
+        x = gpu_run(cfg, tk, psi, r, v)
+        x.tiles = x.tiles[:4] + (x.tiles[4] | 16,)
+        x.enable_graphs(graphs)
+        x.step(7)
+        runs.append(x)
+    assert np.array_equal(runs[0].psi, runs[1].psi)
+    assert np.array_equal(runs[0].trajectory(), runs[1].trajectory())
+
+
 def test_autotune_keeps_a_valid_choice():
     cfg, tk, psi, r, v, meta = make_case("he200_xe_40x48x64", precision=1)
     b = gpu_run(cfg, tk, psi, r, v)
@@ -104,7 +139,8 @@ def test_set_tiles_rejects_out_of_range_shapes():
     cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
     a = gpu_run(cfg, tk, psi, r, v)
     before = a.tiles
-    for bad in [(0, 4, 3, 3, 0), (4, 4, -1, 3, 0), (4, 4, 3, 9, 0), (4, 100, 3, 3, 0), (4, 4, 3, 3, 16)]:
+    for bad in [(0, 4, 3, 3, 0), (4, 4, -1, 3, 0), (4, 4, 3, 9, 0), (4, 100, 3, 3, 0), (4, 4, 3, 3, 16),
+                (4, 4, 3, 3, 64)]:
         with pytest.raises(he4gpu.He4gError):
             a.tiles = bad
     assert a.tiles == before
