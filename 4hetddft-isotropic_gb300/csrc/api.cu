@@ -20,7 +20,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -122,8 +121,6 @@ struct he4g_run {
 
   int iter = 0;
   bool have_state = false;
-  int device = 0;        // the device current at he4g_create
-  bool l2_window = false;  // a persisting L2 window is set on the stream
   bool delj4_valid = false;
   long long ring_read = 0;
 
@@ -856,7 +853,6 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   if (c.precision != HE4G_PREC_FP64 && c.precision != HE4G_PREC_MIXED) return bad("unsupported precision");
   r->prec = c.precision;
   r->rs = mixed(r) ? 4 : 8;
-  cudaGetDevice(&r->device);
   if (cudaStreamCreateWithFlags(&r->s, cudaStreamNonBlocking) != cudaSuccess) return bad("no CUDA device");
 
   Grid& g = r->g;
@@ -1023,59 +1019,9 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   return HE4G_OK;
 }
 
-extern "C++" {
-namespace {
-// Runs with an L2 window share their context's persisting L2 limit: the
-// first raises it (remembering the value it found), the last to drop its
-// window restores that value, so that runs without a window get the whole
-// L2 again. Per device; the calls come from the host thread(s) driving runs.
-struct L2Share {
-  int users = 0;
-  size_t orig = 0;
-};
-std::mutex g_l2_mu;
-L2Share g_l2[64];
-
-// L2 residency of the spectrum scratch spec0, which every line pass of an
-// evaluation reads or writes: a persisting access-policy window on the run's
-// stream over spec0 (its first l2_window_bytes() when larger), with the
-// context's persisting L2 limit raised to cover it; off: no window.
-void set_l2_window(he4g_run* r, bool on) {
-  cudaStreamAttrValue v{};
-  const size_t bytes = 2 * r->rs * (size_t)r->g.nh;
-  const size_t win = on ? std::min(bytes, l2_window_bytes()) : 0;
-  {
-    std::lock_guard<std::mutex> lock(g_l2_mu);
-    L2Share& sh = g_l2[r->device & 63];
-    if (win && !r->l2_window) {
-      if (sh.users++ == 0) cudaDeviceGetLimit(&sh.orig, cudaLimitPersistingL2CacheSize);
-      r->l2_window = true;
-    } else if (!win && r->l2_window) {
-      r->l2_window = false;
-      if (--sh.users == 0) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, sh.orig);
-    }
-    if (win) {
-      size_t cur = 0;
-      cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
-      if (cur < win) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, win);
-    }
-  }
-  if (win) {
-    v.accessPolicyWindow.base_ptr = r->spec0;
-    v.accessPolicyWindow.num_bytes = win;
-    v.accessPolicyWindow.hitRatio = 1.f;
-    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-  }
-  if (r->s) cudaStreamSetAttribute(r->s, cudaStreamAttributeAccessPolicyWindow, &v);
-}
-}  // namespace
-}  // extern "C++"
-
 void he4g_destroy(he4g_run* r) {
   if (!r) return;
   if (r->s) cudaStreamSynchronize(r->s);
-  if (r->l2_window) set_l2_window(r, false);
   for (auto& p : r->pending) {
     cudaEventDestroy(p.second.first);
     cudaEventDestroy(p.second.second);
@@ -1222,12 +1168,10 @@ bool tiles_fit(const he4g_run* r, const FftTiles& t) {
          fft_smem_bytes(r->prec, PASS_Y, r->plan, t.ltx_y) && fft_smem_bytes(r->prec, PASS_Z, r->plan, t.ltx_z);
 }
 
-// Captured graphs hold the launch shapes (and the access policy) they were
-// captured with.
+// Captured graphs hold the launch shapes they were captured with.
 void apply_tiles(he4g_run* r, const FftTiles& t) {
   r->plan.tiles = t;
   fft_prepare(r->prec, r->plan);
-  set_l2_window(r, (t.engine & ENGINE_L2RES) != 0);
   for (auto& e : r->graphs) cudaGraphExecDestroy(e.exec);
   r->graphs.clear();
 }
@@ -1322,11 +1266,10 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
   sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y, ENGINE_Y);
   sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z, ENGINE_Z);
   sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r, ENGINE_C2R);
-  // Execution options (fused plane kernels, L2 residency of the spectrum):
-  // every combination the device and plane allow, timed over an
+  // The fused plane kernels against the passes they replace, timed over an
   // evaluation's line passes with the tiles chosen above. dencg and pot4 go
   // to delj4, which is rebuilt on demand, so the run's fields stay as they are.
-  const int options = engines & (ENGINE_XY | ENGINE_L2RES);
+  const int options = engines & ENGINE_XY;
   if (options) {
     const bool otc = r->fn.otc;
     const double cp4 = r->cfg.cp4, cpp4 = r->cfg.cpp4;
@@ -1341,7 +1284,7 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
     for (int opt = 0; opt <= options; ++opt) {
       if (opt & ~options) continue;
       trial = best;
-      trial.engine = (trial.engine & ~(ENGINE_XY | ENGINE_L2RES)) | opt;
+      trial.engine = (trial.engine & ~ENGINE_XY) | opt;
       apply_tiles(r, trial);
       const bool xy = (opt & ENGINE_XY) != 0;
       const float ms = per_launch_ms(r, a, b, reps, [&] {
@@ -1369,7 +1312,7 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
         best_opt = opt;
       }
     }
-    best.engine = (best.engine & ~(ENGINE_XY | ENGINE_L2RES)) | best_opt;
+    best.engine = (best.engine & ~ENGINE_XY) | best_opt;
     r->delj4_valid = false;
   }
   cudaEventDestroy(a);

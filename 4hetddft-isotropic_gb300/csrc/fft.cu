@@ -506,16 +506,8 @@ void fft_prepare(int prec, const FftPlan& p) {
   }
 }
 
-size_t l2_window_bytes() {
-  int dev = 0, win = 0, keep = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-  cudaDeviceGetAttribute(&win, cudaDevAttrMaxAccessPolicyWindowSize, dev);
-  cudaDeviceGetAttribute(&keep, cudaDevAttrMaxPersistingL2CacheSize, dev);
-  return (size_t)(win < keep ? win : keep);
-}
-
 int fft_reg_engines(int prec, const FftPlan& p) {
-  int e = l2_window_bytes() ? ENGINE_L2RES : 0;
+  int e = 0;
   if (fft_reg_supported(p.xh.n)) e |= ENGINE_R2C | ENGINE_C2R;
   if (fft_reg_supported(p.y.n)) e |= ENGINE_Y;
   if (fft_reg_supported(p.z.n)) e |= ENGINE_Z;
@@ -536,8 +528,8 @@ FftTiles fft_default_tiles(int prec, const FftPlan& p) {
   while (t.lpb_c2r > 1 && !fft_smem_bytes(prec, PASS_C2R, p, t.lpb_c2r)) t.lpb_c2r >>= 1;
   while (t.ltx_y > 0 && !fft_smem_bytes(prec, PASS_Y, p, t.ltx_y)) --t.ltx_y;
   while (t.ltx_z > 0 && !fft_smem_bytes(prec, PASS_Z, p, t.ltx_z)) --t.ltx_z;
-  // the execution options are the autotuner's choice, not a default
-  t.engine = fft_reg_engines(prec, p) & ~(ENGINE_XY | ENGINE_L2RES);
+  // the fused plane kernels are the autotuner's choice, not a default
+  t.engine = fft_reg_engines(prec, p) & ~ENGINE_XY;
   return t;
 }
 

@@ -109,9 +109,8 @@ int launch_finish_force(const double* partials, int nblocks, const ForceFinish& 
 // block, and which passes run on the register engine (ENGINE_* bits; only
 // lengths with a specialisation, see fft_reg_supported). ENGINE_XY fuses the
 // y pass with the neighbouring x passes per z plane (fft_xy.cu; mixed form,
-// planes with a specialisation, see fft_xy_supported). ENGINE_L2RES keeps
-// the spectrum scratch resident in L2 (l2_window_bytes).
-enum { ENGINE_R2C = 1, ENGINE_C2R = 2, ENGINE_Y = 4, ENGINE_Z = 8, ENGINE_XY = 16, ENGINE_L2RES = 32 };
+// planes with a specialisation, see fft_xy_supported).
+enum { ENGINE_R2C = 1, ENGINE_C2R = 2, ENGINE_Y = 4, ENGINE_Z = 8, ENGINE_XY = 16 };
 struct FftTiles {
   int lpb_r2c, lpb_c2r;
   int ltx_y, ltx_z;
@@ -140,10 +139,6 @@ void fft_prepare(int prec, const FftPlan& p);
 bool fft_reg_supported(int n);
 // ENGINE_* bits of the passes whose lengths the register engine supports
 int fft_reg_engines(int prec, const FftPlan& p);
-// bytes of L2 the device lets a stream keep resident for an address window
-// (the smaller of its largest access-policy window and its persisting L2
-// capacity; 0 when it has none)
-size_t l2_window_bytes();
 // true when the fused plane kernels (fft_xy.cu) cover nx/2 = m, ny = n
 bool fft_xy_supported(int m, int n);
 // Fused plane kernels on FP32 fields; each returns false (and launches

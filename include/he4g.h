@@ -226,17 +226,15 @@ int he4g_step_many(he4g_run** runs, int n, int nsteps);
  * tiles[3] of the generic fused z convolution, tiles[4] the passes that run
  * on the register engine instead (bits 1 forward x, 2 inverse x, 4 y, 8 z;
  * only for lengths it is specialised for: 16, 20, 24, 32, 40, 48, 64, 80, 96,
- * 128, 160, 192, 256) and two execution options: bit 16 fuses the y passes
- * with the x passes per z plane on thread-block clusters (mixed precision,
- * nx/2 x ny planes 128 x 256 and 64 x 128), bit 32 keeps the spectrum
- * scratch resident in L2 (a persisting access-policy window on the run's
- * stream; where the device supports one). No reference counterpart (FFTW
- * picks its own plans in fft.f90:5-153).
+ * 128, 160, 192, 256); bit 16 fuses the y passes with the x passes per z
+ * plane on thread-block clusters (mixed precision, nx/2 x ny planes
+ * 128 x 256 and 64 x 128). No reference counterpart (FFTW picks its own
+ * plans in fft.f90:5-153).
  *
  * he4g_autotune times, for each pass, every generic shape that fits in
- * shared memory and the register engine, then each execution option against
- * the passes it replaces, on this run's own buffers (reps timed launches
- * each, 0 = 5), and keeps the fastest; tiles (nullable)
+ * shared memory and the register engine, then the fused plane kernels
+ * against the passes they replace, on this run's own buffers (reps timed
+ * launches each, 0 = 5), and keeps the fastest; tiles (nullable)
  * receives the choice. Generic shapes change timing only (every line goes
  * through the same arithmetic); the two engines agree to rounding. It
  * overwrites the run's scratch spectra only, and drops captured step

@@ -140,7 +140,7 @@ def test_set_tiles_rejects_out_of_range_shapes():
     a = gpu_run(cfg, tk, psi, r, v)
     before = a.tiles
     for bad in [(0, 4, 3, 3, 0), (4, 4, -1, 3, 0), (4, 4, 3, 9, 0), (4, 100, 3, 3, 0), (4, 4, 3, 3, 16),
-                (4, 4, 3, 3, 64)]:
+                (4, 4, 3, 3, 32)]:
         with pytest.raises(he4gpu.He4gError):
             a.tiles = bad
     assert a.tiles == before
