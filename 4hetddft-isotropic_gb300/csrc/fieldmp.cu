@@ -471,10 +471,11 @@ __global__ void __launch_bounds__(kFX * kFY) k_force_mp(Grid g, StencilF st, con
 // operations and their order are those of k_force_mp; the x neighbours are
 // seven aligned 8-byte shared-memory reads, the y neighbours twelve, the z
 // neighbours a register window of float2. Blocks of 16 x 16 threads cover
-// 32 x 16 columns and march kP2Z planes; the plane tiles are double-buffered
+// 32 x 16 columns and march kP2Z planes (at 256^3 that is 2048 blocks, few
+// enough for the sum to finish in the kernel); the plane tiles are double-buffered
 // (one barrier per plane), the next plane's loads issued before the current
 // plane's arithmetic.
-constexpr int kP2X = 16, kP2Y = 16, kP2Z = 8;
+constexpr int kP2X = 16, kP2Y = 16, kP2Z = 16;
 constexpr int kP2CX = 2 * kP2X;                  // 32 columns
 constexpr int kP2TW = kP2CX + 2 * kTX0;          // 48
 constexpr int kP2TH = kP2Y + 2 * kStencilHalf;   // 28
@@ -524,7 +525,7 @@ struct StencilP2 {
   float2 c[3][kStencilHalf + 1];
 };
 
-__global__ void __launch_bounds__(kP2X * kP2Y, 3) k_force_mp2(Grid g, StencilP2 st, const float* __restrict__ den,
+__global__ void __launch_bounds__(kP2X * kP2Y, 2) k_force_mp2(Grid g, StencilP2 st, const float* __restrict__ den,
                                                               ImpTable tab, ImpState* imp, int center_sel,
                                                               float* uimp_out, double* partials, ForceFinish fin) {
   __shared__ float cf[3];

@@ -19,6 +19,7 @@ import time
 import numpy as np
 
 from . import batch_cases, state_for, step_many
+from . import serve as _serve
 from .serve import make_run
 
 MIXED = 1
@@ -75,7 +76,9 @@ def main(argv=None):
     ap.add_argument("--runs", type=int, default=32)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--fused-planes", action="store_true", help="keep the fused y/x plane kernels")
     args = ap.parse_args(argv)
+    _serve.KEEP_FUSED_PLANES = args.fused_planes
     cases = batch_cases(args.runs, seed=args.seed)
     b, res0 = batched(cases, args.steps)
     s = sequential_fp64(cases, args.steps)
@@ -86,7 +89,7 @@ def main(argv=None):
         grids[m["nx"]] = grids.get(m["nx"], 0) + 1
     out = {"batched_mixed": b, "sequential_fp64": s,
            "ratio": b["grid_point_updates_per_s"] / s["grid_point_updates_per_s"],
-           "alone_equals_batched": same, "grids": grids, "seed": args.seed}
+           "alone_equals_batched": same, "grids": grids, "seed": args.seed, "fused_planes": args.fused_planes}
     print(json.dumps(out), flush=True)
     return 0
 

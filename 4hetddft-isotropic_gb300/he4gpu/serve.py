@@ -29,21 +29,35 @@ MIXED = 1
 FP64 = 0
 
 
-# FFT tile shapes tuned once per (grid, precision) and shared by later runs
+# FFT tile shapes tuned once per (grid, precision, sharing) and reused by later runs
 _TILES = {}
 
+# tiles[4] bit of the fused y/x plane kernels (thread-block clusters)
+FUSED_PLANES = 16
+# whether runs that share the GPU keep them (--fused-planes)
+KEEP_FUSED_PLANES = False
 
-def make_run(meta, precision, graphs=True, tune=True):
+
+def make_run(meta, precision, graphs=True, tune=True, shared=True, fused_planes=None):
+    """A run for `meta`, with FFT tiles tuned once per grid. shared: the run
+    will advance together with others (batch, serving); the autotuner times
+    each pass alone, where the fused plane kernels can win, but with many
+    runs on the GPU their cluster-wide barriers and large blocks cost more
+    than the bytes they save, so shared runs leave them out unless
+    fused_planes (default: KEEP_FUSED_PLANES) is set."""
+    if fused_planes is None:
+        fused_planes = KEEP_FUSED_PLANES
     kw, tk = config_for_case(meta)
     cfg = default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], meta["ymax"], meta["zmax"],
                          precision=precision, **kw)
     run = Run(cfg, selec=tk["selec"], r_cutoff=tk["r_cutoff"], umax=tk["umax"])
     if tune:
-        key = (cfg.nx, cfg.ny, cfg.nz, precision)
-        if key in _TILES:
-            run.tiles = _TILES[key]
-        else:
-            _TILES[key] = run.autotune()
+        drop = shared and not fused_planes
+        key = (cfg.nx, cfg.ny, cfg.nz, precision, drop)
+        if key not in _TILES:
+            t = tuple(run.autotune())
+            _TILES[key] = t[:4] + (t[4] & ~FUSED_PLANES,) if drop else t
+        run.tiles = _TILES[key]
     if graphs:
         run.enable_graphs(True)
     return run, cfg
@@ -181,7 +195,10 @@ def main(argv=None):
     ap.add_argument("--max-active", type=int, default=64)
     ap.add_argument("--hbm-gb", type=float, default=0.0, help="budget; 0 = 90%% of the free memory")
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--fused-planes", action="store_true", help="keep the fused y/x plane kernels")
     args = ap.parse_args(argv)
+    global KEEP_FUSED_PLANES
+    KEEP_FUSED_PLANES = args.fused_planes
     stream = serve_stream(args.jobs, seed=args.seed, rate_per_s=args.rate, step_scale=args.step_scale)
     if args.hbm_gb > 0:
         budget = int(args.hbm_gb * 1e9)
@@ -194,7 +211,8 @@ def main(argv=None):
     check = alone_vs_mix(stream, kept)
     out = {"serve_mixed": rep, "one_at_a_time_fp64": base, "speedup_jobs_per_h": rep["jobs_per_h"] / base["jobs_per_h"],
            "alone_vs_mix": check, "stream": {"jobs": args.jobs, "rate_per_s": args.rate, "step_scale": args.step_scale,
-                                             "seed": args.seed, "hbm_budget_gb": budget / 1e9}}
+                                             "seed": args.seed, "hbm_budget_gb": budget / 1e9,
+                                             "fused_planes": args.fused_planes}}
     print(json.dumps(out), flush=True)
     return 0
 
