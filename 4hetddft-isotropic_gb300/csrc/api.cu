@@ -11,7 +11,9 @@
 // Precision: HE4G_PREC_FP64 keeps every array in FP64. HE4G_PREC_MIXED keeps
 // psi, its history, pc and q in FP64 and everything else (fields, spectra,
 // tables, hpsiold) in FP32, plus an FP32 copy of psi for the stencils
-// (psi32[cur32], ping-ponged with psi32[1 - cur32]).
+// (psi32[cur32], ping-ponged with psi32[1 - cur32]). HE4G_PREC_DF64 keeps
+// the arrays of the FP64 form and runs its 3D FFT convolutions in paired-FP32
+// (df64) arithmetic on df64 spectra.
 //
 // The mean field sums the Lennard-Jones convolution and the correlation
 // convolution in k-space before one shared inverse transform, so delj4 is
@@ -26,6 +28,7 @@
 #include <string>
 #include <vector>
 
+#include "df64.cuh"
 #include "he4g_internal.cuh"
 
 using namespace he4g;
@@ -249,6 +252,12 @@ int download_field(he4g_run* r, const void* src, double* dst, size_t n, const ch
   return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, where);
 }
 
+// df64 split of a long double: hi = RN(v), lo = RN(v - hi)
+df64 df_of(long double v) {
+  const float hi = static_cast<float>(v);
+  return df64(hi, static_cast<float>(v - static_cast<long double>(hi)));
+}
+
 void make_axis(he4g_run* r, FftAxis& ax, int n) {
   ax.n = n;
   ax.nf = 0;
@@ -285,18 +294,23 @@ void make_axis(he4g_run* r, FftAxis& ax, int n) {
   }
   std::vector<double2> tw(n);
   std::vector<float2> twf(n);
+  std::vector<df2> twd(n);
   for (int t = 0; t < n; ++t) {
     const long double a = 2.0L * 3.141592653589793238462643383279502884L * t / n;
     tw[t] = make_double2(static_cast<double>(cosl(a)), static_cast<double>(-sinl(a)));
     twf[t] = make_float2(static_cast<float>(cosl(a)), static_cast<float>(-sinl(a)));
+    twd[t] = df2{df_of(cosl(a)), df_of(-sinl(a))};
   }
   double2* d = dalloc<double2>(r, n, false);
   float2* df = dalloc<float2>(r, n, false);
+  df2* dd = dalloc<df2>(r, n, false);
   cudaMemcpyAsync(d, tw.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, r->s);
   cudaMemcpyAsync(df, twf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice, r->s);
+  cudaMemcpyAsync(dd, twd.data(), sizeof(df2) * n, cudaMemcpyHostToDevice, r->s);
   cudaStreamSynchronize(r->s);  // the host vectors go out of scope
   ax.tw = d;
   ax.twf = df;
+  ax.twd = dd;
 }
 
 bool radix_ok(int n) {
@@ -850,7 +864,11 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   if (!radix_ok(c.nx) || !radix_ok(c.ny) || !radix_ok(c.nz)) return bad("grid sizes must be 2^a 3^b 5^c");
   if (c.core == HE4G_CORE_OTC && !kalfs) return bad("core OTC needs the kalfs table");
   if (c.npot < 2 || !(c.delinter > 0)) return bad("bad potential table");
-  if (c.precision != HE4G_PREC_FP64 && c.precision != HE4G_PREC_MIXED) return bad("unsupported precision");
+  if (c.precision != HE4G_PREC_FP64 && c.precision != HE4G_PREC_MIXED && c.precision != HE4G_PREC_DF64)
+    return bad("unsupported precision");
+  if (c.precision == HE4G_PREC_DF64 &&
+      !(fft_reg_supported(c.nx / 2) && fft_reg_supported(c.ny) && fft_reg_supported(c.nz)))
+    return bad("HE4G_PREC_DF64 needs nx/2, ny and nz in {16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 256}");
   r->prec = c.precision;
   r->rs = mixed(r) ? 4 : 8;
   if (cudaStreamCreateWithFlags(&r->s, cudaStreamNonBlocking) != cudaSuccess) return bad("no CUDA device");
@@ -989,22 +1007,27 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   {
     std::vector<double2> twx(c.nx / 2);
     std::vector<float2> twxf(c.nx / 2);
+    std::vector<df2> twxd(c.nx / 2);
     for (int k = 0; k < c.nx / 2; ++k) {
       const long double a = 2.0L * 3.141592653589793238462643383279502884L * k / c.nx;
       twx[k] = make_double2(static_cast<double>(cosl(a)), static_cast<double>(-sinl(a)));
       twxf[k] = make_float2(static_cast<float>(cosl(a)), static_cast<float>(-sinl(a)));
+      twxd[k] = df2{df_of(cosl(a)), df_of(-sinl(a))};
     }
     double2* d = dalloc<double2>(r, c.nx / 2, false);
     float2* df = dalloc<float2>(r, c.nx / 2, false);
-    if (!d || !df) {
+    df2* dd = dalloc<df2>(r, c.nx / 2, false);
+    if (!d || !df || !dd) {
       he4g_destroy(r);
       return HE4G_ENOMEM;
     }
     cudaMemcpyAsync(d, twx.data(), sizeof(double2) * (c.nx / 2), cudaMemcpyHostToDevice, r->s);
     cudaMemcpyAsync(df, twxf.data(), sizeof(float2) * (c.nx / 2), cudaMemcpyHostToDevice, r->s);
+    cudaMemcpyAsync(dd, twxd.data(), sizeof(df2) * (c.nx / 2), cudaMemcpyHostToDevice, r->s);
     cudaStreamSynchronize(r->s);
     r->plan.twx = d;
     r->plan.twxf = df;
+    r->plan.twxd = dd;
   }
   r->plan.tiles = fft_default_tiles(r->prec, r->plan);
   fft_prepare(r->prec, r->plan);
@@ -1162,6 +1185,8 @@ constexpr int kMaxLtx = 5;
 
 bool tiles_fit(const he4g_run* r, const FftTiles& t) {
   if (t.engine & ~fft_reg_engines(r->prec, r->plan)) return false;
+  const int all = ENGINE_R2C | ENGINE_C2R | ENGINE_Y | ENGINE_Z;
+  if (r->prec == HE4G_PREC_DF64 && (t.engine & all) != all) return false;  // register engine only
   if (t.lpb_r2c < 1 || t.lpb_r2c > kMaxLpb || t.lpb_c2r < 1 || t.lpb_c2r > kMaxLpb) return false;
   if (t.ltx_y < 0 || t.ltx_y > kMaxLtx || t.ltx_z < 0 || t.ltx_z > kMaxLtx) return false;
   return fft_smem_bytes(r->prec, PASS_R2C, r->plan, t.lpb_r2c) && fft_smem_bytes(r->prec, PASS_C2R, r->plan, t.lpb_c2r) &&
@@ -1262,10 +1287,12 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
     best.*field = best_tile;
     best.engine = best_reg ? (best.engine | bit) : (best.engine & ~bit);
   };
-  sweep(PASS_R2C, 1, kMaxLpb, true, &FftTiles::lpb_r2c, ENGINE_R2C);
-  sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y, ENGINE_Y);
-  sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z, ENGINE_Z);
-  sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r, ENGINE_C2R);
+  if (prec != HE4G_PREC_DF64) {  // df64 has the register engine only
+    sweep(PASS_R2C, 1, kMaxLpb, true, &FftTiles::lpb_r2c, ENGINE_R2C);
+    sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y, ENGINE_Y);
+    sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z, ENGINE_Z);
+    sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r, ENGINE_C2R);
+  }
   // The fused plane kernels against the passes they replace, timed over an
   // evaluation's line passes with the tiles chosen above. dencg and pot4 go
   // to delj4, which is rebuilt on demand, so the run's fields stay as they are.

@@ -394,10 +394,19 @@ void pot4_impl(const Grid& g, const FftPlan& p, const void* conv, const void* de
 }  // namespace
 
 // -------------------------------------------------------------- launchers
+// HE4G_PREC_DF64 runs the register engine only (its lengths are checked when
+// the run is created); its spectra are complex df64 and its real fields FP64.
+namespace {
+const df2* twxd(const FftPlan& p) { return p.twxd; }
+}  // namespace
+
 void fft_x_r2c(const Grid& g, const FftPlan& p, int prec, const void* in, void* out, cudaStream_t s) {
   if (prec == HE4G_PREC_FP64)
     launch_r2c<double, PRO_PLAIN>(g, p, static_cast<const double*>(in), nullptr, 0.0, 0.0,
                                   static_cast<double2*>(out), s);
+  else if (prec == HE4G_PREC_DF64)
+    reg_r2c<df64>(g, p, twxd(p), PRO_PLAIN, static_cast<const double*>(in), nullptr, df64(0), df64(0),
+                  static_cast<df2*>(out), s);
   else
     launch_r2c<float, PRO_PLAIN>(g, p, static_cast<const float*>(in), nullptr, 0.f, 0.f,
                                  static_cast<float2*>(out), s);
@@ -407,6 +416,9 @@ void fft_x_r2c_corr(const Grid& g, const FftPlan& p, int prec, const void* den, 
   if (prec == HE4G_PREC_FP64)
     launch_r2c<double, PRO_CORR>(g, p, static_cast<const double*>(den), static_cast<const double*>(dencg), cp4,
                                  cpp4, static_cast<double2*>(out), s);
+  else if (prec == HE4G_PREC_DF64)
+    reg_r2c<df64>(g, p, twxd(p), PRO_CORR, static_cast<const double*>(den), static_cast<const double*>(dencg),
+                  df64(cp4), df64(cpp4), static_cast<df2*>(out), s);
   else
     launch_r2c<float, PRO_CORR>(g, p, static_cast<const float*>(den), static_cast<const float*>(dencg),
                                 (float)cp4, (float)cpp4, static_cast<float2*>(out), s);
@@ -416,6 +428,9 @@ void fft_x_r2c_prod(const Grid& g, const FftPlan& p, int prec, const void* a, co
   if (prec == HE4G_PREC_FP64)
     launch_r2c<double, PRO_PROD>(g, p, static_cast<const double*>(a), static_cast<const double*>(b), 0.0, 0.0,
                                  static_cast<double2*>(out), s);
+  else if (prec == HE4G_PREC_DF64)
+    reg_r2c<df64>(g, p, twxd(p), PRO_PROD, static_cast<const double*>(a), static_cast<const double*>(b), df64(0),
+                  df64(0), static_cast<df2*>(out), s);
   else
     launch_r2c<float, PRO_PROD>(g, p, static_cast<const float*>(a), static_cast<const float*>(b), 0.f, 0.f,
                                 static_cast<float2*>(out), s);
@@ -423,6 +438,8 @@ void fft_x_r2c_prod(const Grid& g, const FftPlan& p, int prec, const void* a, co
 void fft_y(const Grid& g, const FftPlan& p, int prec, void* const* specs, int nspec, int sign, cudaStream_t s) {
   if (prec == HE4G_PREC_FP64)
     y_impl<double>(g, p, specs, nspec, sign, s);
+  else if (prec == HE4G_PREC_DF64)
+    reg_y<df64>(g, p, specs, nspec, sign, s);
   else
     y_impl<float>(g, p, specs, nspec, sign, s);
 }
@@ -430,22 +447,36 @@ void fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void*
                 const void* const* factors, int nout, double scale, const void* add, cudaStream_t s) {
   if (prec == HE4G_PREC_FP64)
     zconv_impl<double>(g, p, in, outs, factors, nout, scale, add, s);
+  else if (prec == HE4G_PREC_DF64)
+    reg_z<df64>(g, p, in, outs, factors, nout, scale, add, s);
   else
     zconv_impl<float>(g, p, in, outs, factors, nout, scale, add, s);
 }
 void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins, void* const* outs, int nspec,
                cudaStream_t s) {
-  if (prec == HE4G_PREC_FP64)
+  if (prec == HE4G_PREC_FP64) {
     c2r_impl<double>(g, p, ins, outs, nspec, s);
-  else
+  } else if (prec == HE4G_PREC_DF64) {
+    const df2* i0 = static_cast<const df2*>(ins[0]);
+    double* o0 = static_cast<double*>(outs[0]);
+    reg_c2r<df64>(g, p, twxd(p), EPI_STORE, i0, nspec > 1 ? static_cast<const df2*>(ins[1]) : i0, o0,
+                  nspec > 1 ? static_cast<double*>(outs[1]) : o0, nspec, Pot4Args<df64>{}, s);
+  } else {
     c2r_impl<float>(g, p, ins, outs, nspec, s);
+  }
 }
 void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv, const void* dencg,
                     const void* den, const Functional& fn, void* pot4, cudaStream_t s) {
-  if (prec == HE4G_PREC_FP64)
+  if (prec == HE4G_PREC_FP64) {
     pot4_impl<double>(g, p, conv, dencg, den, fn, pot4, s);
-  else
+  } else if (prec == HE4G_PREC_DF64) {
+    const Pot4Args<df64> pa{static_cast<const double*>(dencg), static_cast<const double*>(den), fn};
+    const df2* c = static_cast<const df2*>(conv);
+    double* o = static_cast<double*>(pot4);
+    reg_c2r<df64>(g, p, twxd(p), EPI_POT4, c, c, o, o, 1, pa, s);
+  } else {
     pot4_impl<float>(g, p, conv, dencg, den, fn, pot4, s);
+  }
 }
 
 bool fft_x_c2r_corr(const Grid& g, const FftPlan& p, int prec, void* spec, void* dencg, const void* den, double cp4,
@@ -454,16 +485,36 @@ bool fft_x_c2r_corr(const Grid& g, const FftPlan& p, int prec, void* spec, void*
   if (prec == HE4G_PREC_FP64)
     return reg_c2r_corr<double>(g, p, twx_of<double>(p), static_cast<double2*>(spec), static_cast<double*>(dencg),
                                 static_cast<const double*>(den), cp4, cpp4, s);
+  if (prec == HE4G_PREC_DF64)
+    return reg_c2r_corr<df64>(g, p, twxd(p), static_cast<df2*>(spec), static_cast<double*>(dencg),
+                              static_cast<const double*>(den), df64(cp4), df64(cpp4), s);
   return reg_c2r_corr<float>(g, p, twx_of<float>(p), static_cast<float2*>(spec), static_cast<float*>(dencg),
                              static_cast<const float*>(den), (float)cp4, (float)cpp4, s);
 }
 
 size_t fft_smem_bytes(int prec, int pass, const FftPlan& p, int tile) {
-  const size_t b = prec == HE4G_PREC_FP64 ? smem_of<double>(pass, p, tile) : smem_of<float>(pass, p, tile);
+  // df64 elements have the byte size of FP64 ones
+  const size_t b = prec != HE4G_PREC_MIXED ? smem_of<double>(pass, p, tile) : smem_of<float>(pass, p, tile);
   return b <= kMaxSmemPerBlock ? b : 0;
 }
 
 namespace {
+// raises the register engine's shared-memory limits (no launch)
+template <typename R>
+void prepare_reg(const FftPlan& p) {
+  Grid g{};
+  void* sp[1] = {nullptr};
+  const void* f[1] = {nullptr};
+  Pot4Args<R> pa{};
+  for (int pro : {PRO_PLAIN, PRO_CORR, PRO_PROD})
+    reg_r2c<R>(g, p, nullptr, pro, nullptr, nullptr, (R)0, (R)0, nullptr, nullptr, false);
+  for (int sign : {-1, 1}) reg_y<R>(g, p, sp, 1, sign, nullptr, false);
+  reg_z<R>(g, p, nullptr, sp, f, 1, 1.0, nullptr, nullptr, false);
+  for (int epi : {EPI_STORE, EPI_POT4})
+    reg_c2r<R>(g, p, nullptr, epi, nullptr, nullptr, nullptr, nullptr, 1, pa, nullptr, false);
+  reg_c2r_corr<R>(g, p, nullptr, nullptr, nullptr, nullptr, (R)0, (R)0, nullptr, false);
+}
+
 template <typename R>
 void prepare_impl(const FftPlan& p) {
   const size_t r2c = smem_of<R>(PASS_R2C, p, p.tiles.lpb_r2c);
@@ -477,23 +528,15 @@ void prepare_impl(const FftPlan& p) {
   set_smem(k_z_conv<R>, smem_of<R>(PASS_Z, p, p.tiles.ltx_z));
   set_smem(k_x_c2r<R, EPI_STORE>, c2r);
   set_smem(k_x_c2r<R, EPI_POT4>, c2r);
-  // the register engine's kernels (no launch)
-  Grid g{};
-  void* sp[1] = {nullptr};
-  const void* f[1] = {nullptr};
-  Pot4Args<R> pa{};
-  for (int pro : {PRO_PLAIN, PRO_CORR, PRO_PROD})
-    reg_r2c<R>(g, p, nullptr, pro, nullptr, nullptr, (R)0, (R)0, nullptr, nullptr, false);
-  for (int sign : {-1, 1}) reg_y<R>(g, p, sp, 1, sign, nullptr, false);
-  reg_z<R>(g, p, nullptr, sp, f, 1, 1.0, nullptr, nullptr, false);
-  for (int epi : {EPI_STORE, EPI_POT4}) reg_c2r<R>(g, p, nullptr, epi, nullptr, nullptr, nullptr, nullptr, 1, pa, nullptr, false);
-  reg_c2r_corr<R>(g, p, nullptr, nullptr, nullptr, nullptr, (R)0, (R)0, nullptr, false);
+  prepare_reg<R>(p);
 }
 }  // namespace
 
 void fft_prepare(int prec, const FftPlan& p) {
   if (prec == HE4G_PREC_FP64) {
     prepare_impl<double>(p);
+  } else if (prec == HE4G_PREC_DF64) {
+    prepare_reg<df64>(p);
   } else {
     prepare_impl<float>(p);
     if (p.tiles.engine & ENGINE_XY) {

@@ -5,8 +5,10 @@
 #pragma once
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <utility>
 
+#include "df64.cuh"
 #include "he4g_internal.cuh"
 
 namespace he4g {
@@ -30,8 +32,28 @@ struct Cx<float> {
   static constexpr int kTile = 8;
   static constexpr int kPad = 4;
 };
+template <>
+struct Cx<df64> {
+  using T = df2;
+  static constexpr int kTile = 8;
+  static constexpr int kPad = 3;
+};
 template <typename R>
 using C2 = typename Cx<R>::T;
+
+// Storage type of the real fields a transform reads or writes (den, dencg,
+// pot4, the form factors): the arithmetic type itself, except that the df64
+// transforms of HE4G_PREC_DF64 read and write the FP64 fields of that form.
+template <typename R>
+struct FieldOf {
+  using T = R;
+};
+template <>
+struct FieldOf<df64> {
+  using T = double;
+};
+template <typename R>
+using Fld = typename FieldOf<R>::T;
 
 template <typename R>
 __device__ __forceinline__ int pidx(int i) {
@@ -158,6 +180,10 @@ template <>
 __device__ __forceinline__ const float2* twiddles<float>(const FftAxis& ax) {
   return ax.twf;
 }
+template <>
+__device__ __forceinline__ const df2* twiddles<df64>(const FftAxis& ax) {
+  return ax.twd;
+}
 
 // One Stockham pass of radix RAD over `nlines` lines of length n held in
 // shared memory at src + l*ld (natural order in, autosorted order out).
@@ -236,9 +262,32 @@ __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
+// Loads of real fields into the arithmetic type: one value (ldf), an
+// aligned pair of x-adjacent values (ld_pair); st_pair stores a pair.
 template <typename R>
-__device__ __forceinline__ C2<R> ld_pair(const R* p) {
+__device__ __forceinline__ R ldf(const Fld<R>* p) {
+  return __ldg(p);
+}
+template <>
+__device__ __forceinline__ df64 ldf<df64>(const double* p) {
+  return df_split(__ldg(p));
+}
+template <typename R>
+__device__ __forceinline__ C2<R> ld_pair(const Fld<R>* p) {
   return __ldg(reinterpret_cast<const C2<R>*>(p));
+}
+template <>
+__device__ __forceinline__ df2 ld_pair<df64>(const double* p) {
+  const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+  return df2{df_split(v.x), df_split(v.y)};
+}
+template <typename R>
+__device__ __forceinline__ void st_pair(Fld<R>* p, C2<R> v) {
+  *reinterpret_cast<C2<R>*>(p) = v;
+}
+template <>
+__device__ __forceinline__ void st_pair<df64>(double* p, df2 v) {
+  *reinterpret_cast<double2*>(p) = make_double2(df_to_double(v.x), df_to_double(v.y));
 }
 
 // Block-strided loop over w < total that issues the global loads of S
@@ -462,6 +511,17 @@ __device__ __forceinline__ R solid_penalty(R d, R beta, R dm, R cs) {
   const R x = beta * (d - dm);
   if constexpr (sizeof(R) == 4) {
     return penalty_f32(x, beta * d, cs);
+  } else if constexpr (std::is_same<R, df64>::value) {
+    // as the FP64 form: FP32 where x < -10, the FP64 tanh elsewhere
+    if (x.hi < -10.f) {
+      const float e = expf(2.f * x.hi);
+      const float inv = 1.f / (1.f + e);
+      const float bd = (beta * d).hi;
+      return df64((cs.hi * 2.f * e * inv) * (1.f + 2.f * bd * inv));
+    }
+    const double t = tanh(df_to_double(x));
+    const double p = df_to_double(cs) * (1.0 + t + df_to_double(beta * d) * (1.0 - t * t));
+    return df_split(p);
   } else {
     if (x < -10.0) {
       const float e = expf(2.f * (float)x);
@@ -480,8 +540,8 @@ enum { EPI_STORE = 0, EPI_POT4 = 1 };
 
 template <typename R>
 struct Pot4Args {
-  const R* dencg;
-  const R* den;
+  const Fld<R>* dencg;
+  const Fld<R>* den;
   Functional fn;
 };
 
@@ -492,7 +552,7 @@ struct SpecList {
 
 template <typename R>
 struct FactorList {
-  const R* f[3];
+  const Fld<R>* f[3];
   C2<R>* out[3];
 };
 
@@ -524,13 +584,13 @@ template <typename R>
 bool reg_z(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors, int nout,
            double scale, const void* add, cudaStream_t s, bool launch = true);
 template <typename R>
-bool reg_r2c(const Grid& g, const FftPlan& p, const C2<R>* twx, int pro, const R* a, const R* b, R c0, R c1,
-             C2<R>* out, cudaStream_t s, bool launch = true);
+bool reg_r2c(const Grid& g, const FftPlan& p, const C2<R>* twx, int pro, const Fld<R>* a, const Fld<R>* b, R c0,
+             R c1, C2<R>* out, cudaStream_t s, bool launch = true);
 template <typename R>
-bool reg_c2r(const Grid& g, const FftPlan& p, const C2<R>* twx, int epi, const C2<R>* i0, const C2<R>* i1, R* o0,
-             R* o1, int nspec, const Pot4Args<R>& pa, cudaStream_t s, bool launch = true);
+bool reg_c2r(const Grid& g, const FftPlan& p, const C2<R>* twx, int epi, const C2<R>* i0, const C2<R>* i1,
+             Fld<R>* o0, Fld<R>* o1, int nspec, const Pot4Args<R>& pa, cudaStream_t s, bool launch = true);
 template <typename R>
-bool reg_c2r_corr(const Grid& g, const FftPlan& p, const C2<R>* twx, C2<R>* spec, R* dencg, const R* den, R c0,
-                  R c1, cudaStream_t s, bool launch = true);
+bool reg_c2r_corr(const Grid& g, const FftPlan& p, const C2<R>* twx, C2<R>* spec, Fld<R>* dencg,
+                  const Fld<R>* den, R c0, R c1, cudaStream_t s, bool launch = true);
 
 }  // namespace he4g

@@ -18,8 +18,10 @@ constexpr int kMaxN = 320;        // largest tstgrid.f90 size
 constexpr int kStencilHalf = 6;   // 13-point stencils
 constexpr int kRedBlock = 256;    // threads of the reduction blocks
 
+struct df2;  // complex df64 (df64.cuh)
+
 // One 1D transform length with its mixed-radix factorisation and its
-// forward twiddles tw[t] = exp(-2 pi i t / n), t < n, in FP64 and FP32.
+// forward twiddles tw[t] = exp(-2 pi i t / n), t < n, in FP64, FP32 and df64.
 // mag_nr/mag_ns: ceil(2^32 / d) for the per-pass divisors d = n/R and
 // d = (product of the earlier radices), so that w / d = umulhi(w, mag) for
 // every index that occurs (w < 2^16, d <= 320).
@@ -31,6 +33,7 @@ struct FftAxis {
   unsigned mag_ns[kMaxFactors];
   const double2* tw;
   const float2* twf;
+  const df2* twd;
 };
 
 // Geometry of one run.
@@ -122,6 +125,7 @@ struct FftPlan {
   FftAxis y, z;
   const double2* twx;  // exp(-2 pi i k / nx), k < nx/2 (r2c/c2r packing)
   const float2* twxf;
+  const df2* twxd;
   FftTiles tiles;
 };
 

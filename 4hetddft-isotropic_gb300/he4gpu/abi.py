@@ -20,6 +20,8 @@ HE4G_ESTATE = -7
 CORE_OT = 0
 CORE_OTC = 1
 PREC_FP64 = 0
+PREC_MIXED = 1
+PREC_DF64 = 2
 
 ERRORS = {
     HE4G_EINVAL: "invalid argument",

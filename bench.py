@@ -12,7 +12,8 @@ flush is needed between steps.
 The headline line is the FP64 form (the reference's arithmetic). The same
 line carries a `mixed` block: the mixed-precision form (FP32 fields, FP64
 accumulators and reductions) on the same workload, with its deviation from
-the FP64 form after the same steps.
+the FP64 form after the same steps, and a `df64` block: the FP64 form with its
+FFT convolutions in paired-FP32 arithmetic, with the same deviation record.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -40,6 +41,8 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
 FP64 = 0
 MIXED = 1
+DF64 = 2
+FORM_NAME = {FP64: "FP64", MIXED: "mixed-precision", DF64: "df64"}
 
 
 def set_case(name):
@@ -59,7 +62,7 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64, fused_corr=False, fused_xy
     n = nx * ny * nz
     nh = (nx // 2 + 1) * ny * nz
     ev = 2  # potential evaluations per step
-    if prec == FP64:
+    if prec != MIXED:  # FP64 and df64: 8-byte reals, 16-byte complex values
         r, c = 8, 16  # real / complex element
         # R psi 16 pot4 8 uimp 8 timec 4 p3 16 h1 16 h2 16 pc 16 | W p3 16 pc 16 h2 16 den 8
         pred = 156 * n
@@ -76,7 +79,7 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64, fused_corr=False, fused_xy
         "pc_correct": corr,
         # FP64: its own pass writing uimp; mixed: uimp is evaluated in the
         # force kernel, whose bytes below include the uimp write
-        "potenimp": ev * r * n if prec == FP64 else 0,
+        "potenimp": ev * r * n if prec != MIXED else 0,
         # den -> spectrum; den, dencg -> spectrum (correlation prologue)
         "fft_x_r2c": ev * ((r * n + c * nh) + (2 * r * n + c * nh)),
         # fwd 1, inv 1, fwd 1, inv 1 spectrum: read + write each
@@ -304,7 +307,7 @@ def metric_name(case, prec=FP64):
         nx, ny, nz = case_grid(case)
         grid = f"{nx}^3" if nx == ny == nz else f"{nx}x{ny}x{nz}"
         m = f"steps/s at {grid} (FP64 predictor-corrector step, He_{c['n4']} + {c['imp']})"
-    return m if prec == FP64 else m.replace("FP64", "mixed-precision")
+    return m if prec == FP64 else m.replace("FP64", FORM_NAME[prec])
 
 
 def reference_arm(args):
@@ -375,7 +378,7 @@ def timed_steps(run, cfg, prec, steps, barrier, clock_gpu):
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
         "peak_source": peak_kind, "kernel": top["family"],
-        "traffic": (TRAFFIC_256[prec].get(top["family"])
+        "traffic": (TRAFFIC_256.get(prec, {}).get(top["family"])
                     if (cfg.nx, cfg.ny, cfg.nz) == (256, 256, 256) else None),
         "traffic_source": "ncu dram bytes per launch (profiles/, 256^3 capture)",
         "step_algorithmic_bytes": step_bytes, "step_gbs": step_gbs, "step_frac": step_gbs / peak,
@@ -401,7 +404,7 @@ def ours(args):
 
     import he4gpu
     he4gpu.abi.load()
-    prec = MIXED if args.precision == "mixed" else FP64
+    prec = {"fp64": FP64, "mixed": MIXED, "df64": DF64}[args.precision]
     run, cfg, psi, r, v, meta = make_run(prec)
     run.set_state(psi, r, v)
     warm = max(args.warmup, 3)
@@ -415,9 +418,11 @@ def ours(args):
             e2e_val, h2d, d2h = None, 0, 0
         else:
             e2e_val, h2d, d2h = e2e_measure(run, psi, max(3, min(args.steps, 10)))
-        mixed_block = None
+        mixed_block = df64_block = None
         if prec == FP64 and ws == 1 and not args.no_mixed:
-            mixed_block = mixed_measure(args, run, barrier, local)
+            mixed_block = form_measure(args, run, barrier, local, MIXED)
+        if prec == FP64 and ws == 1 and not args.no_df64:
+            df64_block = form_measure(args, run, barrier, local, DF64)
         cpu = None
         if ws == 1 and not args.no_cpu:
             try:
@@ -433,9 +438,9 @@ def ours(args):
             "metric": metric_name(CASE, prec),
             "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps, "warmup": warm,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if prec == FP64 else "mixed (f32 fields, f64 accumulators)",
+            "dtype": DTYPE[prec],
             "data": "synthetic (seeded Woods-Saxon droplet + Xe)",
-            "config": {"workload": CASE + (" FP64" if prec == FP64 else " mixed") + " predictor-corrector step",
+            "config": {"workload": f"{CASE} {FORM_NAME[prec]} predictor-corrector step",
                        "grid": [cfg.nx, cfg.ny, cfg.nz], "h": meta["h"], "n4": meta["n4"], "impurity": meta["imp"],
                        "v_A_per_ps": meta["v"], "impact_parameter": f"{meta['b_frac']} R",
                        "l2": "inputs larger than L2 (psi 268 MB, history 1.9 GB); no flush",
@@ -454,6 +459,7 @@ def ours(args):
             "clocks": res["clocks"],
             "wall_s_timed": res["wall_s"],
             "mixed": mixed_block,
+            "df64": df64_block,
         }
     if dist:
         dist.barrier()
@@ -464,16 +470,27 @@ def ours(args):
     return 0
 
 
-def mixed_measure(args, run64, barrier, gpu):
-    """The mixed-precision form on the same workload, and its deviation from
-    the FP64 run after the same number of steps."""
+DTYPE = {
+    FP64: "f64",
+    MIXED: "mixed (f32 fields, f64 accumulators)",
+    DF64: "df64 (FFT convolutions in paired f32, 48-bit significands; f64 fields, stencils, updates, reductions)",
+}
+FORM_DTYPE = {
+    MIXED: "f32 fields/stencils/FFTs; f64 psi accumulator, reductions, force sum, trajectory",
+    DF64: "df64 FFT convolutions (paired f32); f64 fields, stencils, predictor-corrector, reductions, trajectory",
+}
+
+
+def form_measure(args, run64, barrier, gpu, prec):
+    """Another arithmetic form (mixed or df64) on the same workload, and its
+    deviation from the FP64 run after the same number of steps."""
     import numpy as np
-    run, cfg, psi, r, v, meta = make_run(MIXED)
+    run, cfg, psi, r, v, meta = make_run(prec)
     run.set_state(psi, r, v)
     steps64 = run64.steps_taken
     warm = max(args.warmup, 3)
     run.step(warm)
-    res = timed_steps(run, cfg, MIXED, args.steps, barrier, gpu)
+    res = timed_steps(run, cfg, prec, args.steps, barrier, gpu)
     # bring both runs to the same step count, then compare
     run.step(max(0, steps64 - run.steps_taken))
     extra = run.steps_taken - run64.steps_taken
@@ -494,7 +511,7 @@ def mixed_measure(args, run64, barrier, gpu):
     run.close()
     rf = res["roofline"]
     return {"value": args.steps / (ms * 1e-3), "unit": "steps/s", "ms_per_step": ms / args.steps,
-            "dtype": "f32 fields/stencils/FFTs; f64 psi accumulator, reductions, force sum, trajectory",
+            "dtype": FORM_DTYPE[prec],
             "fft_tiles": tiles,
             "hbm_gbs": rf["step_gbs"], "roofline": rf, "gpu_launches": res["launches"],
             "clocks": res["clocks"], "vs_fp64": dev}
@@ -511,10 +528,11 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "df64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision block")
+    ap.add_argument("--no-df64", action="store_true", help="skip the df64 block")
     ap.add_argument("--case", default=CASE, help="workload (profiling runs use smaller ones)")
     ap.add_argument("--tiles", default=None,
                     help="FFT tiles lpb_r2c,lpb_c2r,log2cols_y,log2cols_z instead of autotuning (profiling runs)")

@@ -52,9 +52,15 @@ extern "C" {
  * HE4G_PREC_MIXED: FFT convolutions, stencils, H.psi and the pointwise
  * functional in FP32; psi, its history, pc and q (the update accumulator),
  * the norm and energy sums, the force sum and the impurity trajectory in
- * FP64. */
+ * FP64.
+ * HE4G_PREC_DF64: the fields and state of HE4G_PREC_FP64, with the 3D FFT
+ * convolutions of poten (and the alpha_s term) in paired-FP32 ("double-
+ * float", df64) arithmetic: 48-bit significands, about 2^-48 relative
+ * rounding, at FP32 instruction rates. Needs nx/2, ny and nz in
+ * {16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 256}. */
 #define HE4G_PREC_FP64 0
 #define HE4G_PREC_MIXED 1
+#define HE4G_PREC_DF64 2
 
 /*
  * Run configuration. Defaults (he4g_default_config) are the reference's module
@@ -68,7 +74,7 @@ typedef struct he4g_config {
   int32_t core;        /* HE4G_CORE_OT or HE4G_CORE_OTC                      */
   int32_t lsolid;      /* solid penalty term (he4 lsolid); forces core OT    */
   int32_t lrk;         /* 1: Runge–Kutta–Gill every step (DFT4He3d.f90:840)  */
-  int32_t precision;   /* HE4G_PREC_FP64                                     */
+  int32_t precision;   /* HE4G_PREC_FP64, HE4G_PREC_MIXED or HE4G_PREC_DF64  */
   int32_t npot;        /* potential-table nodes (potenimpini.f90:13)         */
   double xmax, ymax, zmax; /* box half-extent; h = 2*xmax/nx (:274-276)      */
   double deltat;       /* time step in K^-1                                  */

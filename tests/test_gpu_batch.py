@@ -13,7 +13,7 @@ from helpers import gpu_run, make_case, rel_field
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_graph_replay_matches_direct_launches(precision):
     cfg, tk, psi, r, v, meta = make_case("he100_xe_32", precision=precision)
     a = gpu_run(cfg, tk, psi, r, v)
@@ -28,7 +28,7 @@ def test_graph_replay_matches_direct_launches(precision):
     assert a.launch_count == b.launch_count
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_runs_in_the_mix_match_runs_alone(precision):
     import he4gpu
     cases = ["he100_xe_32", "he300_ar_48", "he200_xe_40x48x64"]

@@ -1,0 +1,101 @@
+"""GPU parity of the df64 form (HE4G_PREC_DF64): the FP64 fields and state of
+the reference's arithmetic, with the 3D FFT convolutions of poten (and of the
+alpha_s term) in paired-FP32 arithmetic, against the FP64 CPU oracle.
+
+Tolerances are those of the FP64 form: fields after one potential evaluation
+agree to 1e-12 of their maximum; after N steps the density, psi, every energy
+component, the norm and the impurity trajectory agree to 1e-10 relative.
+uimp and the density gradient do not pass through a transform and stay
+bit-identical to the oracle's.
+"""
+import numpy as np
+import pytest
+
+from helpers import gpu_run, make_case, oracle_run, rel, rel_field, rel_vec
+
+pytestmark = pytest.mark.gpu
+
+DF64 = 2
+FIELD_TOL = 1e-12
+STEP_TOL = 1e-10
+
+
+@pytest.mark.parametrize("case", ["he100_xe_32", "he300_ar_48", "he200_xe_40x48x64"])
+def test_initial_evaluation(case):
+    cfg, tk, psi, r, v, meta = make_case(case, precision=DF64)
+    g = gpu_run(cfg, tk, psi, r, v)
+    o = oracle_run(cfg, tk, psi, r, v)
+    assert np.array_equal(g.field("uimp"), o.field("uimp"))
+    for name in ("dencg", "delj4", "pot4"):
+        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
+    for name in ("dxden", "dyden", "dzden"):
+        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
+    eg, eo = g.energy(), o.energy()
+    for k in eo:
+        assert abs(eg[k] - eo[k]) <= 1e-11 * max(abs(eo[k]), 1e-6), k
+    g.close()
+    o.close()
+
+
+@pytest.mark.parametrize("case,nsteps", [("he100_xe_32", 12), ("he300_ar_48", 8), ("he200_xe_40x48x64", 7),
+                                         ("he1000_xe_128", 5)])
+def test_steps_match_oracle(case, nsteps):
+    """3 RK-Gill + PC steps with the trailing re-evaluation (DFT4He3d.f90:840-852)."""
+    cfg, tk, psi, r, v, meta = make_case(case, precision=DF64)
+    g = gpu_run(cfg, tk, psi, r, v)
+    o = oracle_run(cfg, tk, psi, r, v)
+    eg = g.step(nsteps)
+    eo = o.step(nsteps)
+    assert rel_field(g.den, o.den) < STEP_TOL
+    assert rel_field(g.psi, o.psi) < STEP_TOL
+    assert abs(eg[0] - eo[0]) <= 1e-10 * np.max(np.abs(psi))
+    rg, vg, ag = g.impurity()
+    ro, vo, ao = o.impurity()
+    assert rel_vec(rg, ro) < STEP_TOL and rel_vec(vg, vo) < STEP_TOL and rel_vec(ag, ao) < 1e-8
+    enG, enO = g.energy(), o.energy()
+    for k in enO:
+        assert abs(enG[k] - enO[k]) <= STEP_TOL * max(abs(enO[k]), 1e-3), k
+    assert rel(g.den.sum(), o.den.sum()) < 1e-12
+    g.close()
+    o.close()
+
+
+def test_otc_alpha_s_matches_oracle():
+    """Core OTC (lsolid off): the alpha_s convolutions in df64 (term_alfa.f90)."""
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", core=1, lsolid=0, hcg=2.190323, precision=DF64)
+    g = gpu_run(cfg, tk, psi, r, v)
+    o = oracle_run(cfg, tk, psi, r, v)
+    for name in ("denalf", "ualphas", "pot4", "dencg"):
+        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
+    g.step(5)
+    o.step(5)
+    assert rel_field(g.den, o.den) < STEP_TOL
+    eg, eo = g.energy(), o.energy()
+    for k in eo:
+        assert abs(eg[k] - eo[k]) <= STEP_TOL * max(abs(eo[k]), 1e-3), k
+    g.close()
+    o.close()
+
+
+def test_df64_tracks_the_fp64_form():
+    """The df64 and FP64 forms on the GPU stay within rounding of each other."""
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", precision=DF64)
+    cfg64, *_ = make_case("he100_xe_32")
+    a = gpu_run(cfg, tk, psi, r, v)
+    b = gpu_run(cfg64, tk, psi, r, v)
+    a.step(20)
+    b.step(20)
+    assert rel_field(a.psi, b.psi) < 1e-11
+    assert rel_vec(a.impurity()[0], b.impurity()[0]) < 1e-12
+    a.close()
+    b.close()
+
+
+def test_lengths_without_a_register_pass_are_refused():
+    """nx/2 = 36 has no register specialisation: df64 refuses the grid at
+    creation instead of falling back to another arithmetic."""
+    import he4gpu
+    cfg = he4gpu.default_config(72, 64, 64, 14.4, precision=DF64)
+    with pytest.raises(he4gpu.He4gError) as err:
+        he4gpu.Run(cfg)
+    assert err.value.code == he4gpu.abi.HE4G_EINVAL
