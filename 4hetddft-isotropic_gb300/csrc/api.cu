@@ -11,9 +11,11 @@
 // Precision: HE4G_PREC_FP64 keeps every array in FP64. HE4G_PREC_MIXED keeps
 // psi, its history, pc and q in FP64 and everything else (fields, spectra,
 // tables, hpsiold) in FP32, plus an FP32 copy of psi for the stencils
-// (psi32[cur32], ping-ponged with psi32[1 - cur32]). HE4G_PREC_DF64 keeps
-// the arrays of the FP64 form and runs its 3D FFT convolutions in paired-FP32
-// (df64) arithmetic on df64 spectra.
+// (psi32[cur32], ping-ponged with psi32[1 - cur32]). HE4G_PREC_DF64 holds
+// every per-point array in df64 (paired FP32, fielddf.cu) in the byte layout
+// of the FP64 form and computes the step in df64 arithmetic; the ABI converts
+// at its boundary, and energy, observables and field readback run the FP64
+// kernels on converted copies (the m_* mirrors).
 //
 // The mean field sums the Lennard-Jones convolution and the correlation
 // convolution in k-space before one shared inverse transform, so delj4 is
@@ -29,6 +31,7 @@
 #include <vector>
 
 #include "df64.cuh"
+#include "he4g_df.cuh"
 #include "he4g_internal.cuh"
 
 using namespace he4g;
@@ -109,6 +112,13 @@ struct he4g_run {
   void *ualphas = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr,
        *t6 = nullptr;
   float* timec = nullptr;
+  // df64 form only: stencil rows, h2o2m4 and grids in df64; FP64 mirrors of
+  // psi and the real fields for the FP64 energy and readback kernels
+  StencilD std{};
+  df64 h2d{};
+  df64 *xsd = nullptr, *ysd = nullptr, *zsd = nullptr;
+  double2* m_psi = nullptr;
+  double *m_den = nullptr, *m_dencg = nullptr, *m_delj4 = nullptr, *m_uimp = nullptr;
   // mixed precision only
   float2* psi32[2] = {nullptr, nullptr};
   int cur32 = 0;
@@ -141,6 +151,13 @@ struct he4g_run {
 namespace {
 
 bool mixed(const he4g_run* r) { return r->prec == HE4G_PREC_MIXED; }
+bool dfm(const he4g_run* r) { return r->prec == HE4G_PREC_DF64; }
+
+// df64 split of a long double: hi = RN(v), lo = RN(v - hi)
+df64 df_of(long double v) {
+  const float hi = static_cast<float>(v);
+  return df64(hi, static_cast<float>(v - static_cast<long double>(hi)));
+}
 
 int fail(he4g_run* r, int code, const std::string& msg) {
   if (r) r->err = msg;
@@ -227,6 +244,13 @@ void collect_timing(he4g_run* r) {
 
 // upload of a host double array into a precision-typed device array
 void upload_field(he4g_run* r, void* dst, const double* src, size_t n) {
+  if (dfm(r)) {
+    std::vector<df64> d(n);
+    for (size_t i = 0; i < n; ++i) d[i] = df_of(src[i]);
+    cudaMemcpyAsync(dst, d.data(), sizeof(df64) * n, cudaMemcpyHostToDevice, r->s);
+    cudaStreamSynchronize(r->s);
+    return;
+  }
   if (!mixed(r)) {
     cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, r->s);
     cudaStreamSynchronize(r->s);
@@ -240,6 +264,10 @@ void upload_field(he4g_run* r, void* dst, const double* src, size_t n) {
 
 int download_field(he4g_run* r, const void* src, double* dst, size_t n, const char* where) {
   cudaError_t e;
+  if (dfm(r)) {  // through the FP64 mirror of den
+    launch_df_to_f64(static_cast<const df64*>(src), r->m_den, (long long)n, r->s);
+    src = r->m_den;
+  }
   if (!mixed(r)) {
     e = cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, r->s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
@@ -250,12 +278,6 @@ int download_field(he4g_run* r, const void* src, double* dst, size_t n, const ch
     for (size_t i = 0; i < n; ++i) dst[i] = f[i];
   }
   return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, where);
-}
-
-// df64 split of a long double: hi = RN(v), lo = RN(v - hi)
-df64 df_of(long double v) {
-  const float hi = static_cast<float>(v);
-  return df64(hi, static_cast<float>(v - static_cast<long double>(hi)));
 }
 
 void make_axis(he4g_run* r, FftAxis& ax, int n) {
@@ -327,9 +349,16 @@ ImpTable imp_table(const he4g_run* r) {
                   static_cast<float>(1.0 / r->cfg.delinter), static_cast<float>(r->cfg.npot - 1)};
 }
 
+ImpTableD imp_table_d(const he4g_run* r) {
+  return ImpTableD{r->xsd, r->ysd, r->zsd, static_cast<const df64*>(r->potion), r->cfg.npot,
+                   static_cast<float>(r->cfg.npot - 1), df_of(1.0L / static_cast<long double>(r->cfg.delinter))};
+}
+
 void potenimp_dev(he4g_run* r, int sel) {
   Tick t(r, F_POTENIMP);
-  if (mixed(r))
+  if (dfm(r))
+    launch_potenimp_df(r->g, imp_table_d(r), r->imp, sel, static_cast<df64*>(r->uimp), r->s);
+  else if (mixed(r))
     launch_potenimp_mp(r->g, imp_table(r), r->imp, sel, static_cast<float*>(r->uimp), r->s);
   else
     launch_potenimp(r->g, r->xs, r->ys, r->zs, static_cast<const double*>(r->potion), r->cfg.npot, r->cfg.delinter,
@@ -553,7 +582,10 @@ void delj4_dev(he4g_run* r) {
 void force_dev(he4g_run* r, int store_accel, int sel = 1, bool store_uimp = false, bool record = false) {
   const ForceFinish fin{r->imp, r->counters, record ? r->ring : nullptr, r->g.dxyz, r->mass, store_accel};
   Tick t(r, F_FORCE);
-  if (mixed(r))
+  if (dfm(r))
+    t.launched(launch_force_df(r->g, r->std, static_cast<const df64*>(r->den), imp_table_d(r), r->imp, sel,
+                               store_uimp ? static_cast<df64*>(r->uimp) : nullptr, r->partials, fin, r->s));
+  else if (mixed(r))
     t.launched(launch_force_mp(r->g, r->stf, static_cast<const float*>(r->den), imp_table(r), r->imp, sel,
                                store_uimp ? static_cast<float*>(r->uimp) : nullptr, r->partials, fin, r->s));
   else
@@ -564,7 +596,7 @@ void force_dev(he4g_run* r, int store_accel, int sel = 1, bool store_uimp = fals
 // potenimp(centre sel); poten(); forceimp(rimp, aimp); aimp /= m;
 // record: the step's trajectory row after the force
 void evaluate_at(he4g_run* r, int sel, bool record = false) {
-  if (mixed(r)) {
+  if (mixed(r) || dfm(r)) {
     poten_dev(r);  // does not read uimp
     force_dev(r, 1, sel, true, record);
   } else {
@@ -600,7 +632,12 @@ void steprk_dev(he4g_run* r, double dt) {
       // stage 1 shifts the histories: hpsiold(2) = hpsiold(1), hpsiold(1) = H.psi,
       // psiold(3..1) = psiold(2..1), psi
       void* f_out = j == 0 ? r->h[1] : nullptr;
-      if (mixed(r)) {
+      if (dfm(r)) {
+        launch_rk_stage_df(r->g, r->std, r->h2d, reinterpret_cast<const df2*>(r->psi), reinterpret_cast<df2*>(r->scratch),
+                           reinterpret_cast<df2*>(r->q), static_cast<df2*>(f_out), static_cast<const df64*>(r->pot4),
+                           static_cast<const df64*>(r->uimp), r->timec, static_cast<df64*>(r->den), df_of(arun[j]),
+                           df_of(brun[j]), df_of(crun[j]), df_of(dt), health, r->s);
+      } else if (mixed(r)) {
         launch_rk_stage_mp(r->g, r->stf, r->fn, r->psi32[r->cur32], r->psi, r->scratch, r->psi32[1 - r->cur32],
                            r->q, static_cast<float2*>(f_out), static_cast<const float*>(r->pot4),
                            static_cast<const float*>(r->uimp), r->timec, static_cast<float*>(r->den), arun[j],
@@ -663,7 +700,14 @@ void steppc_dev(he4g_run* r, double dt) {
   const bool mp = mixed(r);
   {
     Tick t(r, F_PC_PREDICT);
-    if (mp) {
+    if (dfm(r)) {
+      launch_pc_predict_df(r->g, r->std, r->h2d, reinterpret_cast<const df2*>(r->psi),
+                           reinterpret_cast<df2*>(r->old[2]), static_cast<const df2*>(r->h[0]),
+                           static_cast<df2*>(r->h[1]), reinterpret_cast<df2*>(r->pc), static_cast<const df64*>(r->pot4),
+                           static_cast<const df64*>(r->uimp), r->timec, static_cast<df64*>(r->den),
+                           df_of(4.0L / 3.0L * static_cast<long double>(dt)), df_of(112.0L / 121.0L), c4o3 * dt, c112, r->imp,
+                           r->s);
+    } else if (mp) {
       launch_pc_predict_mp(r->g, r->stf, r->fn, r->psi32[r->cur32], r->old[2], r->psi32[1 - r->cur32],
                            static_cast<const float2*>(r->h[0]), static_cast<float2*>(r->h[1]), r->pc,
                            static_cast<const float*>(r->pot4), static_cast<const float*>(r->uimp), r->timec,
@@ -680,7 +724,14 @@ void steppc_dev(he4g_run* r, double dt) {
   const PcFinish fin{r->imp, r->counters, dt, c9, static_cast<double>(r->g.n)};
   {
     Tick t(r, F_PC_CORRECT);
-    if (mp) {
+    if (dfm(r)) {
+      t.launched(launch_pc_correct_df(
+          r->g, r->std, r->h2d, reinterpret_cast<const df2*>(psit), reinterpret_cast<const df2*>(r->old[2]),
+          reinterpret_cast<const df2*>(r->old[1]), static_cast<const df2*>(r->h[0]), static_cast<const df2*>(r->h[1]),
+          reinterpret_cast<df2*>(r->pc), static_cast<const df64*>(r->pot4), static_cast<const df64*>(r->uimp), r->timec,
+          reinterpret_cast<df2*>(r->scratch), static_cast<df64*>(r->den), r->partials, df_of(3.0L * dt),
+          df_of(9.0L / 121.0L), &r->imp->health, fin, r->s));
+    } else if (mp) {
       t.launched(launch_pc_correct_mp(r->g, r->stf, r->fn, r->psi32[r->cur32], r->old[2], r->old[1],
                            static_cast<const float2*>(r->h[0]), static_cast<const float2*>(r->h[1]), r->pc,
                            static_cast<const float*>(r->pot4), static_cast<const float*>(r->uimp), r->timec,
@@ -807,6 +858,7 @@ int he4g_footprint(const he4g_config* c, uint64_t* bytes) {
   const uint64_t n = (uint64_t)c->nx * c->ny * c->nz;
   const uint64_t nh = (uint64_t)(c->nx / 2 + 1) * c->ny * c->nz;
   const bool mp = c->precision == HE4G_PREC_MIXED;
+  const bool dfp = c->precision == HE4G_PREC_DF64;
   const bool otc = c->core == HE4G_CORE_OTC && !c->lsolid;
   const uint64_t rs = mp ? 4 : 8;
   uint64_t b = 0, nalloc = 0;
@@ -827,6 +879,11 @@ int he4g_footprint(const he4g_config* c, uint64_t* bytes) {
     add(8 * n, 2);                                  // FP32 copies of psi
     add(4 * (uint64_t)(c->nx + c->ny + c->nz), 3);  // FP32 grids
   }
+  if (dfp) {
+    add(8 * (uint64_t)(c->nx + c->ny + c->nz), 3);  // df64 grids
+    add(16 * n);                                    // FP64 mirror of psi
+    add(8 * n, 4);                                  // FP64 mirrors of den, dencg, delj4, uimp
+  }
   if (otc) {
     add(2 * rs * nh);
     add(rs * nh);
@@ -838,7 +895,7 @@ int he4g_footprint(const he4g_config* c, uint64_t* bytes) {
   add(64 * 8);
   add(sizeof(ImpState));
   add((uint64_t)kRingRows * kRingCols * 8);
-  add(24 * (uint64_t)(c->nx / 2 + c->ny + c->nz + c->nx / 2), 4);  // twiddle tables
+  add(40 * (uint64_t)(c->nx / 2 + c->ny + c->nz + c->nx / 2), 4);  // twiddle tables (FP64, FP32, df64)
   // allocation granularity (2 MiB pages) bounds the rounding of each buffer
   *bytes = b + nalloc * (2ull << 20);
   return HE4G_OK;
@@ -869,6 +926,8 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   if (c.precision == HE4G_PREC_DF64 &&
       !(fft_reg_supported(c.nx / 2) && fft_reg_supported(c.ny) && fft_reg_supported(c.nz)))
     return bad("HE4G_PREC_DF64 needs nx/2, ny and nz in {16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 256}");
+  if (c.precision == HE4G_PREC_DF64 && c.core == HE4G_CORE_OTC)
+    return bad("HE4G_PREC_DF64 supports core OT (the alpha_s term of core OTC runs in FP64 or mixed precision)");
   r->prec = c.precision;
   r->rs = mixed(r) ? 4 : 8;
   if (cudaStreamCreateWithFlags(&r->s, cudaStreamNonBlocking) != cudaSuccess) return bad("no CUDA device");
@@ -907,6 +966,24 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
     r->st.d2c += r->st.d2[a][0];
   }
   r->stf.d2c = static_cast<float>(r->st.d2c);
+  {
+    // df64 rows from the exact rationals (long double), split hi + lo
+    const long double q1[7] = {0.0L, 6.0L / 7.0L, -15.0L / 56.0L, 5.0L / 63.0L, -1.0L / 56.0L, 1.0L / 385.0L,
+                               -1.0L / 5544.0L};
+    const long double q2[7] = {-5369.0L / 1800.0L, 12.0L / 7.0L, -15.0L / 56.0L, 10.0L / 189.0L,
+                               -1.0L / 112.0L,     2.0L / 1925.0L, -1.0L / 16632.0L};
+    long double c2 = 0.0L;
+    for (int a = 0; a < 3; ++a) {
+      const long double h = hh[a];
+      for (int k = 0; k <= kStencilHalf; ++k) {
+        r->std.d1[a][k] = df_of(q1[k] / h);
+        r->std.d2[a][k] = df_of(q2[k] / (h * h));
+      }
+      c2 += q2[0] / (h * h);
+    }
+    r->std.d2c = df_of(c2);
+    r->h2d = df_of(static_cast<long double>(c.h2o2m4));
+  }
   Functional& fn = r->fn;
   fn.h2o2m4 = c.h2o2m4;
   fn.cp4 = c.cp4;
@@ -941,6 +1018,13 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   chk(r->ys = dalloc<double>(r, c.ny, false));
   chk(r->zs = dalloc<double>(r, c.nz, false));
   for (void** p : {&r->dx, &r->dy, &r->dz}) chk(*p = dalloc_bytes(r, rs * n));
+  if (dfm(r)) {
+    chk(r->xsd = dalloc<df64>(r, c.nx, false));
+    chk(r->ysd = dalloc<df64>(r, c.ny, false));
+    chk(r->zsd = dalloc<df64>(r, c.nz, false));
+    chk(r->m_psi = dalloc<double2>(r, n, false));
+    for (double** p : {&r->m_den, &r->m_dencg, &r->m_delj4, &r->m_uimp}) chk(*p = dalloc<double>(r, n, false));
+  }
   if (mixed(r)) {
     for (int i = 0; i < 2; ++i) chk(r->psi32[i] = dalloc<float2>(r, n));
     chk(r->xsf = dalloc<float>(r, c.nx, false));
@@ -999,6 +1083,15 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
     cudaMemcpyAsync(r->xsf, xf.data(), sizeof(float) * c.nx, cudaMemcpyHostToDevice, r->s);
     cudaMemcpyAsync(r->ysf, yf.data(), sizeof(float) * c.ny, cudaMemcpyHostToDevice, r->s);
     cudaMemcpyAsync(r->zsf, zf.data(), sizeof(float) * c.nz, cudaMemcpyHostToDevice, r->s);
+  }
+  std::vector<df64> xd(c.nx), yd(c.ny), zd(c.nz);
+  if (dfm(r)) {
+    for (int i = 0; i < c.nx; ++i) xd[i] = df_of(x[i]);
+    for (int i = 0; i < c.ny; ++i) yd[i] = df_of(y[i]);
+    for (int i = 0; i < c.nz; ++i) zd[i] = df_of(z[i]);
+    cudaMemcpyAsync(r->xsd, xd.data(), sizeof(df64) * c.nx, cudaMemcpyHostToDevice, r->s);
+    cudaMemcpyAsync(r->ysd, yd.data(), sizeof(df64) * c.ny, cudaMemcpyHostToDevice, r->s);
+    cudaMemcpyAsync(r->zsd, zd.data(), sizeof(df64) * c.nz, cudaMemcpyHostToDevice, r->s);
   }
   cudaStreamSynchronize(r->s);  // the host vectors go out of scope below
   make_axis(r, r->plan.xh, c.nx / 2);
@@ -1059,7 +1152,8 @@ void he4g_destroy(he4g_run* r) {
 int he4g_set_state(he4g_run* r, const double* psi, const double rimp[3], const double vimp[3]) {
   if (!r || !psi || !rimp || !vimp) return HE4G_EINVAL;
   const size_t n = r->g.n;
-  cudaError_t e = cudaMemcpyAsync(r->psi, psi, sizeof(double2) * n, cudaMemcpyHostToDevice, r->s);
+  // the df64 form receives psi in its FP64 mirror and converts it
+  cudaError_t e = cudaMemcpyAsync(dfm(r) ? r->m_psi : r->psi, psi, sizeof(double2) * n, cudaMemcpyHostToDevice, r->s);
   if (e != cudaSuccess) return cuda_fail(r, e, "set_state");
   cudaMemsetAsync(r->q, 0, sizeof(double2) * n, r->s);
   cudaMemsetAsync(r->pc, 0, sizeof(double2) * n, r->s);
@@ -1072,7 +1166,12 @@ int he4g_set_state(he4g_run* r, const double* psi, const double rimp[3], const d
   for (int a = 0; a < 3; ++a) h.ioldr[a] = h.ioldv[a] = a;
   for (int a = 0; a < 2; ++a) h.iolda[a] = a;
   cudaMemcpyAsync(r->imp, &h, sizeof h, cudaMemcpyHostToDevice, r->s);
-  if (mixed(r)) {
+  if (dfm(r)) {
+    launch_df_from_f64(reinterpret_cast<const double*>(r->m_psi), reinterpret_cast<df64*>(r->psi), 2 * (long long)n,
+                       r->s);
+    launch_density(r->g, r->m_psi, r->m_den, r->s);
+    launch_df_from_f64(r->m_den, static_cast<df64*>(r->den), (long long)n, r->s);
+  } else if (mixed(r)) {
     r->cur32 = 0;
     launch_split_mp(r->g, r->psi, r->psi32[0], static_cast<float*>(r->den), r->s);
   } else {
@@ -1414,7 +1513,12 @@ int he4g_get_trajectory(he4g_run* r, double* rows, int cap, int* n) {
 
 int he4g_get_psi(he4g_run* r, double* psi) {
   if (!r || !psi) return HE4G_EINVAL;
-  cudaError_t e = cudaMemcpyAsync(psi, r->psi, sizeof(double2) * r->g.n, cudaMemcpyDeviceToHost, r->s);
+  const double2* src = r->psi;
+  if (dfm(r)) {
+    launch_df_to_f64(reinterpret_cast<const df64*>(r->psi), reinterpret_cast<double*>(r->m_psi), 2 * r->g.n, r->s);
+    src = r->m_psi;
+  }
+  cudaError_t e = cudaMemcpyAsync(psi, src, sizeof(double2) * r->g.n, cudaMemcpyDeviceToHost, r->s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
   return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "get_psi");
 }
@@ -1440,6 +1544,13 @@ int he4g_get_field(he4g_run* r, int which, double* out) {
     case 5:
     case 6: {
       void* d = which == 4 ? r->dx : which == 5 ? r->dy : r->dz;
+      if (dfm(r)) {  // the FP64 stencil on the converted density; d is FP64
+        launch_df_to_f64(static_cast<const df64*>(r->den), r->m_den, r->g.n, r->s);
+        launch_grad1(r->g, r->st, which - 4, r->m_den, static_cast<double*>(d), r->s);
+        cudaError_t e = cudaMemcpyAsync(out, d, sizeof(double) * r->g.n, cudaMemcpyDeviceToHost, r->s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
+        return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "get_field");
+      }
       grad1_dev(r, which - 4, r->den, d);
       src = d;
       break;
@@ -1483,6 +1594,27 @@ int he4g_set_impurity(he4g_run* r, const double rr[3], const double v[3], const 
   return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "set_impurity");
 }
 
+namespace {
+// FP64 views of psi and the real fields for the FP64 energy kernels: the
+// run's own arrays, or in the df64 form their converted mirrors
+struct F64View {
+  const double2* psi;
+  const double *den, *dencg, *delj4, *uimp;
+};
+F64View f64_view(he4g_run* r) {
+  if (!dfm(r))
+    return {r->psi, static_cast<const double*>(r->den), static_cast<const double*>(r->dencg),
+            static_cast<const double*>(r->delj4), static_cast<const double*>(r->uimp)};
+  const long long n = r->g.n;
+  launch_df_to_f64(reinterpret_cast<const df64*>(r->psi), reinterpret_cast<double*>(r->m_psi), 2 * n, r->s);
+  launch_df_to_f64(static_cast<const df64*>(r->den), r->m_den, n, r->s);
+  launch_df_to_f64(static_cast<const df64*>(r->dencg), r->m_dencg, n, r->s);
+  launch_df_to_f64(static_cast<const df64*>(r->delj4), r->m_delj4, n, r->s);
+  launch_df_to_f64(static_cast<const df64*>(r->uimp), r->m_uimp, n, r->s);
+  return {r->m_psi, r->m_den, r->m_dencg, r->m_delj4, r->m_uimp};
+}
+}  // namespace
+
 int he4g_energy(he4g_run* r, he4g_energies* en) {
   int rc = check_ready(r);
   if (rc) return rc;
@@ -1490,6 +1622,7 @@ int he4g_energy(he4g_run* r, he4g_energies* en) {
   const Grid& g = r->g;
   const bool otc = r->fn.otc;
   delj4_dev(r);
+  F64View view{r->psi, nullptr, nullptr, nullptr, nullptr};
   if (mixed(r)) {
     launch_energy_point_mp(g, r->fn, static_cast<const float*>(r->den), static_cast<const float*>(r->dencg),
                            static_cast<const float*>(r->delj4), static_cast<const float*>(r->uimp),
@@ -1498,8 +1631,8 @@ int he4g_energy(he4g_run* r, he4g_energies* en) {
                            static_cast<const float*>(r->ix), static_cast<const float*>(r->iy),
                            static_cast<const float*>(r->iz), r->xs, r->ys, r->zs, r->partials, r->s);
   } else {
-    launch_energy_point(g, r->fn, static_cast<const double*>(r->den), static_cast<const double*>(r->dencg),
-                        static_cast<const double*>(r->delj4), static_cast<const double*>(r->uimp),
+    view = f64_view(r);
+    launch_energy_point(g, r->fn, view.den, view.dencg, view.delj4, view.uimp,
                         otc ? static_cast<const double*>(r->falfs) : nullptr, static_cast<const double*>(r->dx),
                         static_cast<const double*>(r->dy), static_cast<const double*>(r->dz),
                         static_cast<const double*>(r->ix), static_cast<const double*>(r->iy),
@@ -1507,7 +1640,7 @@ int he4g_energy(he4g_run* r, he4g_energies* en) {
   }
   launch_reduce(r->partials, r->pblocks, 12, r->small, r->s);
   cudaMemsetAsync(r->small + 40, 0, sizeof(double) * 3, r->s);
-  launch_energy_grad(g, r->st, r->psi, r->xs, r->ys, r->zs, r->small + 40, r->partials, r->s);
+  launch_energy_grad(g, r->st, view.psi, r->xs, r->ys, r->zs, r->small + 40, r->partials, r->s);
   launch_reduce(r->partials, r->pblocks, 7, r->small + 16, r->s);
   double v[24];
   ImpState h;
@@ -1542,14 +1675,15 @@ int he4g_observables(he4g_run* r, double npart, he4g_obs* o) {
   if (!o) return HE4G_EINVAL;
   const Grid& g = r->g;
   delj4_dev(r);
+  F64View view{r->psi, nullptr, nullptr, nullptr, nullptr};
   if (mixed(r)) {
     launch_energy_point_mp(g, r->fn, static_cast<const float*>(r->den), static_cast<const float*>(r->dencg),
                            static_cast<const float*>(r->delj4), static_cast<const float*>(r->uimp), nullptr, nullptr,
                            nullptr, nullptr, nullptr, nullptr, nullptr, r->xs, r->ys, r->zs, r->partials, r->s);
   } else {
-    launch_energy_point(g, r->fn, static_cast<const double*>(r->den), static_cast<const double*>(r->dencg),
-                        static_cast<const double*>(r->delj4), static_cast<const double*>(r->uimp), nullptr, nullptr,
-                        nullptr, nullptr, nullptr, nullptr, nullptr, r->xs, r->ys, r->zs, r->partials, r->s);
+    view = f64_view(r);
+    launch_energy_point(g, r->fn, view.den, view.dencg, view.delj4, view.uimp, nullptr, nullptr, nullptr, nullptr,
+                        nullptr, nullptr, nullptr, r->xs, r->ys, r->zs, r->partials, r->s);
   }
   launch_reduce(r->partials, r->pblocks, 12, r->small, r->s);
   double v[12];
@@ -1564,7 +1698,7 @@ int he4g_observables(he4g_run* r, double npart, he4g_obs* o) {
     o->r2[a] = v[4 + a] * dxyz;
   }
   cudaMemcpyAsync(r->small + 40, cm, sizeof cm, cudaMemcpyHostToDevice, r->s);
-  launch_energy_grad(g, r->st, r->psi, r->xs, r->ys, r->zs, r->small + 40, r->partials, r->s);
+  launch_energy_grad(g, r->st, view.psi, r->xs, r->ys, r->zs, r->small + 40, r->partials, r->s);
   launch_reduce(r->partials, r->pblocks, 7, r->small + 16, r->s);
   double w[7];
   cudaMemcpyAsync(w, r->small + 16, sizeof w, cudaMemcpyDeviceToHost, r->s);

@@ -1,5 +1,5 @@
-// df64.cuh — paired-FP32 ("double-float") arithmetic for the FFT passes of
-// the HE4G_PREC_DF64 form.
+// df64.cuh — paired-FP32 ("double-float") arithmetic of the HE4G_PREC_DF64
+// form: its FFT passes, stencils, updates and impurity kernels.
 //
 // A df64 is the unevaluated sum hi + lo of two FP32 numbers with
 // |lo| <= ulp(hi)/2: a 48-bit significand (rounding about 2^-48 = 3.6e-15
@@ -85,6 +85,27 @@ __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) {
   return df_fast2sum(s, t + (e + c.lo));
 }
 
+// a * b for an FP32 factor b (exact products of b with both parts)
+__device__ __forceinline__ df64 mulf(df64 a, float b) {
+  const float p = a.hi * b;
+  float e = fmaf(a.hi, b, -p);
+  e = fmaf(a.lo, b, e);
+  return df_fast2sum(p, e);
+}
+// a * 2^k (s a power of two: exact)
+__device__ __forceinline__ df64 scale2(df64 a, float s) { return df64(a.hi * s, a.lo * s); }
+
+// sqrt(a), a >= 0: the correctly rounded FP32 root y of hi and one Newton
+// step y + (a - y^2) / (2y) with a - y^2 formed exactly (TwoProd)
+__device__ __forceinline__ df64 df_sqrt(df64 a) {
+  if (!(a.hi > 0.f)) return df64(0.f, 0.f);
+  const float y = sqrtf(a.hi);
+  const float p = y * y;
+  const float pe = fmaf(y, y, -p);
+  const float d = ((a.hi - p) - pe) + a.lo;
+  return df_fast2sum(y, __fdividef(d, 2.f * y));
+}
+
 #ifdef __CUDACC__
 // double -> df64 on the device without the conversion instructions (which
 // GB300 issues on its FP64 pipe): hi = RN(d) by integer operations, the
@@ -106,5 +127,9 @@ __device__ __forceinline__ double df_to_double(df64 a) { return f2d(a.hi) + f2d(
 __device__ __forceinline__ he4g::df2 __ldg(const he4g::df2* p) {
   const float4 v = __ldg(reinterpret_cast<const float4*>(p));
   return he4g::df2{he4g::df64(v.x, v.y), he4g::df64(v.z, v.w)};
+}
+__device__ __forceinline__ he4g::df64 __ldg(const he4g::df64* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return he4g::df64(v.x, v.y);
 }
 #endif

@@ -395,7 +395,7 @@ void pot4_impl(const Grid& g, const FftPlan& p, const void* conv, const void* de
 
 // -------------------------------------------------------------- launchers
 // HE4G_PREC_DF64 runs the register engine only (its lengths are checked when
-// the run is created); its spectra are complex df64 and its real fields FP64.
+// the run is created); its spectra are complex df64 and its real fields df64.
 namespace {
 const df2* twxd(const FftPlan& p) { return p.twxd; }
 }  // namespace
@@ -405,7 +405,7 @@ void fft_x_r2c(const Grid& g, const FftPlan& p, int prec, const void* in, void* 
     launch_r2c<double, PRO_PLAIN>(g, p, static_cast<const double*>(in), nullptr, 0.0, 0.0,
                                   static_cast<double2*>(out), s);
   else if (prec == HE4G_PREC_DF64)
-    reg_r2c<df64>(g, p, twxd(p), PRO_PLAIN, static_cast<const double*>(in), nullptr, df64(0), df64(0),
+    reg_r2c<df64>(g, p, twxd(p), PRO_PLAIN, static_cast<const df64*>(in), nullptr, df64(0), df64(0),
                   static_cast<df2*>(out), s);
   else
     launch_r2c<float, PRO_PLAIN>(g, p, static_cast<const float*>(in), nullptr, 0.f, 0.f,
@@ -417,7 +417,7 @@ void fft_x_r2c_corr(const Grid& g, const FftPlan& p, int prec, const void* den, 
     launch_r2c<double, PRO_CORR>(g, p, static_cast<const double*>(den), static_cast<const double*>(dencg), cp4,
                                  cpp4, static_cast<double2*>(out), s);
   else if (prec == HE4G_PREC_DF64)
-    reg_r2c<df64>(g, p, twxd(p), PRO_CORR, static_cast<const double*>(den), static_cast<const double*>(dencg),
+    reg_r2c<df64>(g, p, twxd(p), PRO_CORR, static_cast<const df64*>(den), static_cast<const df64*>(dencg),
                   df64(cp4), df64(cpp4), static_cast<df2*>(out), s);
   else
     launch_r2c<float, PRO_CORR>(g, p, static_cast<const float*>(den), static_cast<const float*>(dencg),
@@ -429,7 +429,7 @@ void fft_x_r2c_prod(const Grid& g, const FftPlan& p, int prec, const void* a, co
     launch_r2c<double, PRO_PROD>(g, p, static_cast<const double*>(a), static_cast<const double*>(b), 0.0, 0.0,
                                  static_cast<double2*>(out), s);
   else if (prec == HE4G_PREC_DF64)
-    reg_r2c<df64>(g, p, twxd(p), PRO_PROD, static_cast<const double*>(a), static_cast<const double*>(b), df64(0),
+    reg_r2c<df64>(g, p, twxd(p), PRO_PROD, static_cast<const df64*>(a), static_cast<const df64*>(b), df64(0),
                   df64(0), static_cast<df2*>(out), s);
   else
     launch_r2c<float, PRO_PROD>(g, p, static_cast<const float*>(a), static_cast<const float*>(b), 0.f, 0.f,
@@ -458,9 +458,9 @@ void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins
     c2r_impl<double>(g, p, ins, outs, nspec, s);
   } else if (prec == HE4G_PREC_DF64) {
     const df2* i0 = static_cast<const df2*>(ins[0]);
-    double* o0 = static_cast<double*>(outs[0]);
+    df64* o0 = static_cast<df64*>(outs[0]);
     reg_c2r<df64>(g, p, twxd(p), EPI_STORE, i0, nspec > 1 ? static_cast<const df2*>(ins[1]) : i0, o0,
-                  nspec > 1 ? static_cast<double*>(outs[1]) : o0, nspec, Pot4Args<df64>{}, s);
+                  nspec > 1 ? static_cast<df64*>(outs[1]) : o0, nspec, Pot4Args<df64>{}, s);
   } else {
     c2r_impl<float>(g, p, ins, outs, nspec, s);
   }
@@ -470,9 +470,9 @@ void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv,
   if (prec == HE4G_PREC_FP64) {
     pot4_impl<double>(g, p, conv, dencg, den, fn, pot4, s);
   } else if (prec == HE4G_PREC_DF64) {
-    const Pot4Args<df64> pa{static_cast<const double*>(dencg), static_cast<const double*>(den), fn};
+    const Pot4Args<df64> pa{static_cast<const df64*>(dencg), static_cast<const df64*>(den), fn};
     const df2* c = static_cast<const df2*>(conv);
-    double* o = static_cast<double*>(pot4);
+    df64* o = static_cast<df64*>(pot4);
     reg_c2r<df64>(g, p, twxd(p), EPI_POT4, c, c, o, o, 1, pa, s);
   } else {
     pot4_impl<float>(g, p, conv, dencg, den, fn, pot4, s);
@@ -486,8 +486,8 @@ bool fft_x_c2r_corr(const Grid& g, const FftPlan& p, int prec, void* spec, void*
     return reg_c2r_corr<double>(g, p, twx_of<double>(p), static_cast<double2*>(spec), static_cast<double*>(dencg),
                                 static_cast<const double*>(den), cp4, cpp4, s);
   if (prec == HE4G_PREC_DF64)
-    return reg_c2r_corr<df64>(g, p, twxd(p), static_cast<df2*>(spec), static_cast<double*>(dencg),
-                              static_cast<const double*>(den), df64(cp4), df64(cpp4), s);
+    return reg_c2r_corr<df64>(g, p, twxd(p), static_cast<df2*>(spec), static_cast<df64*>(dencg),
+                              static_cast<const df64*>(den), df64(cp4), df64(cpp4), s);
   return reg_c2r_corr<float>(g, p, twx_of<float>(p), static_cast<float2*>(spec), static_cast<float*>(dencg),
                              static_cast<const float*>(den), (float)cp4, (float)cpp4, s);
 }

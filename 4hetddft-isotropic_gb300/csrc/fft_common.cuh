@@ -42,15 +42,12 @@ template <typename R>
 using C2 = typename Cx<R>::T;
 
 // Storage type of the real fields a transform reads or writes (den, dencg,
-// pot4, the form factors): the arithmetic type itself, except that the df64
-// transforms of HE4G_PREC_DF64 read and write the FP64 fields of that form.
+// pot4, the form factors). It is the arithmetic type in every form; the alias
+// keeps the signatures open to a form whose fields are stored in another type
+// than the one its transforms compute in.
 template <typename R>
 struct FieldOf {
   using T = R;
-};
-template <>
-struct FieldOf<df64> {
-  using T = double;
 };
 template <typename R>
 using Fld = typename FieldOf<R>::T;
@@ -268,26 +265,13 @@ template <typename R>
 __device__ __forceinline__ R ldf(const Fld<R>* p) {
   return __ldg(p);
 }
-template <>
-__device__ __forceinline__ df64 ldf<df64>(const double* p) {
-  return df_split(__ldg(p));
-}
 template <typename R>
 __device__ __forceinline__ C2<R> ld_pair(const Fld<R>* p) {
   return __ldg(reinterpret_cast<const C2<R>*>(p));
 }
-template <>
-__device__ __forceinline__ df2 ld_pair<df64>(const double* p) {
-  const double2 v = __ldg(reinterpret_cast<const double2*>(p));
-  return df2{df_split(v.x), df_split(v.y)};
-}
 template <typename R>
 __device__ __forceinline__ void st_pair(Fld<R>* p, C2<R> v) {
   *reinterpret_cast<C2<R>*>(p) = v;
-}
-template <>
-__device__ __forceinline__ void st_pair<df64>(double* p, df2 v) {
-  *reinterpret_cast<double2*>(p) = make_double2(df_to_double(v.x), df_to_double(v.y));
 }
 
 // Block-strided loop over w < total that issues the global loads of S

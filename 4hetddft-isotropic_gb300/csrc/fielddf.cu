@@ -1,0 +1,436 @@
+// fielddf.cu — the per-point kernels of the df64 form (HE4G_PREC_DF64): the
+// 13-point stencils with H.psi and the Runge–Kutta–Gill / Hamming
+// predictor–corrector updates, the impurity potential and the force
+// reduction, all in paired-FP32 arithmetic (df64.cuh) on df64 arrays; and the
+// conversions between df64 and FP64 arrays at the boundary of the form.
+//
+// They restate the FP64 kernels of field.cu (steprk.f90:57-92,
+// steppc.f90:45-65,119-134, potenimp.f90:44-46,71-95, derden.f90:26-28):
+// the same operations in the same order, each df64 operation rounding at
+// about 2^-48 instead of 2^-53, and FP32 instructions instead of FP64 ones,
+// which GB300 issues at about 61 times the rate. The block partials of the
+// sums and everything after them (the impurity updates, errHe) stay FP64.
+//
+// Two departures, both within the form's rounding: the impurity potential
+// takes the table node and the interpolation weight from one quotient
+// t = r/delinter (node floor(t), weight t - floor(t)), where the FP64 kernel
+// forms int(r/delinter) and mod(r,delinter)/delinter as the reference does;
+// the interpolation is continuous across nodes, so this moves uimp by
+// rounding only. And the density check of a Runge–Kutta stage tests |psi|^2
+// in FP64, as the FP64 form does, so that a density below FP32's range is not
+// taken for zero.
+#include "df64.cuh"
+#include "fpconv.cuh"
+#include "he4g_df.cuh"
+#include "impurity.cuh"
+
+namespace he4g {
+
+namespace {
+
+constexpr int kBX = 64, kBY = 4;  // point-kernel blocks (256 threads)
+constexpr int kZD = 8;            // z planes per thread of the force kernel
+
+struct Pt {
+  int i, j, k;
+  long long p;
+  bool ok;
+};
+__device__ __forceinline__ Pt point(const Grid& g) {
+  Pt t;
+  t.i = blockIdx.x * kBX + threadIdx.x;
+  t.j = blockIdx.y * kBY + threadIdx.y;
+  t.k = blockIdx.z;
+  t.ok = t.i < g.nx && t.j < g.ny;
+  t.p = ((long long)t.k * g.ny + t.j) * g.nx + t.i;
+  return t;
+}
+dim3 point_grid(const Grid& g) { return dim3((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, g.nz); }
+__device__ __forceinline__ int block_linear() {
+  return (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+}
+
+// plain (coherent) 16-byte load and store of a complex df64
+__device__ __forceinline__ df2 ldv(const df2* p) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  return df2{df64(v.x, v.y), df64(v.z, v.w)};
+}
+__device__ __forceinline__ void stv(df2* p, df2 v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo);
+}
+__device__ __forceinline__ void sts(df64* p, df64 v) { *reinterpret_cast<float2*>(p) = make_float2(v.hi, v.lo); }
+
+// health bits of a density: 1 not > 0, 2 non-finite (FP64 test)
+__device__ __forceinline__ int den_health(double d) {
+  const long long b = __double_as_longlong(d);
+  if (b > 0 && b < 0x7FF0000000000000LL) return 0;
+  if ((b & 0x7FF0000000000000LL) == 0x7FF0000000000000LL) return 3;
+  return 1;
+}
+// non-finite test on the high part (bit 2 of the health word)
+__device__ __forceinline__ int nonfinite(df64 d) {
+  return (__float_as_uint(d.hi) & 0x7F800000u) == 0x7F800000u ? 2 : 0;
+}
+
+// |z|^2
+__device__ __forceinline__ df64 norm2(df2 z) { return fma(z.x, z.x, z.y * z.y); }
+
+// (d2x + d2y + d2z) psi at a point, zero padded (Deriv3D_pc, id = 2):
+// symmetric pairs summed before the coefficient product
+__device__ __forceinline__ df2 lap13(const df2* __restrict__ f, const Pt& t, const Grid& g, const StencilD& st) {
+  const df2 c = __ldg(f + t.p);
+  df64 ar = st.d2c * c.x, ai = st.d2c * c.y;
+  const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+  const df2 zero{df64(0.f, 0.f), df64(0.f, 0.f)};
+#pragma unroll
+  for (int o = 1; o <= kStencilHalf; ++o) {
+    df2 a = t.i - o >= 0 ? __ldg(f + t.p - o) : zero;
+    df2 b = t.i + o < g.nx ? __ldg(f + t.p + o) : zero;
+    ar = fma(st.d2[0][o], a.x + b.x, ar);
+    ai = fma(st.d2[0][o], a.y + b.y, ai);
+    a = t.j - o >= 0 ? __ldg(f + t.p - o * sy) : zero;
+    b = t.j + o < g.ny ? __ldg(f + t.p + o * sy) : zero;
+    ar = fma(st.d2[1][o], a.x + b.x, ar);
+    ai = fma(st.d2[1][o], a.y + b.y, ai);
+    a = t.k - o >= 0 ? __ldg(f + t.p - o * sz) : zero;
+    b = t.k + o < g.nz ? __ldg(f + t.p + o * sz) : zero;
+    ar = fma(st.d2[2][o], a.x + b.x, ar);
+    ai = fma(st.d2[2][o], a.y + b.y, ai);
+  }
+  return df2{ar, ai};
+}
+
+// Sto4c = timec*(lap*h2o2m4 - pot4*psi) - i*uimp*psi (steppc.f90:55,123;
+// steprk.f90:74); timec = T + i with T single precision (DFT4He3d.f90:694),
+// exact as an FP32 factor
+__device__ __forceinline__ df2 hpsi(df2 lap, df2 ps, df64 pot, df64 u, float T, df64 h2) {
+  const df64 ar = fma(lap.x, h2, -(pot * ps.x));
+  const df64 ai = fma(lap.y, h2, -(pot * ps.y));
+  const df64 br = mulf(ar, T) - ai;
+  const df64 bi = mulf(ai, T) + ar;
+  return df2{fma(u, ps.y, br), fma(-u, ps.x, bi)};
+}
+
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* partials) {
+  __shared__ double sh[NV][kRedBlock / 32];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int a = 0; a < NV; ++a) {
+    double x = v[a];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[a][wid] = x;
+  }
+  __syncthreads();
+  if (tid < 32) {
+    const int nw = (blockDim.x * blockDim.y) >> 5;
+#pragma unroll
+    for (int a = 0; a < NV; ++a) {
+      double x = lane < nw ? sh[a][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) partials[(long long)block_linear() * NV + a] = x;
+    }
+  }
+}
+
+// FP32 warp sums of the |pc| terms, FP64 across warps (as the FP64 form)
+__device__ __forceinline__ void block_sum_f1(float x, double* partials) {
+  __shared__ double sh[kRedBlock / 32];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  if (lane == 0) sh[wid] = f2d(x);
+  __syncthreads();
+  if (tid == 0) {
+    const int nw = (blockDim.x * blockDim.y) >> 5;
+    double sum = 0.0;
+    for (int w = 0; w < nw; ++w) sum += sh[w];
+    partials[block_linear()] = sum;
+  }
+}
+
+// ------------------------------------------------------------ integrators
+// Predictor + modifier (steppc.f90:45-65); roles as k_pc_predict in field.cu.
+__global__ void __launch_bounds__(256) k_pc_predict_df(Grid g, StencilD st, df64 h2o2m4,
+                                                        const df2* __restrict__ psi, df2* p3,
+                                                        const df2* __restrict__ h1, df2* h2, df2* pc,
+                                                        const df64* __restrict__ pot4,
+                                                        const df64* __restrict__ uimp,
+                                                        const float* __restrict__ timec, df64* den, df64 c4o3dt,
+                                                        df64 c112, double c4o3dt_d, double c112_d, ImpState* imp) {
+  const Pt t = point(g);
+  if (imp && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    imp_pc_predict_body(imp, c4o3dt_d, c112_d);
+  if (!t.ok) return;
+  const df2 lap = lap13(psi, t, g, st);
+  const df2 ps = __ldg(psi + t.p);
+  const df2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), h2o2m4);
+  const df2 a1 = ldv(h1 + t.p), a2 = ldv(h2 + t.p), o3 = ldv(p3 + t.p), q = ldv(pc + t.p);
+  // 2 f_n - f_{n-1} + 2 f_{n-2}
+  const df64 tr = scale2(a2.x + f.x, 2.f) - a1.x;
+  const df64 ti = scale2(a2.y + f.y, 2.f) - a1.y;
+  const df2 s1{fma(c4o3dt, tr, o3.x), fma(c4o3dt, ti, o3.y)};
+  const df2 pn{fma(-c112, q.x, s1.x), fma(-c112, q.y, s1.y)};
+  stv(p3 + t.p, pn);
+  stv(pc + t.p, s1);
+  stv(h2 + t.p, f);
+  sts(den + t.p, norm2(pn));
+}
+
+// Corrector (steppc.f90:119-134): psi_out = C + c9*pc, pc -= C, the |pc|
+// partial sums of errHe and, in the last block, the impurity corrector.
+__global__ void __launch_bounds__(256) k_pc_correct_df(Grid g, StencilD st, df64 h2o2m4,
+                                                        const df2* __restrict__ psit, const df2* __restrict__ p3,
+                                                        const df2* __restrict__ p2, const df2* __restrict__ h1,
+                                                        const df2* __restrict__ h2, df2* pc,
+                                                        const df64* __restrict__ pot4,
+                                                        const df64* __restrict__ uimp,
+                                                        const float* __restrict__ timec, df2* psi_out, df64* den,
+                                                        double* partials, df64 f3, df64 c9, int* health,
+                                                        PcFinish fin) {
+  const Pt t = point(g);
+  float v = 0.f;
+  if (t.ok) {
+    const df2 lap = lap13(psit, t, g, st);
+    const df2 ps = __ldg(psit + t.p);
+    const df2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), h2o2m4);
+    const df2 a1 = __ldg(h1 + t.p), a2 = __ldg(h2 + t.p), o3 = __ldg(p3 + t.p), o2 = __ldg(p2 + t.p);
+    // f* + 2 f_n - f_{n-1}
+    const df64 tr = (scale2(a1.x, 2.f) + f.x) - a2.x;
+    const df64 ti = (scale2(a1.y, 2.f) + f.y) - a2.y;
+    const df2 s5{scale2(fma(f3, tr, mulf(o3.x, 9.f) - o2.x), 0.125f),
+                 scale2(fma(f3, ti, mulf(o3.y, 9.f) - o2.y), 0.125f)};
+    df2 q = ldv(pc + t.p);
+    q = df2{q.x - s5.x, q.y - s5.y};
+    stv(pc + t.p, q);
+    const df2 pn{fma(c9, q.x, s5.x), fma(c9, q.y, s5.y)};
+    stv(psi_out + t.p, pn);
+    const df64 d = norm2(pn);
+    sts(den + t.p, d);
+    v = sqrtf(fmaf(q.x.hi, q.x.hi, q.y.hi * q.y.hi));
+    const int h = nonfinite(d);
+    if (h) atomicOr(health, h);
+  }
+  block_sum_f1(v, partials);
+  if (threadIdx.y * blockDim.x + threadIdx.x >= 32) return;  // warp 0 finishes (when fin.cnt is set)
+  double tot[1];
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  if (fin.cnt && finish_sum<1>(partials, nb, fin.cnt, tot) && threadIdx.x == 0 && threadIdx.y == 0)
+    imp_pc_correct_body(fin.imp, tot[0], fin.dt, fin.c9, fin.nxyz);
+}
+
+// One Runge–Kutta–Gill stage (steprk.f90:57-92); f_out (stage 1 only)
+// receives H.psi as the new hpsiold(1).
+__global__ void __launch_bounds__(256) k_rk_stage_df(Grid g, StencilD st, df64 h2o2m4,
+                                                      const df2* __restrict__ psi, df2* psi_out, df2* q,
+                                                      df2* f_out, const df64* __restrict__ pot4,
+                                                      const df64* __restrict__ uimp,
+                                                      const float* __restrict__ timec, df64* den, df64 ar, df64 br,
+                                                      df64 cr, df64 dt, int* health) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const df2 lap = lap13(psi, t, g, st);
+  const df2 ps = __ldg(psi + t.p);
+  const df2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), h2o2m4);
+  df2 qq = ldv(q + t.p);
+  const df2 s1{ar * fma(-br, qq.x, f.x), ar * fma(-br, qq.y, f.y)};
+  qq = df2{fma(-cr, f.x, mulf(s1.x, 3.f) + qq.x), fma(-cr, f.y, mulf(s1.y, 3.f) + qq.y)};
+  stv(q + t.p, qq);
+  if (f_out) stv(f_out + t.p, f);
+  const df2 pn{fma(dt, s1.x, ps.x), fma(dt, s1.y, ps.y)};
+  stv(psi_out + t.p, pn);
+  sts(den + t.p, norm2(pn));
+  // steprk.f90:89-92 on |psi|^2 in FP64
+  const double xr = df_to_double(pn.x), xi = df_to_double(pn.y);
+  const int h = den_health(fma(xr, xr, xi * xi));
+  if (h) atomicOr(health, h);
+}
+
+// ------------------------------------------------------------- impurity
+// updatepoten (potenimp.f90:71-95) at the point (x, y, z) about centre c:
+// t = |x - c| / delinter, node floor(t), weight t - floor(t). Points beyond
+// the table give 0 and set *bad.
+__device__ __forceinline__ df64 uimp_at(df64 x, df64 y, df64 z, const df64 (&c)[3], const ImpTableD& tab,
+                                        int& bad) {
+  const df64 dx = x - c[0], dy = y - c[1], dz = z - c[2];
+  const df64 r = df_sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+  const df64 tq = r * tab.inv;
+  float fl = floorf(tq.hi);
+  if (fl == tq.hi && tq.lo < 0.f) fl -= 1.f;
+  if (!(fl >= 0.f && fl < tab.nlast)) {  // also catches NaN
+    bad = 1;
+    return df64(0.f, 0.f);
+  }
+  // fl < 2^23: adding 2^23 leaves the integer in the low mantissa bits
+  const int ir = __float_as_int(fl + 8388608.f) - 0x4B000000;
+  const df64 w = df_fast2sum(tq.hi - fl, tq.lo);
+  const df64 p0 = __ldg(tab.potion + ir), p1 = __ldg(tab.potion + ir + 1);
+  return fma(w, p1 - p0, p0);
+}
+
+__device__ __forceinline__ void centre_of(ImpState* imp, int sel, df64 (&c)[3]) {
+  const double* cd = sel == 0 ? imp->rimp : imp->center;
+  c[0] = df_split(cd[0]);
+  c[1] = df_split(cd[1]);
+  c[2] = df_split(cd[2]);
+}
+
+__global__ void __launch_bounds__(256) k_potenimp_df(Grid g, ImpTableD tab, ImpState* imp, int sel, df64* uimp) {
+  const Pt t = point(g);
+  df64 c[3];
+  centre_of(imp, sel, c);
+  if (sel == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    imp->center[0] = imp->rimp[0];
+    imp->center[1] = imp->rimp[1];
+    imp->center[2] = imp->rimp[2];
+  }
+  if (!t.ok) return;
+  int bad = 0;
+  const df64 u = uimp_at(__ldg(tab.xs + t.i), __ldg(tab.ys + t.j), __ldg(tab.zs + t.k), c, tab, bad);
+  if (bad) atomicOr(&imp->health, 4);
+  sts(uimp + t.p, u);
+}
+
+// derden (derden.f90:26-28) fused with uimp (stored when uimp_out is set) and
+// the force sums of forceimp (potenimp.f90:44-46). Each thread walks kZD z
+// planes of one (x, y) column with the z neighbours in a register window;
+// its df64 sums become FP64 before the block reduction.
+__global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df64* __restrict__ den,
+                                                   ImpTableD tab, ImpState* imp, int sel, df64* uimp_out,
+                                                   double* partials, ForceFinish fin) {
+  const int i = blockIdx.x * kBX + threadIdx.x;
+  const int j = blockIdx.y * kBY + threadIdx.y;
+  const int k0 = blockIdx.z * kZD;
+  df64 c[3];
+  centre_of(imp, sel, c);
+  double v[3] = {0.0, 0.0, 0.0};
+  int bad = 0;
+  if (i < g.nx && j < g.ny) {
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const long long col = (long long)j * g.nx + i;
+    const df64 zero(0.f, 0.f);
+    constexpr int W = kZD + 2 * kStencilHalf;
+    df64 wz[W];  // den at planes k0-6 .. k0+kZD+5 of this column
+#pragma unroll
+    for (int m = 0; m < W; ++m) {
+      const int k = k0 - kStencilHalf + m;
+      wz[m] = (k >= 0 && k < g.nz) ? __ldg(den + col + k * sz) : zero;
+    }
+    const df64 xi = __ldg(tab.xs + i), yj = __ldg(tab.ys + j);
+    df64 s[3] = {zero, zero, zero};
+#pragma unroll
+    for (int m = 0; m < kZD; ++m) {
+      const int k = k0 + m;
+      if (k < g.nz) {
+        const long long p = col + k * sz;
+        df64 gx = zero, gy = zero, gz = zero;
+#pragma unroll
+        for (int o = 1; o <= kStencilHalf; ++o) {
+          df64 a = i - o >= 0 ? __ldg(den + p - o) : zero;
+          df64 b = i + o < g.nx ? __ldg(den + p + o) : zero;
+          gx = fma(st.d1[0][o], b - a, gx);
+          a = j - o >= 0 ? __ldg(den + p - o * sy) : zero;
+          b = j + o < g.ny ? __ldg(den + p + o * sy) : zero;
+          gy = fma(st.d1[1][o], b - a, gy);
+          gz = fma(st.d1[2][o], wz[m + kStencilHalf + o] - wz[m + kStencilHalf - o], gz);
+        }
+        const df64 u = uimp_at(xi, yj, __ldg(tab.zs + k), c, tab, bad);
+        if (uimp_out) sts(uimp_out + p, u);
+        s[0] = fma(gx, u, s[0]);
+        s[1] = fma(gy, u, s[1]);
+        s[2] = fma(gz, u, s[2]);
+      }
+    }
+    for (int a = 0; a < 3; ++a) v[a] = df_to_double(s[a]);
+  }
+  if (bad) atomicOr(&imp->health, 4);
+  if (sel == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    // the centre of the stored uimp (k_potenimp's role in the FP64 form)
+    imp->center[0] = imp->rimp[0];
+    imp->center[1] = imp->rimp[1];
+    imp->center[2] = imp->rimp[2];
+  }
+  block_sum<3>(v, partials);
+  if (threadIdx.y * blockDim.x + threadIdx.x >= 32) return;  // warp 0 finishes (when fin.cnt is set)
+  double tot[3];
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  if (fin.cnt && finish_sum<3>(partials, nb, fin.cnt, tot) && threadIdx.x == 0 && threadIdx.y == 0) {
+    imp_force_body(fin.imp, tot, fin.dxyz, fin.mass, fin.store_accel);
+    if (fin.ring) imp_record_body(fin.imp, fin.ring);
+  }
+}
+
+// ------------------------------------------------------------ conversions
+__global__ void k_df_from_f64(const double* __restrict__ in, df64* __restrict__ out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    sts(out + i, df_split(in[i]));
+}
+__global__ void k_df_to_f64(const df64* __restrict__ in, double* __restrict__ out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = df_to_double(__ldg(in + i));
+}
+unsigned conv_blocks(long long n) {
+  const long long b = (n + 255) / 256;
+  return (unsigned)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16);
+}
+
+}  // namespace
+
+int force_blocks_df(const Grid& g) {
+  return ((g.nx + kBX - 1) / kBX) * ((g.ny + kBY - 1) / kBY) * ((g.nz + kZD - 1) / kZD);
+}
+
+void launch_pc_predict_df(const Grid& g, const StencilD& st, df64 h2o2m4, const df2* psi, df2* p3_out,
+                          const df2* h1, df2* h2_out, df2* pc, const df64* pot4, const df64* uimp,
+                          const float* timec, df64* den, df64 c4o3dt, df64 c112, double c4o3dt_d, double c112_d,
+                          ImpState* imp, cudaStream_t s) {
+  k_pc_predict_df<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, h2o2m4, psi, p3_out, h1, h2_out, pc, pot4, uimp,
+                                                           timec, den, c4o3dt, c112, c4o3dt_d, c112_d, imp);
+}
+
+int launch_pc_correct_df(const Grid& g, const StencilD& st, df64 h2o2m4, const df2* psit, const df2* p3,
+                         const df2* p2, const df2* h1, const df2* h2, df2* pc, const df64* pot4, const df64* uimp,
+                         const float* timec, df2* psi_out, df64* den, double* partials, df64 f3, df64 c9,
+                         int* health, const PcFinish& fin, cudaStream_t s) {
+  const dim3 grid = point_grid(g);
+  const int nb = (int)(grid.x * grid.y * grid.z);
+  PcFinish f = fin;
+  if (nb > kFinishInKernelMax) f.cnt = nullptr;
+  k_pc_correct_df<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, h2o2m4, psit, p3, p2, h1, h2, pc, pot4, uimp, timec,
+                                                  psi_out, den, partials, f3, c9, health, f);
+  return 1 + (f.cnt ? 0 : launch_finish_pc(partials, nb, fin, s));
+}
+
+void launch_rk_stage_df(const Grid& g, const StencilD& st, df64 h2o2m4, const df2* psi, df2* psi_out, df2* q,
+                        df2* f_out, const df64* pot4, const df64* uimp, const float* timec, df64* den, df64 ar,
+                        df64 br, df64 cr, df64 dt, int* health, cudaStream_t s) {
+  k_rk_stage_df<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, h2o2m4, psi, psi_out, q, f_out, pot4, uimp, timec,
+                                                         den, ar, br, cr, dt, health);
+}
+
+int launch_force_df(const Grid& g, const StencilD& st, const df64* den, const ImpTableD& tab, ImpState* imp,
+                    int sel, df64* uimp_out, double* partials, const ForceFinish& fin, cudaStream_t s) {
+  dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZD - 1) / kZD);
+  const int nb = (int)(grid.x * grid.y * grid.z);
+  ForceFinish f = fin;
+  if (nb > kFinishInKernelMax) f.cnt = nullptr;
+  k_force_df<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, tab, imp, sel, uimp_out, partials, f);
+  return 1 + (f.cnt ? 0 : launch_finish_force(partials, nb, fin, s));
+}
+
+void launch_potenimp_df(const Grid& g, const ImpTableD& tab, ImpState* imp, int sel, df64* uimp, cudaStream_t s) {
+  k_potenimp_df<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, tab, imp, sel, uimp);
+}
+
+void launch_df_from_f64(const double* in, df64* out, long long n, cudaStream_t s) {
+  k_df_from_f64<<<conv_blocks(n), 256, 0, s>>>(in, out, n);
+}
+void launch_df_to_f64(const df64* in, double* out, long long n, cudaStream_t s) {
+  k_df_to_f64<<<conv_blocks(n), 256, 0, s>>>(in, out, n);
+}
+
+}  // namespace he4g

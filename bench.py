@@ -77,9 +77,9 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64, fused_corr=False, fused_xy
     fam = {
         "pc_predict": pred,
         "pc_correct": corr,
-        # FP64: its own pass writing uimp; mixed: uimp is evaluated in the
-        # force kernel, whose bytes below include the uimp write
-        "potenimp": ev * r * n if prec != MIXED else 0,
+        # FP64: its own pass writing uimp; mixed and df64: uimp is evaluated
+        # in the force kernel, whose bytes below include the uimp write
+        "potenimp": ev * r * n if prec == FP64 else 0,
         # den -> spectrum; den, dencg -> spectrum (correlation prologue)
         "fft_x_r2c": ev * ((r * n + c * nh) + (2 * r * n + c * nh)),
         # fwd 1, inv 1, fwd 1, inv 1 spectrum: read + write each
@@ -90,7 +90,7 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64, fused_corr=False, fused_xy
         "fft_x_c2r": ev * (c * nh + r * n),
         # spectrum + dencg + den -> pot4
         "fft_x_c2r_pot4": ev * (c * nh + 3 * r * n),
-        # FP64: R den + uimp; mixed: R den, W uimp
+        # FP64: R den + uimp; mixed and df64: R den, W uimp
         "force": ev * 2 * r * n,
         "impurity_scalar": 0,
         "fft_x_c2r_corr": 0,

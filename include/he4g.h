@@ -53,11 +53,13 @@ extern "C" {
  * functional in FP32; psi, its history, pc and q (the update accumulator),
  * the norm and energy sums, the force sum and the impurity trajectory in
  * FP64.
- * HE4G_PREC_DF64: the fields and state of HE4G_PREC_FP64, with the 3D FFT
- * convolutions of poten (and the alpha_s term) in paired-FP32 ("double-
- * float", df64) arithmetic: 48-bit significands, about 2^-48 relative
- * rounding, at FP32 instruction rates. Needs nx/2, ny and nz in
- * {16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 256}. */
+ * HE4G_PREC_DF64: every field, the state and every step kernel (stencils,
+ * H.psi, the RK-Gill and predictor-corrector updates, the FFT convolutions,
+ * uimp and the force) in paired-FP32 ("double-float", df64) arithmetic:
+ * 48-bit significands, about 2^-48 relative rounding, at FP32 instruction
+ * rates; the block partials of the sums and the impurity stay FP64. The ABI
+ * takes and returns FP64 values as in HE4G_PREC_FP64. Core OT only; needs
+ * nx/2, ny and nz in {16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 256}. */
 #define HE4G_PREC_FP64 0
 #define HE4G_PREC_MIXED 1
 #define HE4G_PREC_DF64 2

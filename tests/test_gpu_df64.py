@@ -1,12 +1,16 @@
-"""GPU parity of the df64 form (HE4G_PREC_DF64): the FP64 fields and state of
-the reference's arithmetic, with the 3D FFT convolutions of poten (and of the
-alpha_s term) in paired-FP32 arithmetic, against the FP64 CPU oracle.
+"""GPU parity of the df64 form (HE4G_PREC_DF64): every per-point array and
+every step kernel (stencils, H.psi, the Runge–Kutta–Gill and predictor–
+corrector updates, the 3D FFT convolutions, the impurity potential and the
+force) in paired-FP32 arithmetic with 48-bit significands, against the FP64
+CPU oracle.
 
 Tolerances are those of the FP64 form: fields after one potential evaluation
 agree to 1e-12 of their maximum; after N steps the density, psi, every energy
 component, the norm and the impurity trajectory agree to 1e-10 relative.
-uimp and the density gradient do not pass through a transform and stay
-bit-identical to the oracle's.
+uimp, which the FP64 form matches bit for bit, agrees to 2e-12 of its
+maximum: the table coordinate t = r/delinter reaches 1e4, and its 48-bit
+rounding moves the interpolation weight by about 1e-10 next to the steepest
+table step.
 """
 import numpy as np
 import pytest
@@ -17,6 +21,7 @@ pytestmark = pytest.mark.gpu
 
 DF64 = 2
 FIELD_TOL = 1e-12
+UIMP_TOL = 2e-12
 STEP_TOL = 1e-10
 
 
@@ -25,7 +30,7 @@ def test_initial_evaluation(case):
     cfg, tk, psi, r, v, meta = make_case(case, precision=DF64)
     g = gpu_run(cfg, tk, psi, r, v)
     o = oracle_run(cfg, tk, psi, r, v)
-    assert np.array_equal(g.field("uimp"), o.field("uimp"))
+    assert rel_field(g.field("uimp"), o.field("uimp")) < UIMP_TOL
     for name in ("dencg", "delj4", "pot4"):
         assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
     for name in ("dxden", "dyden", "dzden"):
@@ -60,21 +65,38 @@ def test_steps_match_oracle(case, nsteps):
     o.close()
 
 
-def test_otc_alpha_s_matches_oracle():
-    """Core OTC (lsolid off): the alpha_s convolutions in df64 (term_alfa.f90)."""
+def test_reference_routines_compose_like_the_driver():
+    """steprk/steppc/potenimp/poten/forceimp called one by one, as the Fortran
+    driver calls them, give the same state as he4g_step in the df64 form."""
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", precision=DF64)
+    a = gpu_run(cfg, tk, psi, r, v)
+    b = gpu_run(cfg, tk, psi, r, v)
+    a.step(5)
+    dt = cfg.deltat
+    m = cfg.mimpur * 0.02061484
+    for it in range(1, 6):
+        if it <= 3:
+            b.steprk(dt)
+        else:
+            b.steppc(dt)
+        rb, vb, _ = b.impurity()
+        b.potenimp(rb)
+        b.poten()
+        F = b.forceimp(rb)
+        b.set_impurity(rb, vb, F / m)
+    assert np.array_equal(b.psi, a.psi)
+    assert all(np.array_equal(x, y) for x, y in zip(a.impurity(), b.impurity()))
+    a.close()
+    b.close()
+
+
+def test_otc_core_is_refused():
+    """The alpha_s term of core OTC has no df64 kernels: the form refuses it."""
+    import he4gpu
     cfg, tk, psi, r, v, meta = make_case("he100_xe_32", core=1, lsolid=0, hcg=2.190323, precision=DF64)
-    g = gpu_run(cfg, tk, psi, r, v)
-    o = oracle_run(cfg, tk, psi, r, v)
-    for name in ("denalf", "ualphas", "pot4", "dencg"):
-        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
-    g.step(5)
-    o.step(5)
-    assert rel_field(g.den, o.den) < STEP_TOL
-    eg, eo = g.energy(), o.energy()
-    for k in eo:
-        assert abs(eg[k] - eo[k]) <= STEP_TOL * max(abs(eo[k]), 1e-3), k
-    g.close()
-    o.close()
+    with pytest.raises(he4gpu.He4gError) as err:
+        gpu_run(cfg, tk, psi, r, v)
+    assert err.value.code == he4gpu.abi.HE4G_EINVAL
 
 
 def test_df64_tracks_the_fp64_form():
