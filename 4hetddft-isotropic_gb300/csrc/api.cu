@@ -383,7 +383,7 @@ void conv_dev(he4g_run* r, const void* a, const void* b, const void* tab, void* 
   {
     Tick t(r, F_FFT_Z_CONV);
     const void* f[1] = {tab};
-    fft_z_conv(g, r->plan, r->prec, r->spec0, sp, f, 1, 0.5 * g.renor, nullptr, r->s);
+    t.launched(fft_z_conv(g, r->plan, r->prec, r->spec0, sp, f, 1, 0.5 * g.renor, nullptr, r->s));
   }
   {
     Tick t(r, F_FFT_Y);
@@ -493,7 +493,7 @@ void poten_dev(he4g_run* r) {
     Tick t(r, F_FFT_Z_CONV);
     void* outs[3] = {r->spec0, r->spec1, r->spec2};
     const void* facs[3] = {r->wcgk, r->fvlj4, r->kalfs};
-    fft_z_conv(g, r->plan, prec, r->spec0, outs, facs, otc ? 3 : 2, 0.5 * g.renor, nullptr, r->s);
+    t.launched(fft_z_conv(g, r->plan, prec, r->spec0, outs, facs, otc ? 3 : 2, 0.5 * g.renor, nullptr, r->s));
   }
   // inverse y, dencg and the correlation prologue, forward y: one fused
   // plane kernel, else the y passes around one fused row pass on the
@@ -537,7 +537,7 @@ void poten_dev(he4g_run* r) {
     // correlation convolution, plus the Lennard-Jones field already in spec1
     Tick t(r, F_FFT_Z_CONV);
     const void* f1[1] = {r->wcgk};
-    fft_z_conv(g, r->plan, prec, r->spec0, sp0, f1, 1, 0.5 * g.renor, r->spec1, r->s);
+    t.launched(fft_z_conv(g, r->plan, prec, r->spec0, sp0, f1, 1, 0.5 * g.renor, r->spec1, r->s));
   }
   bool inv = false;
   if (xy) {
@@ -1391,6 +1391,24 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
     sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y, ENGINE_Y);
     sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z, ENGINE_Z);
     sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r, ENGINE_C2R);
+  } else {
+    // the fused z convolution against the split passes, on an evaluation's
+    // two z convolutions (two products, then one product plus a spectrum)
+    void* zo2[2] = {r->spec0, r->spec1};
+    const void* zf2[2] = {r->wcgk, r->fvlj4};
+    const void* zf1[1] = {r->wcgk};
+    float ms[2] = {0.f, 0.f};
+    for (int split = 0; split < 2; ++split) {
+      trial = best;
+      trial.engine = split ? (trial.engine | ENGINE_ZSPLIT) : (trial.engine & ~ENGINE_ZSPLIT);
+      r->plan.tiles = trial;
+      fft_prepare(prec, r->plan);
+      ms[split] = per_launch_ms(r, a, b, reps, [&] {
+        fft_z_conv(g, r->plan, prec, r->spec0, zo2, zf2, 2, 0.5 * g.renor, nullptr, r->s);
+        fft_z_conv(g, r->plan, prec, r->spec0, sp, zf1, 1, 0.5 * g.renor, r->spec1, r->s);
+      });
+    }
+    best.engine = ms[1] < ms[0] ? (best.engine | ENGINE_ZSPLIT) : (best.engine & ~ENGINE_ZSPLIT);
   }
   // The fused plane kernels against the passes they replace, timed over an
   // evaluation's line passes with the tiles chosen above. dencg and pot4 go

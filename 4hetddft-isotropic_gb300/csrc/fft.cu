@@ -443,14 +443,18 @@ void fft_y(const Grid& g, const FftPlan& p, int prec, void* const* specs, int ns
   else
     y_impl<float>(g, p, specs, nspec, sign, s);
 }
-void fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* const* outs,
-                const void* const* factors, int nout, double scale, const void* add, cudaStream_t s) {
-  if (prec == HE4G_PREC_FP64)
+int fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* const* outs,
+               const void* const* factors, int nout, double scale, const void* add, cudaStream_t s) {
+  if (prec == HE4G_PREC_FP64) {
     zconv_impl<double>(g, p, in, outs, factors, nout, scale, add, s);
-  else if (prec == HE4G_PREC_DF64)
+    return 1;
+  }
+  if (prec == HE4G_PREC_DF64) {
     reg_z<df64>(g, p, in, outs, factors, nout, scale, add, s);
-  else
-    zconv_impl<float>(g, p, in, outs, factors, nout, scale, add, s);
+    return (p.tiles.engine & ENGINE_ZSPLIT) ? 1 + nout : 1;
+  }
+  zconv_impl<float>(g, p, in, outs, factors, nout, scale, add, s);
+  return 1;
 }
 void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins, void* const* outs, int nspec,
                cudaStream_t s) {
@@ -555,6 +559,7 @@ int fft_reg_engines(int prec, const FftPlan& p) {
   if (fft_reg_supported(p.y.n)) e |= ENGINE_Y;
   if (fft_reg_supported(p.z.n)) e |= ENGINE_Z;
   if (prec == HE4G_PREC_MIXED && fft_xy_supported(p.xh.n, p.y.n)) e |= ENGINE_XY;
+  if (prec == HE4G_PREC_DF64) e |= ENGINE_ZSPLIT;
   return e;
 }
 
@@ -571,8 +576,11 @@ FftTiles fft_default_tiles(int prec, const FftPlan& p) {
   while (t.lpb_c2r > 1 && !fft_smem_bytes(prec, PASS_C2R, p, t.lpb_c2r)) t.lpb_c2r >>= 1;
   while (t.ltx_y > 0 && !fft_smem_bytes(prec, PASS_Y, p, t.ltx_y)) --t.ltx_y;
   while (t.ltx_z > 0 && !fft_smem_bytes(prec, PASS_Z, p, t.ltx_z)) --t.ltx_z;
-  // the fused plane kernels are the autotuner's choice, not a default
-  t.engine = fft_reg_engines(prec, p) & ~ENGINE_XY;
+  // the fused plane kernels are the autotuner's choice, not a default; the
+  // split z convolution of df64 is the default from nz = 192 on (at nz = 256
+  // the fused kernel's two 64 KB line buffers leave one block per SM)
+  t.engine = fft_reg_engines(prec, p) & ~(ENGINE_XY | ENGINE_ZSPLIT);
+  if (prec == HE4G_PREC_DF64 && p.z.n >= 192) t.engine |= ENGINE_ZSPLIT;
   return t;
 }
 

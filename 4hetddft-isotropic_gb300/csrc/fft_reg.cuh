@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(kRegThreads) k_y_reg(Grid g, FftAxis ax, SpecL
 // in a second shared buffer (each thread rereads only its own slots), so
 // that registers hold one line segment at a time.
 template <typename R, int P, int Q>
-__global__ void __launch_bounds__(kRegThreads, sizeof(R) == 8 ? 1 : 2)
+__global__ void __launch_bounds__(kRegThreads, std::is_same<R, double>::value ? 1 : 2)
     k_z_conv_reg(Grid g, FftAxis ax, const C2<R>* in, FactorList<R> fl, int nout, R scale,
                  const C2<R>* __restrict__ add) {
   constexpr int N = P * Q;
@@ -175,6 +175,69 @@ __global__ void __launch_bounds__(kRegThreads, sizeof(R) == 8 ? 1 : 2)
         if (addo) r = cadd<R>(r, addo[e]);
         dst[e] = r;
       }
+    }
+  }
+}
+
+// ------------------------------------------- split z convolution (df64)
+// One z transform of L kx columns of one y row per block, out of place or in
+// place: out = Z(in * fac * scale) (+ add), where fac (nullable) multiplies
+// the input in the (kx, ky, kz) layout of the spectrum and add (nullable) is
+// added to the output. The df64 form runs its z convolutions as a forward
+// pass and one product-and-inverse pass per output: the fused kernel above
+// keeps the forward spectrum in a second shared buffer, which in df64 (16 B
+// per complex value, and twice the registers of the FP32 lines) leaves one
+// block per SM, while these passes run two, like the y pass.
+template <typename R, int P, int Q, int SIGN>
+__global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, const C2<R>* in, C2<R>* out,
+                                                          const Fld<R>* __restrict__ fac, R scale,
+                                                          const C2<R>* __restrict__ add) {
+  constexpr int N = P * Q;
+  constexpr int L = reg_lines<P, Q>();
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
+  C2<R>* tws = buf + N * L;
+  const int kx0 = blockIdx.x * L;
+  const int ncol = min(L, g.nxh - kx0);
+  const long long base = (long long)blockIdx.y * g.nxh + kx0;
+  const long long stride = (long long)g.ny * g.nxh;
+  const int tid = threadIdx.x;
+  const int c1 = tid % L, u = tid / L;
+  const bool act1 = u < Q && c1 < ncol;
+  C2<R> v[P];
+  if (act1) {
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      const long long e = base + (Q * p + u) * stride + c1;
+      v[p] = in[e];
+      if (fac) {
+        const R f = ldf<R>(&fac[e]) * scale;
+        v[p] = mk<R>(v[p].x * f, v[p].y * f);
+      }
+    }
+  }
+  stage_tw<R>(tws, twiddles<R>(ax), N);
+  __syncthreads();
+  if (act1) {
+    RegDft<R, P, SIGN>::run(v);
+#pragma unroll
+    for (int k = 1; k < P; ++k) v[k] = mulw<R, SIGN>(v[k], tws[u * k]);
+#pragma unroll
+    for (int k = 0; k < P; ++k) buf[(k * Q + u) * L + c1] = v[k];
+  }
+  __syncthreads();
+  const int c2 = tid % L, kp = tid / L;
+  if (kp < P && c2 < ncol) {
+    C2<R> w[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) w[q] = buf[(kp * Q + q) * L + c2];
+    RegDft<R, Q, SIGN>::run(w);
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+      const long long e = base + (kp + P * j) * stride + c2;
+      C2<R> r = w[j];
+      if (add) r = cadd<R>(r, add[e]);
+      out[e] = r;
     }
   }
 }
@@ -499,6 +562,31 @@ void run_z(const Grid& g, const FftPlan& p, const C2<R>* in, const FactorList<R>
   k_z_conv_reg<R, P, Q><<<grid, kRegThreads, smem, s>>>(g, p.z, in, fl, nout, scale, add);
 }
 
+// The split z convolution: the forward pass transforms `in` in place, then
+// each output gets its product-and-inverse pass; an output that aliases the
+// input goes last, so that every product reads the forward spectrum.
+template <typename R, int P, int Q>
+void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>& fl, int nout, R scale,
+                 const C2<R>* add, cudaStream_t s, bool launch) {
+  constexpr int L = reg_lines<P, Q>();
+  const size_t smem = sizeof(C2<R>) * (P * Q * L + P * Q);
+  set_smem(k_zcol_reg<R, P, Q, -1>, smem);
+  set_smem(k_zcol_reg<R, P, Q, 1>, smem);
+  if (!launch) return;
+  dim3 grid((g.nxh + L - 1) / L, g.ny);
+  k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, in, nullptr, scale, nullptr);
+  int order[3], n = 0;
+  for (int o = 0; o < nout; ++o)
+    if (fl.out[o] != in) order[n++] = o;
+  for (int o = 0; o < nout; ++o)
+    if (fl.out[o] == in) order[n++] = o;
+  for (int i = 0; i < nout; ++i) {
+    const int o = order[i];
+    k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, fl.out[o], fl.f[o], scale,
+                                                            o == 0 ? add : nullptr);
+  }
+}
+
 template <typename R, int P, int Q, int PRO>
 void run_r2c(const Grid& g, const FftPlan& p, const C2<R>* twx, const Fld<R>* a, const Fld<R>* b, R c0, R c1,
              C2<R>* out, cudaStream_t s, bool launch) {
@@ -584,10 +672,20 @@ bool reg_z(const Grid& g, const FftPlan& p, const void* in, void* const* outs, c
   }
   const C2<R>* ip = static_cast<const C2<R>*>(in);
   const C2<R>* ap = static_cast<const C2<R>*>(add);
+  // df64: the split passes when ENGINE_ZSPLIT is set (launch == false
+  // prepares both forms)
+  constexpr bool df = std::is_same<R, df64>::value;
+  const bool split = df && (p.tiles.engine & ENGINE_ZSPLIT);
   switch (p.z.n) {
-#define HE4G_CASE(N, P, Q)                                      \
-  case N:                                                       \
-    run_z<R, P, Q>(g, p, ip, fl, nout, (R)scale, ap, s, launch); \
+#define HE4G_CASE(N, P, Q)                                                                           \
+  case N:                                                                                            \
+    if constexpr (df) {                                                                              \
+      if (split || !launch)                                                                          \
+        run_z_split<R, P, Q>(g, p, const_cast<C2<R>*>(ip), fl, nout, (R)scale, ap, s, launch);       \
+      if (!split || !launch) run_z<R, P, Q>(g, p, ip, fl, nout, (R)scale, ap, s, launch);            \
+    } else {                                                                                         \
+      run_z<R, P, Q>(g, p, ip, fl, nout, (R)scale, ap, s, launch);                                   \
+    }                                                                                                \
     return true;
     HE4G_REG_SIZES(HE4G_CASE)
 #undef HE4G_CASE

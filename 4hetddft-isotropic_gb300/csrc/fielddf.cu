@@ -297,8 +297,10 @@ __global__ void __launch_bounds__(256) k_potenimp_df(Grid g, ImpTableD tab, ImpS
 
 // derden (derden.f90:26-28) fused with uimp (stored when uimp_out is set) and
 // the force sums of forceimp (potenimp.f90:44-46). Each thread walks kZD z
-// planes of one (x, y) column with the z neighbours in a register window;
-// its df64 sums become FP64 before the block reduction.
+// planes of one (x, y) column with the z neighbours in a register window
+// that shifts by one plane per step (the plane loop stays rolled, which keeps
+// the kernel's code small enough for the instruction cache); its df64 sums
+// become FP64 before the block reduction.
 __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df64* __restrict__ den,
                                                    ImpTableD tab, ImpState* imp, int sel, df64* uimp_out,
                                                    double* partials, ForceFinish fin) {
@@ -313,8 +315,8 @@ __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df6
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
     const long long col = (long long)j * g.nx + i;
     const df64 zero(0.f, 0.f);
-    constexpr int W = kZD + 2 * kStencilHalf;
-    df64 wz[W];  // den at planes k0-6 .. k0+kZD+5 of this column
+    constexpr int W = 2 * kStencilHalf + 1;
+    df64 wz[W];  // den at planes k-6 .. k+6 of this column, k the current plane
 #pragma unroll
     for (int m = 0; m < W; ++m) {
       const int k = k0 - kStencilHalf + m;
@@ -322,7 +324,7 @@ __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df6
     }
     const df64 xi = __ldg(tab.xs + i), yj = __ldg(tab.ys + j);
     df64 s[3] = {zero, zero, zero};
-#pragma unroll
+#pragma unroll 1
     for (int m = 0; m < kZD; ++m) {
       const int k = k0 + m;
       if (k < g.nz) {
@@ -336,7 +338,7 @@ __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df6
           a = j - o >= 0 ? __ldg(den + p - o * sy) : zero;
           b = j + o < g.ny ? __ldg(den + p + o * sy) : zero;
           gy = fma(st.d1[1][o], b - a, gy);
-          gz = fma(st.d1[2][o], wz[m + kStencilHalf + o] - wz[m + kStencilHalf - o], gz);
+          gz = fma(st.d1[2][o], wz[kStencilHalf + o] - wz[kStencilHalf - o], gz);
         }
         const df64 u = uimp_at(xi, yj, __ldg(tab.zs + k), c, tab, bad);
         if (uimp_out) sts(uimp_out + p, u);
@@ -344,6 +346,11 @@ __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df6
         s[1] = fma(gy, u, s[1]);
         s[2] = fma(gz, u, s[2]);
       }
+      // shift the window: wz[q] becomes plane k - 5 + q
+#pragma unroll
+      for (int q = 0; q < W - 1; ++q) wz[q] = wz[q + 1];
+      const int kn = k0 - kStencilHalf + m + W;
+      wz[W - 1] = (kn >= 0 && kn < g.nz) ? __ldg(den + col + kn * sz) : zero;
     }
     for (int a = 0; a < 3; ++a) v[a] = df_to_double(s[a]);
   }

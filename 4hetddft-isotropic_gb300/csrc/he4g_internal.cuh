@@ -112,8 +112,10 @@ int launch_finish_force(const double* partials, int nblocks, const ForceFinish& 
 // block, and which passes run on the register engine (ENGINE_* bits; only
 // lengths with a specialisation, see fft_reg_supported). ENGINE_XY fuses the
 // y pass with the neighbouring x passes per z plane (fft_xy.cu; mixed form,
-// planes with a specialisation, see fft_xy_supported).
-enum { ENGINE_R2C = 1, ENGINE_C2R = 2, ENGINE_Y = 4, ENGINE_Z = 8, ENGINE_XY = 16 };
+// planes with a specialisation, see fft_xy_supported). ENGINE_ZSPLIT (df64
+// form) runs the z convolution as a forward pass and one product-and-inverse
+// pass per output instead of one fused kernel.
+enum { ENGINE_R2C = 1, ENGINE_C2R = 2, ENGINE_Y = 4, ENGINE_Z = 8, ENGINE_XY = 16, ENGINE_ZSPLIT = 32 };
 struct FftTiles {
   int lpb_r2c, lpb_c2r;
   int ltx_y, ltx_z;
@@ -170,9 +172,12 @@ void fft_x_r2c_prod(const Grid& g, const FftPlan& p, int prec, const void* a, co
                     cudaStream_t s);
 void fft_y(const Grid& g, const FftPlan& p, int prec, void* const* specs, int nspec, int sign, cudaStream_t s);
 // forward z, multiply by nout tables (each scaled by `scale`), inverse z;
-// `add` (nullable) is added to output 0
-void fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* const* outs,
-                const void* const* factors, int nout, double scale, const void* add, cudaStream_t s);
+// `add` (nullable) is added to output 0. Returns the kernels launched: one
+// fused kernel, or in the df64 form a forward pass that transforms `in` in
+// place (it is overwritten even when no output aliases it) and one
+// product-and-inverse pass per output.
+int fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* const* outs,
+               const void* const* factors, int nout, double scale, const void* add, cudaStream_t s);
 void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins, void* const* outs, int nspec,
                cudaStream_t s);
 // c2r of the coarse-grained density spectrum (stored to dencg) fused with the

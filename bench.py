@@ -297,6 +297,13 @@ def case_grid(case):
     return list(n) if not isinstance(n, int) else [n, n, n]
 
 
+def l2_note(cfg):
+    n = cfg.nx * cfg.ny * cfg.nz
+    return (f"inputs larger than L2 (psi {16 * n / 1e6:.0f} MB, history {7 * 16 * n / 1e9:.2f} GB); no flush"
+            if 16 * n > 129e6 else
+            f"psi {16 * n / 1e6:.0f} MB, history {7 * 16 * n / 1e6:.0f} MB: the step's working set exceeds L2; no flush")
+
+
 def metric_name(case, prec=FP64):
     """The headline metric for the 256^3 collision; the same wording with the
     grid and system of any other workload."""
@@ -443,7 +450,7 @@ def ours(args):
             "config": {"workload": f"{CASE} {FORM_NAME[prec]} predictor-corrector step",
                        "grid": [cfg.nx, cfg.ny, cfg.nz], "h": meta["h"], "n4": meta["n4"], "impurity": meta["imp"],
                        "v_A_per_ps": meta["v"], "impact_parameter": f"{meta['b_frac']} R",
-                       "l2": "inputs larger than L2 (psi 268 MB, history 1.9 GB); no flush",
+                       "l2": l2_note(cfg),
                        "parallelism": f"replicas x{ws}", "fft_tiles": list(run.tiles)},
             "grid_point_updates_per_s": value * cfg.nx * cfg.ny * cfg.nz,
             "hbm_gbs": rf["step_gbs"],
@@ -473,11 +480,11 @@ def ours(args):
 DTYPE = {
     FP64: "f64",
     MIXED: "mixed (f32 fields, f64 accumulators)",
-    DF64: "df64 (FFT convolutions in paired f32, 48-bit significands; f64 fields, stencils, updates, reductions)",
+    DF64: "df64 (paired f32, 48-bit significands: fields, stencils, updates, FFTs, uimp, force; f64 block sums, impurity)",
 }
 FORM_DTYPE = {
     MIXED: "f32 fields/stencils/FFTs; f64 psi accumulator, reductions, force sum, trajectory",
-    DF64: "df64 FFT convolutions (paired f32); f64 fields, stencils, predictor-corrector, reductions, trajectory",
+    DF64: "df64 (paired f32) fields, stencils, updates, FFT convolutions, uimp, force; f64 block sums, trajectory",
 }
 
 

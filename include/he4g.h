@@ -236,12 +236,15 @@ int he4g_step_many(he4g_run** runs, int n, int nsteps);
  * only for lengths it is specialised for: 16, 20, 24, 32, 40, 48, 64, 80, 96,
  * 128, 160, 192, 256); bit 16 fuses the y passes with the x passes per z
  * plane on thread-block clusters (mixed precision, nx/2 x ny planes
- * 128 x 256 and 64 x 128). No reference counterpart (FFTW picks its own
- * plans in fft.f90:5-153).
+ * 128 x 256 and 64 x 128); bit 32 (HE4G_PREC_DF64, which runs every pass on
+ * the register engine) splits each z convolution into a forward pass and one
+ * product-and-inverse pass per output. No reference counterpart (FFTW picks
+ * its own plans in fft.f90:5-153).
  *
  * he4g_autotune times, for each pass, every generic shape that fits in
  * shared memory and the register engine, then the fused plane kernels
- * against the passes they replace, on this run's own buffers (reps timed
+ * against the passes they replace (df64: the fused z convolution against
+ * the split one), on this run's own buffers (reps timed
  * launches each, 0 = 5), and keeps the fastest; tiles (nullable)
  * receives the choice. Generic shapes change timing only (every line goes
  * through the same arithmetic); the two engines agree to rounding. It

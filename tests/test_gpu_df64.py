@@ -121,3 +121,23 @@ def test_lengths_without_a_register_pass_are_refused():
     with pytest.raises(he4gpu.He4gError) as err:
         he4gpu.Run(cfg)
     assert err.value.code == he4gpu.abi.HE4G_EINVAL
+
+
+def test_split_and_fused_z_convolutions_agree():
+    """The z convolution as one fused kernel or as a forward pass plus one
+    product-and-inverse pass per output (tiles bit 32): the same products,
+    the inverse factored in the other order, so equal to rounding."""
+    cfg, tk, psi, r, v, meta = make_case("he200_xe_40x48x64", precision=DF64)
+    runs = []
+    for split in (0, 32):
+        x = gpu_run(cfg, tk, psi, r, v)
+        t = list(x.tiles)
+        t[4] = 15 | split
+        x.tiles = tuple(t)
+        x.step(8)
+        runs.append(x)
+    a, b = runs
+    assert rel_field(a.psi, b.psi) < 1e-12
+    assert rel_vec(a.impurity()[0], b.impurity()[0]) < 1e-13
+    a.close()
+    b.close()
