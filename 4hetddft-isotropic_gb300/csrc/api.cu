@@ -1039,7 +1039,7 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
       chk(*p = dalloc_bytes(r, rs * n));
   }
   r->pblocks = pc_blocks(g);
-  r->fblocks = r->prec == HE4G_PREC_MIXED ? force_blocks_mp(g) : force_blocks(g);
+  r->fblocks = mixed(r) ? force_blocks_mp(g) : dfm(r) ? force_blocks_df(g) : force_blocks(g);
   chk(r->partials = dalloc<double>(r, (size_t)r->pblocks * 12));
   chk(r->counters = dalloc<unsigned>(r, kFinishCounters, true));
   chk(r->small = dalloc<double>(r, 64));

@@ -29,7 +29,12 @@ namespace he4g {
 namespace {
 
 constexpr int kBX = 64, kBY = 4;  // point-kernel blocks (256 threads)
-constexpr int kZD = 8;            // z planes per thread of the force kernel
+// z planes per thread of the force kernel: 16 where that still leaves four
+// waves of blocks (256^3), else 8
+int force_planes(const Grid& g) {
+  const long long cols = (long long)((g.nx + kBX - 1) / kBX) * ((g.ny + kBY - 1) / kBY);
+  return cols * ((g.nz + 15) / 16) >= 4 * 152 * 3 ? 16 : 8;
+}
 
 struct Pt {
   int i, j, k;
@@ -75,29 +80,60 @@ __device__ __forceinline__ int nonfinite(df64 d) {
 // |z|^2
 __device__ __forceinline__ df64 norm2(df2 z) { return fma(z.x, z.x, z.y * z.y); }
 
+// Stencil sums: sum_k c_k (a_k +- b_k) in an unnormalised accumulator. Each
+// term's pair goes through TwoSum on the high parts (low parts and the
+// TwoSum error in FP32), its product with the df64 coefficient keeps the
+// exact error of the high product, and the accumulator's high part goes
+// through TwoSum while every error term collects in its low part; one
+// Fast2Sum at the end normalises. 20 FP32 instructions a term against 23 for
+// a df64 add followed by a df64 multiply-add, with the same 2^-48 bound
+// relative to the terms (Ogita, Rump and Oishi's Dot2 scheme, SIAM J. Sci.
+// Comput. 26 (2005) 1955-1988, with df64 operands).
+struct Acc {
+  float hi, lo;
+};
+template <int SGN>  // +1: c*(a + b); -1: c*(b - a)
+__device__ __forceinline__ void acc_pair(Acc& acc, df64 c, df64 a, df64 b) {
+  const float ah = SGN > 0 ? a.hi : -a.hi, al = SGN > 0 ? a.lo : -a.lo;
+  const float sh = b.hi + ah;
+  const float v = sh - b.hi;
+  const float t = ((b.hi - (sh - v)) + (ah - v)) + (b.lo + al);
+  const float p = c.hi * sh;
+  float ep = fmaf(c.hi, sh, -p);
+  ep = fmaf(c.hi, t, ep);
+  ep = fmaf(c.lo, sh, ep);
+  const float h = acc.hi + p;
+  const float w = h - acc.hi;
+  const float e2 = (acc.hi - (h - w)) + (p - w);
+  acc.hi = h;
+  acc.lo += e2 + ep;
+}
+__device__ __forceinline__ Acc acc_of(df64 x) { return Acc{x.hi, x.lo}; }
+__device__ __forceinline__ df64 acc_value(Acc a) { return df_fast2sum(a.hi, a.lo); }
+
 // (d2x + d2y + d2z) psi at a point, zero padded (Deriv3D_pc, id = 2):
 // symmetric pairs summed before the coefficient product
 __device__ __forceinline__ df2 lap13(const df2* __restrict__ f, const Pt& t, const Grid& g, const StencilD& st) {
   const df2 c = __ldg(f + t.p);
-  df64 ar = st.d2c * c.x, ai = st.d2c * c.y;
+  Acc ar = acc_of(st.d2c * c.x), ai = acc_of(st.d2c * c.y);
   const long long sy = g.nx, sz = (long long)g.nx * g.ny;
   const df2 zero{df64(0.f, 0.f), df64(0.f, 0.f)};
 #pragma unroll
   for (int o = 1; o <= kStencilHalf; ++o) {
     df2 a = t.i - o >= 0 ? __ldg(f + t.p - o) : zero;
     df2 b = t.i + o < g.nx ? __ldg(f + t.p + o) : zero;
-    ar = fma(st.d2[0][o], a.x + b.x, ar);
-    ai = fma(st.d2[0][o], a.y + b.y, ai);
+    acc_pair<1>(ar, st.d2[0][o], a.x, b.x);
+    acc_pair<1>(ai, st.d2[0][o], a.y, b.y);
     a = t.j - o >= 0 ? __ldg(f + t.p - o * sy) : zero;
     b = t.j + o < g.ny ? __ldg(f + t.p + o * sy) : zero;
-    ar = fma(st.d2[1][o], a.x + b.x, ar);
-    ai = fma(st.d2[1][o], a.y + b.y, ai);
+    acc_pair<1>(ar, st.d2[1][o], a.x, b.x);
+    acc_pair<1>(ai, st.d2[1][o], a.y, b.y);
     a = t.k - o >= 0 ? __ldg(f + t.p - o * sz) : zero;
     b = t.k + o < g.nz ? __ldg(f + t.p + o * sz) : zero;
-    ar = fma(st.d2[2][o], a.x + b.x, ar);
-    ai = fma(st.d2[2][o], a.y + b.y, ai);
+    acc_pair<1>(ar, st.d2[2][o], a.x, b.x);
+    acc_pair<1>(ai, st.d2[2][o], a.y, b.y);
   }
-  return df2{ar, ai};
+  return df2{acc_value(ar), acc_value(ai)};
 }
 
 // Sto4c = timec*(lap*h2o2m4 - pot4*psi) - i*uimp*psi (steppc.f90:55,123;
@@ -111,27 +147,29 @@ __device__ __forceinline__ df2 hpsi(df2 lap, df2 ps, df64 pot, df64 u, float T, 
   return df2{fma(u, ps.y, br), fma(-u, ps.x, bi)};
 }
 
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double* partials) {
-  __shared__ double sh[NV][kRedBlock / 32];
+// Block sums of three df64 values: df64 shuffle trees inside each warp (FP32
+// instructions), FP64 across the warps, one row of partials per block
+__device__ __forceinline__ void block_sum_df3(const df64 (&v)[3], double* partials) {
+  __shared__ double sh[3][kRedBlock / 32];
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   const int lane = tid & 31, wid = tid >> 5;
 #pragma unroll
-  for (int a = 0; a < NV; ++a) {
-    double x = v[a];
+  for (int a = 0; a < 3; ++a) {
+    df64 x = v[a];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[a][wid] = x;
+    for (int o = 16; o > 0; o >>= 1)
+      x = x + df64(__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o));
+    if (lane == 0) sh[a][wid] = df_to_double(x);
   }
   __syncthreads();
   if (tid < 32) {
     const int nw = (blockDim.x * blockDim.y) >> 5;
 #pragma unroll
-    for (int a = 0; a < NV; ++a) {
+    for (int a = 0; a < 3; ++a) {
       double x = lane < nw ? sh[a][lane] : 0.0;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if (lane == 0) partials[(long long)block_linear() * NV + a] = x;
+      if (lane == 0) partials[(long long)block_linear() * 3 + a] = x;
     }
   }
 }
@@ -296,25 +334,25 @@ __global__ void __launch_bounds__(256) k_potenimp_df(Grid g, ImpTableD tab, ImpS
 }
 
 // derden (derden.f90:26-28) fused with uimp (stored when uimp_out is set) and
-// the force sums of forceimp (potenimp.f90:44-46). Each thread walks kZD z
+// the force sums of forceimp (potenimp.f90:44-46). Each thread walks zd z
 // planes of one (x, y) column with the z neighbours in a register window
 // that shifts by one plane per step (the plane loop stays rolled, which keeps
 // the kernel's code small enough for the instruction cache); its df64 sums
 // become FP64 before the block reduction.
 __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df64* __restrict__ den,
                                                    ImpTableD tab, ImpState* imp, int sel, df64* uimp_out,
-                                                   double* partials, ForceFinish fin) {
+                                                   double* partials, ForceFinish fin, int zd) {
   const int i = blockIdx.x * kBX + threadIdx.x;
   const int j = blockIdx.y * kBY + threadIdx.y;
-  const int k0 = blockIdx.z * kZD;
+  const int k0 = blockIdx.z * zd;
   df64 c[3];
   centre_of(imp, sel, c);
-  double v[3] = {0.0, 0.0, 0.0};
+  const df64 zero(0.f, 0.f);
+  df64 s[3] = {zero, zero, zero};
   int bad = 0;
   if (i < g.nx && j < g.ny) {
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
     const long long col = (long long)j * g.nx + i;
-    const df64 zero(0.f, 0.f);
     constexpr int W = 2 * kStencilHalf + 1;
     df64 wz[W];  // den at planes k-6 .. k+6 of this column, k the current plane
 #pragma unroll
@@ -323,23 +361,23 @@ __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df6
       wz[m] = (k >= 0 && k < g.nz) ? __ldg(den + col + k * sz) : zero;
     }
     const df64 xi = __ldg(tab.xs + i), yj = __ldg(tab.ys + j);
-    df64 s[3] = {zero, zero, zero};
 #pragma unroll 1
-    for (int m = 0; m < kZD; ++m) {
+    for (int m = 0; m < zd; ++m) {
       const int k = k0 + m;
       if (k < g.nz) {
         const long long p = col + k * sz;
-        df64 gx = zero, gy = zero, gz = zero;
+        Acc ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f};
 #pragma unroll
         for (int o = 1; o <= kStencilHalf; ++o) {
           df64 a = i - o >= 0 ? __ldg(den + p - o) : zero;
           df64 b = i + o < g.nx ? __ldg(den + p + o) : zero;
-          gx = fma(st.d1[0][o], b - a, gx);
+          acc_pair<-1>(ax, st.d1[0][o], a, b);
           a = j - o >= 0 ? __ldg(den + p - o * sy) : zero;
           b = j + o < g.ny ? __ldg(den + p + o * sy) : zero;
-          gy = fma(st.d1[1][o], b - a, gy);
-          gz = fma(st.d1[2][o], wz[kStencilHalf + o] - wz[kStencilHalf - o], gz);
+          acc_pair<-1>(ay, st.d1[1][o], a, b);
+          acc_pair<-1>(az, st.d1[2][o], wz[kStencilHalf - o], wz[kStencilHalf + o]);
         }
+        const df64 gx = acc_value(ax), gy = acc_value(ay), gz = acc_value(az);
         const df64 u = uimp_at(xi, yj, __ldg(tab.zs + k), c, tab, bad);
         if (uimp_out) sts(uimp_out + p, u);
         s[0] = fma(gx, u, s[0]);
@@ -352,7 +390,6 @@ __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df6
       const int kn = k0 - kStencilHalf + m + W;
       wz[W - 1] = (kn >= 0 && kn < g.nz) ? __ldg(den + col + kn * sz) : zero;
     }
-    for (int a = 0; a < 3; ++a) v[a] = df_to_double(s[a]);
   }
   if (bad) atomicOr(&imp->health, 4);
   if (sel == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -361,7 +398,7 @@ __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df6
     imp->center[1] = imp->rimp[1];
     imp->center[2] = imp->rimp[2];
   }
-  block_sum<3>(v, partials);
+  block_sum_df3(s, partials);
   if (threadIdx.y * blockDim.x + threadIdx.x >= 32) return;  // warp 0 finishes (when fin.cnt is set)
   double tot[3];
   const int nb = gridDim.x * gridDim.y * gridDim.z;
@@ -388,7 +425,8 @@ unsigned conv_blocks(long long n) {
 }  // namespace
 
 int force_blocks_df(const Grid& g) {
-  return ((g.nx + kBX - 1) / kBX) * ((g.ny + kBY - 1) / kBY) * ((g.nz + kZD - 1) / kZD);
+  const int zd = force_planes(g);
+  return ((g.nx + kBX - 1) / kBX) * ((g.ny + kBY - 1) / kBY) * ((g.nz + zd - 1) / zd);
 }
 
 void launch_pc_predict_df(const Grid& g, const StencilD& st, df64 h2o2m4, const df2* psi, df2* p3_out,
@@ -421,11 +459,12 @@ void launch_rk_stage_df(const Grid& g, const StencilD& st, df64 h2o2m4, const df
 
 int launch_force_df(const Grid& g, const StencilD& st, const df64* den, const ImpTableD& tab, ImpState* imp,
                     int sel, df64* uimp_out, double* partials, const ForceFinish& fin, cudaStream_t s) {
-  dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + kZD - 1) / kZD);
+  const int zd = force_planes(g);
+  dim3 grid((g.nx + kBX - 1) / kBX, (g.ny + kBY - 1) / kBY, (g.nz + zd - 1) / zd);
   const int nb = (int)(grid.x * grid.y * grid.z);
   ForceFinish f = fin;
   if (nb > kFinishInKernelMax) f.cnt = nullptr;
-  k_force_df<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, tab, imp, sel, uimp_out, partials, f);
+  k_force_df<<<grid, dim3(kBX, kBY), 0, s>>>(g, st, den, tab, imp, sel, uimp_out, partials, f, zd);
   return 1 + (f.cnt ? 0 : launch_finish_force(partials, nb, fin, s));
 }
 
