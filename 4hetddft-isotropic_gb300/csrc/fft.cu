@@ -474,7 +474,8 @@ void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv,
   if (prec == HE4G_PREC_FP64) {
     pot4_impl<double>(g, p, conv, dencg, den, fn, pot4, s);
   } else if (prec == HE4G_PREC_DF64) {
-    const Pot4Args<df64> pa{static_cast<const df64*>(dencg), static_cast<const df64*>(den), fn};
+    const Pot4Args<df64> pa{static_cast<const df64*>(dencg), static_cast<const df64*>(den), fn,
+                            {df64(fn.a0), df64(fn.a1), df64(fn.beta_solid), df64(fn.den_m), df64(fn.c_solid)}};
     const df2* c = static_cast<const df2*>(conv);
     df64* o = static_cast<df64*>(pot4);
     reg_c2r<df64>(g, p, twxd(p), EPI_POT4, c, c, o, o, 1, pa, s);

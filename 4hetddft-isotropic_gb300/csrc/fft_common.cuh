@@ -259,6 +259,30 @@ __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
+// Asynchronous global -> shared copies of 16 or 8 bytes (both addresses
+// aligned to the size). The data travels without registers, so a thread
+// keeps every copy of its tile in flight at once; cp_async_wait_all()
+// commits the thread's copies and waits until they have landed (visible to
+// the thread itself; a block barrier after it makes them visible to all).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+// Closes the thread's current group of copies; cp_async_wait<N>() waits until
+// at most N of its closed groups are still in flight (the oldest land first).
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // Loads of real fields into the arithmetic type: one value (ldf), an
 // aligned pair of x-adjacent values (ld_pair); st_pair stores a pair.
 template <typename R>
@@ -527,6 +551,10 @@ struct Pot4Args {
   const Fld<R>* dencg;
   const Fld<R>* den;
   Functional fn;
+  // df64 only: a0, a1, beta_solid, den_m, c_solid split into df64 on the
+  // host (the device split of a double issues conversions on the FP64 pipe);
+  // the other forms convert fn's doubles in the kernel
+  R k[5];
 };
 
 template <typename R>

@@ -188,15 +188,30 @@ __global__ void __launch_bounds__(kRegThreads, std::is_same<R, double>::value ? 
 // keeps the forward spectrum in a second shared buffer, which in df64 (16 B
 // per complex value, and twice the registers of the FP32 lines) leaves one
 // block per SM, while these passes run two, like the y pass.
+//
+// The column tile (and the factor tile) reach shared memory by asynchronous
+// copies: each thread copies exactly the slots it reads back, so the copies
+// need no barrier, and all of a thread's P (or 2P) loads are in flight at
+// once without holding registers; the rows of `add` are prefetched into L2
+// at the start. Shared memory: the tile [N][L], the N twiddles and, for a
+// product pass, the factor tile [N][L] (zcol_smem).
+template <typename R, int P, int Q>
+__host__ __device__ constexpr size_t zcol_smem(bool with_factor) {
+  return sizeof(C2<R>) * (P * Q * reg_lines<P, Q>() + P * Q) +
+         (with_factor ? sizeof(Fld<R>) * P * Q * reg_lines<P, Q>() : 0);
+}
+
 template <typename R, int P, int Q, int SIGN>
 __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, const C2<R>* in, C2<R>* out,
                                                           const Fld<R>* __restrict__ fac, R scale,
                                                           const C2<R>* __restrict__ add) {
+  static_assert(sizeof(C2<R>) == 16 && sizeof(Fld<R>) == 8, "asynchronous copies of 16-byte values, 8-byte factors");
   constexpr int N = P * Q;
   constexpr int L = reg_lines<P, Q>();
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
   C2<R>* tws = buf + N * L;
+  Fld<R>* fs = reinterpret_cast<Fld<R>*>(tws + N);  // factor tile, product passes only
   const int kx0 = blockIdx.x * L;
   const int ncol = min(L, g.nxh - kx0);
   const long long base = (long long)blockIdx.y * g.nxh + kx0;
@@ -204,19 +219,29 @@ __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, co
   const int tid = threadIdx.x;
   const int c1 = tid % L, u = tid / L;
   const bool act1 = u < Q && c1 < ncol;
-  C2<R> v[P];
   if (act1) {
 #pragma unroll
     for (int p = 0; p < P; ++p) {
       const long long e = base + (Q * p + u) * stride + c1;
-      v[p] = in[e];
+      cp_async16(&buf[(Q * p + u) * L + c1], &in[e]);
+      if (fac) cp_async8(&fs[(Q * p + u) * L + c1], &fac[e]);
+    }
+  }
+  if (add && tid < N && ncol > 0)  // row tid of the added tile: ncol values, 16-byte aligned
+    prefetch_l2(&add[base + (long long)tid * stride], (unsigned)(ncol * sizeof(C2<R>)));
+  stage_tw<R>(tws, twiddles<R>(ax), N);
+  cp_async_wait_all();
+  C2<R> v[P];
+  if (act1) {
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      v[p] = buf[(Q * p + u) * L + c1];
       if (fac) {
-        const R f = ldf<R>(&fac[e]) * scale;
+        const R f = fs[(Q * p + u) * L + c1] * scale;
         v[p] = mk<R>(v[p].x * f, v[p].y * f);
       }
     }
   }
-  stage_tw<R>(tws, twiddles<R>(ax), N);
   __syncthreads();
   if (act1) {
     RegDft<R, P, SIGN>::run(v);
@@ -252,6 +277,22 @@ __device__ __forceinline__ int xpad(int i) {
   return i + i / Q;
 }
 
+// Rows per block of the x passes: kRegThreads / Q with P >= Q. The phase
+// that runs Q threads a row covers the block's rows in one sweep; the phase
+// that runs P threads a row sweeps them in ceil(L*P / kRegThreads) rounds, so
+// that both phases keep every thread busy (with rows per block sized by P,
+// the heavier P-point phase would run on Q/P of the threads).
+template <int P, int Q>
+__host__ __device__ constexpr int xlines() {
+  static_assert(P >= Q, "x passes split the line as P >= Q");
+  return kRegThreads / Q;
+}
+// rounds of a phase that runs T threads a row over L rows
+template <int L, int T>
+__host__ __device__ constexpr int xrounds() {
+  return (L + kRegThreads / T - 1) / (kRegThreads / T);
+}
+
 // Forward real transform along x: packed FFT, then untangling into the half
 // spectrum (2*DFT convention of the generic kernels).
 template <typename R, int P, int Q, int PRO>
@@ -260,7 +301,7 @@ __global__ void __launch_bounds__(kRegThreads) k_x_r2c_reg(Grid g, FftAxis ax, c
                                                            const Fld<R>* __restrict__ in1, R c0, R c1,
                                                            C2<R>* __restrict__ out) {
   constexpr int M = P * Q;
-  constexpr int L = reg_lines<P, Q>();
+  constexpr int L = xlines<P, Q>();
   constexpr int LD = M + P + 1;  // >= xpad(M - 1) + 1 and >= M + 1
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
@@ -270,7 +311,7 @@ __global__ void __launch_bounds__(kRegThreads) k_x_r2c_reg(Grid g, FftAxis ax, c
   const int nrows = (int)min((long long)L, nlines - row0);
   const int tid = threadIdx.x;
   const int ra = tid / Q, u = tid % Q;
-  const bool actA = ra < nrows;  // tid < L*Q keeps ra < L
+  const bool actA = ra < nrows;  // ra < L for every tid < L*Q
   C2<R> v[P];
   if (actA) {
     const Fld<R>* a = in0 + (row0 + ra) * g.nx;
@@ -302,18 +343,24 @@ __global__ void __launch_bounds__(kRegThreads) k_x_r2c_reg(Grid g, FftAxis ax, c
     for (int k = 0; k < P; ++k) buf[ra * LD + xpad<Q>(k * Q + u)] = v[k];
   }
   __syncthreads();
-  const int rb = tid / P, kp = tid % P;
-  const bool actB = rb < L && rb < nrows;
-  C2<R> w[Q];
-  if (actB) {
+  // Q-point DFTs, P threads a row; each round reads its rows and writes them
+  // back in natural order (a row's threads sync at the round's barrier)
+  constexpr int RB = kRegThreads / P;
+#pragma unroll 1
+  for (int it = 0; it < xrounds<L, P>(); ++it) {
+    const int rb = tid / P + it * RB, kp = tid % P;
+    const bool actB = tid < RB * P && rb < nrows;
+    C2<R> w[Q];
+    if (actB) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) w[q] = buf[rb * LD + xpad<Q>(kp * Q + q)];
-    RegDft<R, Q, -1>::run(w);
-  }
-  __syncthreads();
-  if (actB) {
+      for (int q = 0; q < Q; ++q) w[q] = buf[rb * LD + xpad<Q>(kp * Q + q)];
+      RegDft<R, Q, -1>::run(w);
+    }
+    __syncthreads();
+    if (actB) {
 #pragma unroll
-    for (int j = 0; j < Q; ++j) buf[rb * LD + kp + P * j] = w[j];
+      for (int j = 0; j < Q; ++j) buf[rb * LD + kp + P * j] = w[j];
+    }
   }
   __syncthreads();
   // untangle: 2X[k] = Fe + W^k (-i) Fo, 2X[M-k] = conj(Fe - W^k (-i) Fo)
@@ -336,6 +383,22 @@ __global__ void __launch_bounds__(kRegThreads) k_x_r2c_reg(Grid g, FftAxis ax, c
   }
 }
 
+// pot4 constants in the arithmetic type: host-split for df64 (Pot4Args::k),
+// converted from fn's doubles otherwise
+template <typename R>
+__device__ __forceinline__ void pot4_consts(const Pot4Args<R>& pa, R (&k)[5]) {
+  if constexpr (std::is_same<R, df64>::value) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) k[i] = pa.k[i];
+  } else {
+    k[0] = (R)pa.fn.a0;
+    k[1] = (R)pa.fn.a1;
+    k[2] = (R)pa.fn.beta_solid;
+    k[3] = (R)pa.fn.den_m;
+    k[4] = (R)pa.fn.c_solid;
+  }
+}
+
 // Inverse real transform along x (unnormalised c2r convention): the tangle
 // into the packed line is done on load, each thread reading X[k] and
 // X[M-k] of its own slots; EPI_POT4 adds the rest of pot4 on store.
@@ -345,7 +408,7 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_reg(Grid g, FftAxis ax, c
                                                            const C2<R>* __restrict__ in1, Fld<R>* out0,
                                                            Fld<R>* out1, Pot4Args<R> pa) {
   constexpr int M = P * Q;
-  constexpr int L = reg_lines<P, Q>();
+  constexpr int L = xlines<P, Q>();
   constexpr int LD = M + P + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
@@ -392,8 +455,13 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_reg(Grid g, FftAxis ax, c
     for (int k = 0; k < P; ++k) buf[ra * LD + xpad<Q>(k * Q + u)] = v[k];
   }
   __syncthreads();
-  const int rb = tid / P, kp = tid % P;
-  if (rb < L && rb < nrows) {
+  R kc[5];
+  pot4_consts<R>(pa, kc);
+  constexpr int RB = kRegThreads / P;
+#pragma unroll 1
+  for (int it = 0; it < xrounds<L, P>(); ++it) {
+    const int rb = tid / P + it * RB, kp = tid % P;
+    if (!(tid < RB * P && rb < nrows)) continue;  // no barrier in this loop
     C2<R> w[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) w[q] = buf[rb * LD + xpad<Q>(kp * Q + q)];
@@ -404,16 +472,13 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_reg(Grid g, FftAxis ax, c
       const long long e = rowe + 2 * (kp + P * j);
       C2<R> val = w[j];
       if (EPI == EPI_POT4) {
-        const Functional& fn = pa.fn;
         const C2<R> cg = ld_pair<R>(pa.dencg + e);
-        const R a0 = (R)fn.a0, a1 = (R)fn.a1;
-        R p0 = fma(cg.x * cg.x, fma(a1, cg.x, a0), val.x);
-        R p1 = fma(cg.y * cg.y, fma(a1, cg.y, a0), val.y);
-        if (fn.lsolid) {
+        R p0 = fma(cg.x * cg.x, fma(kc[1], cg.x, kc[0]), val.x);
+        R p1 = fma(cg.y * cg.y, fma(kc[1], cg.y, kc[0]), val.y);
+        if (pa.fn.lsolid) {
           const C2<R> d = ld_pair<R>(pa.den + e);
-          const R beta = (R)fn.beta_solid, dm = (R)fn.den_m, cs = (R)fn.c_solid;
-          p0 += solid_penalty<R>(d.x, beta, dm, cs);
-          p1 += solid_penalty<R>(d.y, beta, dm, cs);
+          p0 += solid_penalty<R>(d.x, kc[2], kc[3], kc[4]);
+          p1 += solid_penalty<R>(d.y, kc[2], kc[3], kc[4]);
         }
         val = mk<R>(p0, p1);
       }
@@ -434,8 +499,8 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_corr_reg(Grid g, FftAxis 
                                                                 C2<R>* spec, Fld<R>* __restrict__ dencg,
                                                                 const Fld<R>* __restrict__ den, R c0, R c1) {
   constexpr int M = P * Q;
-  constexpr int L = reg_lines<P, Q>();
-  constexpr int LD = M + (P > Q ? P : Q) + 1;
+  constexpr int L = xlines<P, Q>();
+  constexpr int LD = M + P + 1;  // P >= Q: covers xpad<Q> and xpad<P> of M - 1
   extern __shared__ __align__(16) unsigned char smraw[];
   C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
   C2<R>* tws = buf + L * LD;
@@ -478,36 +543,40 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_corr_reg(Grid g, FftAxis 
   }
   __syncthreads();
   // inverse pass, second half, then the prologue and the forward pass's
-  // first half: thread (rb, k'), k' < P
-  const int rb = tid / P, kp = tid % P;
-  const bool actB = rb < L && rb < nrows;
-  C2<R> w[Q];
-  if (actB) {
+  // first half: thread (rb, k'), k' < P, over the block's rows in rounds
+  constexpr int RB = kRegThreads / P;
+#pragma unroll 1
+  for (int it = 0; it < xrounds<L, P>(); ++it) {
+    const int rb = tid / P + it * RB, kp = tid % P;
+    const bool actB = tid < RB * P && rb < nrows;
+    C2<R> w[Q];
+    if (actB) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) w[q] = buf[rb * LD + xpad<Q>(kp * Q + q)];
-    RegDft<R, Q, 1>::run(w);
-    const long long rowe = (row0 + rb) * g.nx;
+      for (int q = 0; q < Q; ++q) w[q] = buf[rb * LD + xpad<Q>(kp * Q + q)];
+      RegDft<R, Q, 1>::run(w);
+      const long long rowe = (row0 + rb) * g.nx;
 #pragma unroll
-    for (int j = 0; j < Q; ++j) {
-      const long long e = rowe + 2 * (kp + P * j);
-      const C2<R> cg = w[j];
-      st_pair<R>(dencg + e, cg);
-      const C2<R> d = ld_pair<R>(den + e);
-      w[j] = mk<R>(d.x * cg.x * fma(c1, cg.x, c0), d.y * cg.y * fma(c1, cg.y, c0));
+      for (int j = 0; j < Q; ++j) {
+        const long long e = rowe + 2 * (kp + P * j);
+        const C2<R> cg = w[j];
+        st_pair<R>(dencg + e, cg);
+        const C2<R> d = ld_pair<R>(den + e);
+        w[j] = mk<R>(d.x * cg.x * fma(c1, cg.x, c0), d.y * cg.y * fma(c1, cg.y, c0));
+      }
+      RegDft<R, Q, -1>::run(w);
+#pragma unroll
+      for (int k = 1; k < Q; ++k) w[k] = mulw<R, -1>(w[k], tws[kp * k]);
     }
-    RegDft<R, Q, -1>::run(w);
+    __syncthreads();  // the round's rows are read: their slots are free again
+    if (actB) {
 #pragma unroll
-    for (int k = 1; k < Q; ++k) w[k] = mulw<R, -1>(w[k], tws[kp * k]);
-  }
-  __syncthreads();  // the exchange buffer is free again
-  if (actB) {
-#pragma unroll
-    for (int k = 0; k < Q; ++k) buf[rb * LD + xpad<P>(k * P + kp)] = w[k];
+      for (int k = 0; k < Q; ++k) buf[rb * LD + xpad<P>(k * P + kp)] = w[k];
+    }
   }
   __syncthreads();
   // forward pass, second half: thread (rc, kq), kq < Q, holds Z[kq + Q*jj]
   const int rc = tid / Q, kq = tid % Q;
-  const bool actC = rc < L && rc < nrows;
+  const bool actC = rc < nrows;
   C2<R> z[P];
   if (actC) {
 #pragma unroll
@@ -569,9 +638,9 @@ template <typename R, int P, int Q>
 void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>& fl, int nout, R scale,
                  const C2<R>* add, cudaStream_t s, bool launch) {
   constexpr int L = reg_lines<P, Q>();
-  const size_t smem = sizeof(C2<R>) * (P * Q * L + P * Q);
+  const size_t smem = zcol_smem<R, P, Q>(false), smem_f = zcol_smem<R, P, Q>(true);
   set_smem(k_zcol_reg<R, P, Q, -1>, smem);
-  set_smem(k_zcol_reg<R, P, Q, 1>, smem);
+  set_smem(k_zcol_reg<R, P, Q, 1>, smem_f);
   if (!launch) return;
   dim3 grid((g.nxh + L - 1) / L, g.ny);
   k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, in, nullptr, scale, nullptr);
@@ -582,7 +651,7 @@ void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>
     if (fl.out[o] == in) order[n++] = o;
   for (int i = 0; i < nout; ++i) {
     const int o = order[i];
-    k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, fl.out[o], fl.f[o], scale,
+    k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, fl.f[o] ? smem_f : smem, s>>>(g, p.z, in, fl.out[o], fl.f[o], scale,
                                                             o == 0 ? add : nullptr);
   }
 }
@@ -590,7 +659,7 @@ void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>
 template <typename R, int P, int Q, int PRO>
 void run_r2c(const Grid& g, const FftPlan& p, const C2<R>* twx, const Fld<R>* a, const Fld<R>* b, R c0, R c1,
              C2<R>* out, cudaStream_t s, bool launch) {
-  constexpr int L = reg_lines<P, Q>();
+  constexpr int L = xlines<P, Q>();
   constexpr int LD = P * Q + P + 1;
   const size_t smem = sizeof(C2<R>) * (L * LD + P * Q);
   set_smem(k_x_r2c_reg<R, P, Q, PRO>, smem);
@@ -603,7 +672,7 @@ void run_r2c(const Grid& g, const FftPlan& p, const C2<R>* twx, const Fld<R>* a,
 template <typename R, int P, int Q, int EPI>
 void run_c2r(const Grid& g, const FftPlan& p, const C2<R>* twx, const C2<R>* i0, const C2<R>* i1, Fld<R>* o0,
              Fld<R>* o1, int nspec, const Pot4Args<R>& pa, cudaStream_t s, bool launch) {
-  constexpr int L = reg_lines<P, Q>();
+  constexpr int L = xlines<P, Q>();
   constexpr int LD = P * Q + P + 1;
   const size_t smem = sizeof(C2<R>) * (L * LD + P * Q);
   set_smem(k_x_c2r_reg<R, P, Q, EPI>, smem);
@@ -616,8 +685,8 @@ void run_c2r(const Grid& g, const FftPlan& p, const C2<R>* twx, const C2<R>* i0,
 template <typename R, int P, int Q>
 void run_c2r_corr(const Grid& g, const FftPlan& p, const C2<R>* twx, C2<R>* spec, Fld<R>* dencg, const Fld<R>* den,
                   R c0, R c1, cudaStream_t s, bool launch) {
-  constexpr int L = reg_lines<P, Q>();
-  constexpr int LD = P * Q + (P > Q ? P : Q) + 1;
+  constexpr int L = xlines<P, Q>();
+  constexpr int LD = P * Q + P + 1;
   const size_t smem = sizeof(C2<R>) * (L * LD + P * Q);
   set_smem(k_x_c2r_corr_reg<R, P, Q>, smem);
   if (!launch) return;

@@ -29,6 +29,7 @@ namespace he4g {
 namespace {
 
 constexpr int kBX = 64, kBY = 4;  // point-kernel blocks (256 threads)
+static_assert(kBX % 32 == 0, "a warp covers 32 consecutive x of one row");
 // z planes per thread of the force kernel: 16 where that still leaves four
 // waves of blocks (256^3), else 8
 int force_planes(const Grid& g) {
@@ -112,7 +113,11 @@ __device__ __forceinline__ Acc acc_of(df64 x) { return Acc{x.hi, x.lo}; }
 __device__ __forceinline__ df64 acc_value(Acc a) { return df_fast2sum(a.hi, a.lo); }
 
 // (d2x + d2y + d2z) psi at a point, zero padded (Deriv3D_pc, id = 2):
-// symmetric pairs summed before the coefficient product
+// symmetric pairs summed before the coefficient product. CHK = false leaves
+// out the padding tests, for warps whose points all have their 6 neighbours
+// inside the grid on every axis (warp_interior); both forms load the same
+// values and do the same arithmetic.
+template <bool CHK>
 __device__ __forceinline__ df2 lap13(const df2* __restrict__ f, const Pt& t, const Grid& g, const StencilD& st) {
   const df2 c = __ldg(f + t.p);
   Acc ar = acc_of(st.d2c * c.x), ai = acc_of(st.d2c * c.y);
@@ -120,20 +125,32 @@ __device__ __forceinline__ df2 lap13(const df2* __restrict__ f, const Pt& t, con
   const df2 zero{df64(0.f, 0.f), df64(0.f, 0.f)};
 #pragma unroll
   for (int o = 1; o <= kStencilHalf; ++o) {
-    df2 a = t.i - o >= 0 ? __ldg(f + t.p - o) : zero;
-    df2 b = t.i + o < g.nx ? __ldg(f + t.p + o) : zero;
+    df2 a = !CHK || t.i - o >= 0 ? __ldg(f + t.p - o) : zero;
+    df2 b = !CHK || t.i + o < g.nx ? __ldg(f + t.p + o) : zero;
     acc_pair<1>(ar, st.d2[0][o], a.x, b.x);
     acc_pair<1>(ai, st.d2[0][o], a.y, b.y);
-    a = t.j - o >= 0 ? __ldg(f + t.p - o * sy) : zero;
-    b = t.j + o < g.ny ? __ldg(f + t.p + o * sy) : zero;
+    a = !CHK || t.j - o >= 0 ? __ldg(f + t.p - o * sy) : zero;
+    b = !CHK || t.j + o < g.ny ? __ldg(f + t.p + o * sy) : zero;
     acc_pair<1>(ar, st.d2[1][o], a.x, b.x);
     acc_pair<1>(ai, st.d2[1][o], a.y, b.y);
-    a = t.k - o >= 0 ? __ldg(f + t.p - o * sz) : zero;
-    b = t.k + o < g.nz ? __ldg(f + t.p + o * sz) : zero;
+    a = !CHK || t.k - o >= 0 ? __ldg(f + t.p - o * sz) : zero;
+    b = !CHK || t.k + o < g.nz ? __ldg(f + t.p + o * sz) : zero;
     acc_pair<1>(ar, st.d2[2][o], a.x, b.x);
     acc_pair<1>(ai, st.d2[2][o], a.y, b.y);
   }
   return df2{acc_value(ar), acc_value(ai)};
+}
+
+// True when every point of the calling warp (32 consecutive x of one (y, z)
+// row: blockDim.x = kBX is a multiple of 32) has all its stencil neighbours
+// inside the grid; the same for every lane, so the branch on it is uniform.
+__device__ __forceinline__ bool warp_interior(const Pt& t, const Grid& g) {
+  const int i0 = t.i - (int)(threadIdx.x & 31u);
+  return i0 >= kStencilHalf && i0 + 31 + kStencilHalf < g.nx && t.j >= kStencilHalf &&
+         t.j + kStencilHalf < g.ny && t.k >= kStencilHalf && t.k + kStencilHalf < g.nz;
+}
+__device__ __forceinline__ df2 lap13_at(const df2* __restrict__ f, const Pt& t, const Grid& g, const StencilD& st) {
+  return warp_interior(t, g) ? lap13<false>(f, t, g, st) : lap13<true>(f, t, g, st);
 }
 
 // Sto4c = timec*(lap*h2o2m4 - pot4*psi) - i*uimp*psi (steppc.f90:55,123;
@@ -193,7 +210,7 @@ __device__ __forceinline__ void block_sum_f1(float x, double* partials) {
 
 // ------------------------------------------------------------ integrators
 // Predictor + modifier (steppc.f90:45-65); roles as k_pc_predict in field.cu.
-__global__ void __launch_bounds__(256) k_pc_predict_df(Grid g, StencilD st, df64 h2o2m4,
+__global__ void __launch_bounds__(256, 5) k_pc_predict_df(Grid g, StencilD st, df64 h2o2m4,
                                                         const df2* __restrict__ psi, df2* p3,
                                                         const df2* __restrict__ h1, df2* h2, df2* pc,
                                                         const df64* __restrict__ pot4,
@@ -204,7 +221,7 @@ __global__ void __launch_bounds__(256) k_pc_predict_df(Grid g, StencilD st, df64
   if (imp && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
     imp_pc_predict_body(imp, c4o3dt_d, c112_d);
   if (!t.ok) return;
-  const df2 lap = lap13(psi, t, g, st);
+  const df2 lap = lap13_at(psi, t, g, st);
   const df2 ps = __ldg(psi + t.p);
   const df2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), h2o2m4);
   const df2 a1 = ldv(h1 + t.p), a2 = ldv(h2 + t.p), o3 = ldv(p3 + t.p), q = ldv(pc + t.p);
@@ -233,7 +250,7 @@ __global__ void __launch_bounds__(256) k_pc_correct_df(Grid g, StencilD st, df64
   const Pt t = point(g);
   float v = 0.f;
   if (t.ok) {
-    const df2 lap = lap13(psit, t, g, st);
+    const df2 lap = lap13_at(psit, t, g, st);
     const df2 ps = __ldg(psit + t.p);
     const df2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), h2o2m4);
     const df2 a1 = __ldg(h1 + t.p), a2 = __ldg(h2 + t.p), o3 = __ldg(p3 + t.p), o2 = __ldg(p2 + t.p);
@@ -271,7 +288,7 @@ __global__ void __launch_bounds__(256) k_rk_stage_df(Grid g, StencilD st, df64 h
                                                       df64 cr, df64 dt, int* health) {
   const Pt t = point(g);
   if (!t.ok) return;
-  const df2 lap = lap13(psi, t, g, st);
+  const df2 lap = lap13_at(psi, t, g, st);
   const df2 ps = __ldg(psi + t.p);
   const df2 f = hpsi(lap, ps, __ldg(pot4 + t.p), __ldg(uimp + t.p), __ldg(timec + t.p), h2o2m4);
   df2 qq = ldv(q + t.p);
@@ -333,12 +350,62 @@ __global__ void __launch_bounds__(256) k_potenimp_df(Grid g, ImpTableD tab, ImpS
   sts(uimp + t.p, u);
 }
 
+// The plane walk of k_force_df for the column (i, j), planes k0 .. k0+zd-1:
+// the z neighbours in a register window that shifts by one plane per step
+// (the plane loop stays rolled, which keeps the kernel's code small enough
+// for the instruction cache). CHK = false leaves out the x/y padding tests,
+// for warps whose columns all have their 6 x and y neighbours inside the
+// grid; both forms load the same values and do the same arithmetic.
+template <bool CHK>
+__device__ __forceinline__ void force_column(const Grid& g, const StencilD& st, const df64* __restrict__ den,
+                                             const ImpTableD& tab, const df64 (&c)[3], df64* uimp_out, int i, int j,
+                                             int k0, int zd, df64 (&s)[3], int& bad) {
+  const df64 zero(0.f, 0.f);
+  const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+  const long long col = (long long)j * g.nx + i;
+  constexpr int W = 2 * kStencilHalf + 1;
+  df64 wz[W];  // den at planes k-6 .. k+6 of this column, k the current plane
+#pragma unroll
+  for (int m = 0; m < W; ++m) {
+    const int k = k0 - kStencilHalf + m;
+    wz[m] = (k >= 0 && k < g.nz) ? __ldg(den + col + k * sz) : zero;
+  }
+  const df64 xi = __ldg(tab.xs + i), yj = __ldg(tab.ys + j);
+#pragma unroll 1
+  for (int m = 0; m < zd; ++m) {
+    const int k = k0 + m;
+    if (k < g.nz) {
+      const long long p = col + k * sz;
+      Acc ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f};
+#pragma unroll
+      for (int o = 1; o <= kStencilHalf; ++o) {
+        df64 a = !CHK || i - o >= 0 ? __ldg(den + p - o) : zero;
+        df64 b = !CHK || i + o < g.nx ? __ldg(den + p + o) : zero;
+        acc_pair<-1>(ax, st.d1[0][o], a, b);
+        a = !CHK || j - o >= 0 ? __ldg(den + p - o * sy) : zero;
+        b = !CHK || j + o < g.ny ? __ldg(den + p + o * sy) : zero;
+        acc_pair<-1>(ay, st.d1[1][o], a, b);
+        acc_pair<-1>(az, st.d1[2][o], wz[kStencilHalf - o], wz[kStencilHalf + o]);
+      }
+      const df64 gx = acc_value(ax), gy = acc_value(ay), gz = acc_value(az);
+      const df64 u = uimp_at(xi, yj, __ldg(tab.zs + k), c, tab, bad);
+      if (uimp_out) sts(uimp_out + p, u);
+      s[0] = fma(gx, u, s[0]);
+      s[1] = fma(gy, u, s[1]);
+      s[2] = fma(gz, u, s[2]);
+    }
+    // shift the window: wz[q] becomes plane k - 5 + q
+#pragma unroll
+    for (int q = 0; q < W - 1; ++q) wz[q] = wz[q + 1];
+    const int kn = k0 - kStencilHalf + m + W;
+    wz[W - 1] = (kn >= 0 && kn < g.nz) ? __ldg(den + col + kn * sz) : zero;
+  }
+}
+
 // derden (derden.f90:26-28) fused with uimp (stored when uimp_out is set) and
 // the force sums of forceimp (potenimp.f90:44-46). Each thread walks zd z
-// planes of one (x, y) column with the z neighbours in a register window
-// that shifts by one plane per step (the plane loop stays rolled, which keeps
-// the kernel's code small enough for the instruction cache); its df64 sums
-// become FP64 before the block reduction.
+// planes of one (x, y) column (force_column); its df64 sums become FP64
+// before the block reduction.
 __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df64* __restrict__ den,
                                                    ImpTableD tab, ImpState* imp, int sel, df64* uimp_out,
                                                    double* partials, ForceFinish fin, int zd) {
@@ -351,45 +418,14 @@ __global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df6
   df64 s[3] = {zero, zero, zero};
   int bad = 0;
   if (i < g.nx && j < g.ny) {
-    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
-    const long long col = (long long)j * g.nx + i;
-    constexpr int W = 2 * kStencilHalf + 1;
-    df64 wz[W];  // den at planes k-6 .. k+6 of this column, k the current plane
-#pragma unroll
-    for (int m = 0; m < W; ++m) {
-      const int k = k0 - kStencilHalf + m;
-      wz[m] = (k >= 0 && k < g.nz) ? __ldg(den + col + k * sz) : zero;
-    }
-    const df64 xi = __ldg(tab.xs + i), yj = __ldg(tab.ys + j);
-#pragma unroll 1
-    for (int m = 0; m < zd; ++m) {
-      const int k = k0 + m;
-      if (k < g.nz) {
-        const long long p = col + k * sz;
-        Acc ax{0.f, 0.f}, ay{0.f, 0.f}, az{0.f, 0.f};
-#pragma unroll
-        for (int o = 1; o <= kStencilHalf; ++o) {
-          df64 a = i - o >= 0 ? __ldg(den + p - o) : zero;
-          df64 b = i + o < g.nx ? __ldg(den + p + o) : zero;
-          acc_pair<-1>(ax, st.d1[0][o], a, b);
-          a = j - o >= 0 ? __ldg(den + p - o * sy) : zero;
-          b = j + o < g.ny ? __ldg(den + p + o * sy) : zero;
-          acc_pair<-1>(ay, st.d1[1][o], a, b);
-          acc_pair<-1>(az, st.d1[2][o], wz[kStencilHalf - o], wz[kStencilHalf + o]);
-        }
-        const df64 gx = acc_value(ax), gy = acc_value(ay), gz = acc_value(az);
-        const df64 u = uimp_at(xi, yj, __ldg(tab.zs + k), c, tab, bad);
-        if (uimp_out) sts(uimp_out + p, u);
-        s[0] = fma(gx, u, s[0]);
-        s[1] = fma(gy, u, s[1]);
-        s[2] = fma(gz, u, s[2]);
-      }
-      // shift the window: wz[q] becomes plane k - 5 + q
-#pragma unroll
-      for (int q = 0; q < W - 1; ++q) wz[q] = wz[q + 1];
-      const int kn = k0 - kStencilHalf + m + W;
-      wz[W - 1] = (kn >= 0 && kn < g.nz) ? __ldg(den + col + kn * sz) : zero;
-    }
+    // the warp's 32 columns share j and span i0 .. i0 + 31
+    const int i0 = i - (int)(threadIdx.x & 31u);
+    const bool inner = i0 >= kStencilHalf && i0 + 31 + kStencilHalf < g.nx && j >= kStencilHalf &&
+                       j + kStencilHalf < g.ny;
+    if (inner)
+      force_column<false>(g, st, den, tab, c, uimp_out, i, j, k0, zd, s, bad);
+    else
+      force_column<true>(g, st, den, tab, c, uimp_out, i, j, k0, zd, s, bad);
   }
   if (bad) atomicOr(&imp->health, 4);
   if (sel == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
