@@ -76,11 +76,46 @@ __device__ __forceinline__ C2<R> csub(C2<R> a, C2<R> b) { return mk<R>(a.x - b.x
 template <typename R>
 __device__ __forceinline__ C2<R> cconj(C2<R> a) { return mk<R>(a.x, -a.y); }
 
+// Sums and products whose result only feeds another df64 addition: the
+// error-free part of the operation without the final renormalisation
+// (Fast2Sum), which the consuming addition performs. The pair hi + lo is
+// exact as before, only |lo| may exceed ulp(hi)/2 by a small factor; the
+// consumer's TwoSum of the high parts is exact for any inputs and its low
+// parts absorb the larger lo, so the bound stays about 2^-48 relative to the
+// operands (a few units of it more). FP64 and FP32: the plain operations.
+template <typename R>
+__device__ __forceinline__ R add_l(R a, R b) {
+  return a + b;
+}
+template <>
+__device__ __forceinline__ df64 add_l<df64>(df64 a, df64 b) {
+  const float s = a.hi + b.hi;
+  const float v = s - a.hi;
+  const float e = (a.hi - (s - v)) + (b.hi - v);
+  return df64(s, e + (a.lo + b.lo));
+}
+template <typename R>
+__device__ __forceinline__ R mul_l(R a, R b) {
+  return a * b;
+}
+template <>
+__device__ __forceinline__ df64 mul_l<df64>(df64 a, df64 b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df64(p, e);
+}
+template <typename R>
+__device__ __forceinline__ C2<R> cadd_l(C2<R> a, C2<R> b) { return mk<R>(add_l<R>(a.x, b.x), add_l<R>(a.y, b.y)); }
+template <typename R>
+__device__ __forceinline__ C2<R> csub_l(C2<R> a, C2<R> b) { return mk<R>(add_l<R>(a.x, -b.x), add_l<R>(a.y, -b.y)); }
+
 // a * w (SIGN < 0) or a * conj(w) (SIGN > 0)
 template <typename R, int SIGN>
 __device__ __forceinline__ C2<R> mulw(C2<R> a, C2<R> w) {
-  if (SIGN < 0) return mk<R>(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
-  return mk<R>(fma(a.x, w.x, a.y * w.y), fma(a.y, w.x, -a.x * w.y));
+  if (SIGN < 0) return mk<R>(fma(a.x, w.x, -mul_l<R>(a.y, w.y)), fma(a.x, w.y, mul_l<R>(a.y, w.x)));
+  return mk<R>(fma(a.x, w.x, mul_l<R>(a.y, w.y)), fma(a.y, w.x, -mul_l<R>(a.x, w.y)));
 }
 // a * (SIGN * i)
 template <typename R, int SIGN>
@@ -94,10 +129,11 @@ __device__ __forceinline__ void bf2(C2<R>* v) {
   v[0] = cadd<R>(t, v[1]);
   v[1] = csub<R>(t, v[1]);
 }
+// the first level's sums feed only the second level's: not renormalised
 template <typename R, int SIGN>
 __device__ __forceinline__ void bf4(C2<R>& a0, C2<R>& a1, C2<R>& a2, C2<R>& a3) {
-  C2<R> t0 = cadd<R>(a0, a2), t1 = csub<R>(a0, a2);
-  C2<R> t2 = cadd<R>(a1, a3), t3 = jmul<R, SIGN>(csub<R>(a1, a3));
+  C2<R> t0 = cadd_l<R>(a0, a2), t1 = csub_l<R>(a0, a2);
+  C2<R> t2 = cadd_l<R>(a1, a3), t3 = jmul<R, SIGN>(csub_l<R>(a1, a3));
   a0 = cadd<R>(t0, t2);
   a2 = csub<R>(t0, t2);
   a1 = cadd<R>(t1, t3);
@@ -399,13 +435,18 @@ __device__ __forceinline__ C2<R> twc(C2<R> a) {
   } else if constexpr (4 * e == 3 * M) {
     return jmul<R, -SIGN>(a);
   } else if constexpr (8 * e == M) {  // (1 - i)/sqrt2, conj for SIGN > 0
-    return SIGN < 0 ? mk<R>((a.x + a.y) * r, (a.y - a.x) * r) : mk<R>((a.x - a.y) * r, (a.y + a.x) * r);
+    // (the sums feed only the products, which renormalise)
+    const R p = add_l<R>(a.x, a.y), m = add_l<R>(a.y, -a.x);
+    return SIGN < 0 ? mk<R>(p * r, m * r) : mk<R>(-m * r, p * r);
   } else if constexpr (8 * e == 3 * M) {  // (-1 - i)/sqrt2
-    return SIGN < 0 ? mk<R>((a.y - a.x) * r, -(a.x + a.y) * r) : mk<R>(-(a.x + a.y) * r, (a.x - a.y) * r);
+    const R p = add_l<R>(a.x, a.y), m = add_l<R>(a.y, -a.x);
+    return SIGN < 0 ? mk<R>(m * r, -p * r) : mk<R>(-p * r, -m * r);
   } else if constexpr (8 * e == 5 * M) {  // (-1 + i)/sqrt2
-    return SIGN < 0 ? mk<R>(-(a.x + a.y) * r, (a.x - a.y) * r) : mk<R>((a.y - a.x) * r, -(a.x + a.y) * r);
+    const R p = add_l<R>(a.x, a.y), m = add_l<R>(a.y, -a.x);
+    return SIGN < 0 ? mk<R>(-p * r, -m * r) : mk<R>(m * r, -p * r);
   } else if constexpr (8 * e == 7 * M) {  // (1 + i)/sqrt2
-    return SIGN < 0 ? mk<R>((a.x - a.y) * r, (a.y + a.x) * r) : mk<R>((a.x + a.y) * r, (a.y - a.x) * r);
+    const R p = add_l<R>(a.x, a.y), m = add_l<R>(a.y, -a.x);
+    return SIGN < 0 ? mk<R>(-m * r, p * r) : mk<R>(p * r, m * r);
   } else {
     constexpr R c = (R)cs2pi(e, M, 0), s = (R)cs2pi(e, M, 1);
     return mulw<R, SIGN>(a, mk<R>(c, -s));
