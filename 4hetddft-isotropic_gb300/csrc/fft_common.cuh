@@ -106,16 +106,34 @@ __device__ __forceinline__ df64 mul_l<df64>(df64 a, df64 b) {
   e = fmaf(a.lo, b.hi, e);
   return df64(p, e);
 }
+// a*b + c with the same treatment (the df64 fma without its Fast2Sum)
+template <typename R>
+__device__ __forceinline__ R fma_l(R a, R b, R c) {
+  return fma(a, b, c);
+}
+template <>
+__device__ __forceinline__ df64 fma_l<df64>(df64 a, df64 b, df64 c) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float s = p + c.hi;
+  const float v = s - p;
+  const float t = (p - (s - v)) + (c.hi - v);
+  return df64(s, t + (e + c.lo));
+}
 template <typename R>
 __device__ __forceinline__ C2<R> cadd_l(C2<R> a, C2<R> b) { return mk<R>(add_l<R>(a.x, b.x), add_l<R>(a.y, b.y)); }
 template <typename R>
 __device__ __forceinline__ C2<R> csub_l(C2<R> a, C2<R> b) { return mk<R>(add_l<R>(a.x, -b.x), add_l<R>(a.y, -b.y)); }
 
-// a * w (SIGN < 0) or a * conj(w) (SIGN > 0)
+// a * w (SIGN < 0) or a * conj(w) (SIGN > 0). Every product with a twiddle
+// feeds an addition (the next butterfly, the tangle or the untangle), so in
+// df64 its result is left for that addition to renormalise.
 template <typename R, int SIGN>
 __device__ __forceinline__ C2<R> mulw(C2<R> a, C2<R> w) {
-  if (SIGN < 0) return mk<R>(fma(a.x, w.x, -mul_l<R>(a.y, w.y)), fma(a.x, w.y, mul_l<R>(a.y, w.x)));
-  return mk<R>(fma(a.x, w.x, mul_l<R>(a.y, w.y)), fma(a.y, w.x, -mul_l<R>(a.x, w.y)));
+  if (SIGN < 0) return mk<R>(fma_l<R>(a.x, w.x, -mul_l<R>(a.y, w.y)), fma_l<R>(a.x, w.y, mul_l<R>(a.y, w.x)));
+  return mk<R>(fma_l<R>(a.x, w.x, mul_l<R>(a.y, w.y)), fma_l<R>(a.y, w.x, -mul_l<R>(a.x, w.y)));
 }
 // a * (SIGN * i)
 template <typename R, int SIGN>
