@@ -157,6 +157,18 @@ __device__ __forceinline__ void bf4(C2<R>& a0, C2<R>& a1, C2<R>& a2, C2<R>& a3) 
   a1 = cadd<R>(t1, t3);
   a3 = csub<R>(t1, t3);
 }
+// bf4 with both levels left unnormalised: the first stage of a composite
+// DFT (reg_ct), whose outputs feed only twiddle products and the second
+// stage's butterflies
+template <typename R, int SIGN>
+__device__ __forceinline__ void bf4_l(C2<R>& a0, C2<R>& a1, C2<R>& a2, C2<R>& a3) {
+  C2<R> t0 = cadd_l<R>(a0, a2), t1 = csub_l<R>(a0, a2);
+  C2<R> t2 = cadd_l<R>(a1, a3), t3 = jmul<R, SIGN>(csub_l<R>(a1, a3));
+  a0 = cadd_l<R>(t0, t2);
+  a2 = csub_l<R>(t0, t2);
+  a1 = cadd_l<R>(t1, t3);
+  a3 = csub_l<R>(t1, t3);
+}
 template <typename R, int SIGN>
 __device__ __forceinline__ void bf8(C2<R>* v) {
   const R r = (R)0.70710678118654752440;
@@ -164,12 +176,13 @@ __device__ __forceinline__ void bf8(C2<R>* v) {
   C2<R> b0 = v[1], b1 = v[3], b2 = v[5], b3 = v[7];
   bf4<R, SIGN>(a0, a1, a2, a3);
   bf4<R, SIGN>(b0, b1, b2, b3);
+  // (the sums feed only the products, which renormalise)
   if (SIGN < 0) {
-    b1 = mk<R>((b1.x + b1.y) * r, (b1.y - b1.x) * r);
-    b3 = mk<R>((b3.y - b3.x) * r, -(b3.x + b3.y) * r);
+    b1 = mk<R>(add_l<R>(b1.x, b1.y) * r, add_l<R>(b1.y, -b1.x) * r);
+    b3 = mk<R>(add_l<R>(b3.y, -b3.x) * r, -add_l<R>(b3.x, b3.y) * r);
   } else {
-    b1 = mk<R>((b1.x - b1.y) * r, (b1.y + b1.x) * r);
-    b3 = mk<R>(-(b3.x + b3.y) * r, (b3.x - b3.y) * r);
+    b1 = mk<R>(add_l<R>(b1.x, -b1.y) * r, add_l<R>(b1.y, b1.x) * r);
+    b3 = mk<R>(-add_l<R>(b3.x, b3.y) * r, add_l<R>(b3.x, -b3.y) * r);
   }
   b2 = jmul<R, SIGN>(b2);
   v[0] = cadd<R>(a0, b0);
@@ -489,7 +502,10 @@ __device__ __forceinline__ void reg_ct(C2<R>* v) {
       constexpr int n1 = decltype(n1c)::value;
       t[n1] = v[B * n1 + n2];
     });
-    RegDft<R, A, SIGN>::run(t);
+    if constexpr (A == 4)
+      bf4_l<R, SIGN>(t[0], t[1], t[2], t[3]);
+    else
+      RegDft<R, A, SIGN>::run(t);
     sfor<A>([&](auto k1c) {
       constexpr int k1 = decltype(k1c)::value;
       y[k1 * B + n2] = twc<R, M, n2 * k1, SIGN>(t[k1]);

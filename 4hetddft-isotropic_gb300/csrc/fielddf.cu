@@ -309,10 +309,15 @@ __global__ void __launch_bounds__(256) k_rk_stage_df(Grid g, StencilD st, df64 h
 // updatepoten (potenimp.f90:71-95) at the point (x, y, z) about centre c:
 // t = |x - c| / delinter, node floor(t), weight t - floor(t). Points beyond
 // the table give 0 and set *bad.
-__device__ __forceinline__ df64 uimp_at(df64 x, df64 y, df64 z, const df64 (&c)[3], const ImpTableD& tab,
-                                        int& bad) {
-  const df64 dx = x - c[0], dy = y - c[1], dz = z - c[2];
-  const df64 r = df_sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+// The x and y part of r^2 (constant along a z column) and the table value at
+// r^2 = dz^2 + dxy2; uimp_at composes them, and the force kernel's plane walk
+// forms dxy2 once per column with the same operations.
+__device__ __forceinline__ df64 uimp_dxy2(df64 x, df64 y, const df64 (&c)[3]) {
+  const df64 dx = x - c[0], dy = y - c[1];
+  return fma(dx, dx, dy * dy);
+}
+__device__ __forceinline__ df64 uimp_r2(df64 r2, const ImpTableD& tab, int& bad) {
+  const df64 r = df_sqrt(r2);
   const df64 tq = r * tab.inv;
   float fl = floorf(tq.hi);
   if (fl == tq.hi && tq.lo < 0.f) fl -= 1.f;
@@ -325,6 +330,11 @@ __device__ __forceinline__ df64 uimp_at(df64 x, df64 y, df64 z, const df64 (&c)[
   const df64 w = df_fast2sum(tq.hi - fl, tq.lo);
   const df64 p0 = __ldg(tab.potion + ir), p1 = __ldg(tab.potion + ir + 1);
   return fma(w, p1 - p0, p0);
+}
+__device__ __forceinline__ df64 uimp_at(df64 x, df64 y, df64 z, const df64 (&c)[3], const ImpTableD& tab,
+                                        int& bad) {
+  const df64 dz = z - c[2];
+  return uimp_r2(fma(dz, dz, uimp_dxy2(x, y, c)), tab, bad);
 }
 
 __device__ __forceinline__ void centre_of(ImpState* imp, int sel, df64 (&c)[3]) {
@@ -370,7 +380,7 @@ __device__ __forceinline__ void force_column(const Grid& g, const StencilD& st, 
     const int k = k0 - kStencilHalf + m;
     wz[m] = (k >= 0 && k < g.nz) ? __ldg(den + col + k * sz) : zero;
   }
-  const df64 xi = __ldg(tab.xs + i), yj = __ldg(tab.ys + j);
+  const df64 dxy2 = uimp_dxy2(__ldg(tab.xs + i), __ldg(tab.ys + j), c);
 #pragma unroll 1
   for (int m = 0; m < zd; ++m) {
     const int k = k0 + m;
@@ -388,7 +398,8 @@ __device__ __forceinline__ void force_column(const Grid& g, const StencilD& st, 
         acc_pair<-1>(az, st.d1[2][o], wz[kStencilHalf - o], wz[kStencilHalf + o]);
       }
       const df64 gx = acc_value(ax), gy = acc_value(ay), gz = acc_value(az);
-      const df64 u = uimp_at(xi, yj, __ldg(tab.zs + k), c, tab, bad);
+      const df64 dz = __ldg(tab.zs + k) - c[2];
+      const df64 u = uimp_r2(fma(dz, dz, dxy2), tab, bad);
       if (uimp_out) sts(uimp_out + p, u);
       s[0] = fma(gx, u, s[0]);
       s[1] = fma(gy, u, s[1]);
