@@ -342,13 +342,6 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
-// Closes the thread's current group of copies; cp_async_wait<N>() waits until
-// at most N of its closed groups are still in flight (the oldest land first).
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 
 // Loads of real fields into the arithmetic type: one value (ldf), an
 // aligned pair of x-adjacent values (ld_pair); st_pair stores a pair.

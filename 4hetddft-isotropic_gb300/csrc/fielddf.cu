@@ -417,7 +417,7 @@ __device__ __forceinline__ void force_column(const Grid& g, const StencilD& st, 
 // the force sums of forceimp (potenimp.f90:44-46). Each thread walks zd z
 // planes of one (x, y) column (force_column); its df64 sums become FP64
 // before the block reduction.
-__global__ void __launch_bounds__(256) k_force_df(Grid g, StencilD st, const df64* __restrict__ den,
+__global__ void __launch_bounds__(256, 4) k_force_df(Grid g, StencilD st, const df64* __restrict__ den,
                                                    ImpTableD tab, ImpState* imp, int sel, df64* uimp_out,
                                                    double* partials, ForceFinish fin, int zd) {
   const int i = blockIdx.x * kBX + threadIdx.x;
