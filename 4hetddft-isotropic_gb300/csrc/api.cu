@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "df64.cuh"
+#include "setup_math.h"
 #include "he4g_df.cuh"
 #include "he4g_internal.cuh"
 
@@ -903,7 +904,9 @@ int he4g_footprint(const he4g_config* c, uint64_t* bytes) {
 
 int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk, const double* kalfs,
                 const double* potion, he4g_run** out) {
-  if (!cfg || !out || !fvlj4 || !wcgk || !potion) return HE4G_EINVAL;
+  if (!cfg || !out || !potion || (!fvlj4) != (!wcgk)) return HE4G_EINVAL;
+  // NULL fvlj4 and wcgk (and kalfs): the tables are built on the device
+  const bool dev_tables = !fvlj4;
   *out = nullptr;
   he4g_run* r = new he4g_run();
   r->cfg = *cfg;
@@ -919,7 +922,7 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
     return bad("grid sizes must lie in [16, 320]");
   if (c.nx % 2 != 0) return bad("nx must be even (packed real transform)");
   if (!radix_ok(c.nx) || !radix_ok(c.ny) || !radix_ok(c.nz)) return bad("grid sizes must be 2^a 3^b 5^c");
-  if (c.core == HE4G_CORE_OTC && !kalfs) return bad("core OTC needs the kalfs table");
+  if (c.core == HE4G_CORE_OTC && !kalfs && !dev_tables) return bad("core OTC needs the kalfs table");
   if (c.npot < 2 || !(c.delinter > 0)) return bad("bad potential table");
   if (c.precision != HE4G_PREC_FP64 && c.precision != HE4G_PREC_MIXED && c.precision != HE4G_PREC_DF64)
     return bad("unsupported precision");
@@ -1049,9 +1052,19 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
     he4g_destroy(r);
     return HE4G_ENOMEM;
   }
-  upload_field(r, r->fvlj4, fvlj4, nh);
-  upload_field(r, r->wcgk, wcgk, nh);
-  if (fn.otc) upload_field(r, r->kalfs, kalfs, nh);
+  if (dev_tables) {
+    const double bf = he4g_setup::bforce_ot(c.eps4, c.sigma4, c.h4);
+    if (launch_build_tables(dfm(r) ? 2 : mixed(r) ? 1 : 0, c.nx, c.ny, c.nz, g.hx, g.hy, g.hz, bf, 8.0 * c.eps4,
+                            std::pow(c.sigma4, 6), c.h4, c.hcg, c.l_alpha, r->fvlj4, r->wcgk,
+                            fn.otc ? r->kalfs : nullptr, r->s) != 0) {
+      he4g_destroy(r);
+      return HE4G_ECUDA;
+    }
+  } else {
+    upload_field(r, r->fvlj4, fvlj4, nh);
+    upload_field(r, r->wcgk, wcgk, nh);
+    if (fn.otc) upload_field(r, r->kalfs, kalfs, nh);
+  }
   upload_field(r, r->potion, potion, c.npot);
   // grids (DFT4He3d.f90:303-313) and the absorber (:689-699), its real part
   // rounded to single precision as the reference's default-kind CMPLX does

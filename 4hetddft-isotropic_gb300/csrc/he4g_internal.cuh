@@ -107,6 +107,12 @@ constexpr int kFinishCounters = 4097;  // 1 + groups of 256 blocks (grids up to 
 int launch_finish_pc(const double* partials, int nblocks, const PcFinish& fin, cudaStream_t s);
 int launch_finish_force(const double* partials, int nblocks, const ForceFinish& fin, cudaStream_t s);
 
+// Device set-up of a run's k-space tables (setup_dev.cu) in the run's table
+// type (prec: 0 FP64, 1 FP32, 2 df64); kalfs may be NULL. 0 on success.
+int launch_build_tables(int prec, int nx, int ny, int nz, double hx, double hy, double hz, double bf, double aux1,
+                        double sigma6, double h4, double hcg, double l_alpha, void* fvlj4, void* wcgk, void* kalfs,
+                        cudaStream_t s);
+
 // Tile shapes of the line passes, chosen per run (he4g_autotune): lines per
 // block of the generic x passes, log2 of the kx columns per generic y/z
 // block, and which passes run on the register engine (ENGINE_* bits; only

@@ -16,58 +16,10 @@
 #include <vector>
 
 #include "../../include/he4g.h"
+#include "setup_math.h"
 
 namespace {
 
-constexpr double kPi = 3.14159265358979323846;
-
-// Si(x) = int_0^x sin(t)/t dt. Below 3: the Maclaurin series; above: the
-// continued fraction of E1(i x) (Abramowitz & Stegun 5.1.22), evaluated with
-// the modified Lentz method, Si(x) = pi/2 + Im(-E1(i x)).
-double sine_integral(double x) {
-  const double ax = std::fabs(x);
-  if (ax == 0.0) return 0.0;
-  double res;
-  if (ax < 3.0) {
-    const double x2 = ax * ax;
-    double term = ax, sum = ax;
-    for (int k = 1; k < 200; ++k) {
-      term *= -x2 / ((2.0 * k) * (2.0 * k + 1.0));
-      const double add = term / (2.0 * k + 1.0);
-      sum += add;
-      if (std::fabs(add) < 1e-18 * std::fabs(sum)) break;
-    }
-    res = sum;
-  } else {
-    // f = b0 + a1/(b1 + a2/(b2 + ...)), b_k = i x + 2k + 1, a_k = -k^2
-    double br = 1.0, bi = ax;
-    double fr = br, fi = bi;
-    double cr = fr, ci = fi, dr = 0.0, di = 0.0;
-    for (int k = 1; k < 100000; ++k) {
-      const double ak = -static_cast<double>(k) * k;
-      br += 2.0;
-      double tr = br + ak * dr, ti = bi + ak * di;
-      double den = tr * tr + ti * ti;
-      dr = tr / den;
-      di = -ti / den;
-      const double cden = cr * cr + ci * ci;
-      cr = br + ak * cr / cden;
-      ci = bi - ak * ci / cden;
-      const double er = cr * dr - ci * di, ei = cr * di + ci * dr;
-      const double nr = fr * er - fi * ei, ni = fr * ei + fi * er;
-      fr = nr;
-      fi = ni;
-      if (std::fabs(er - 1.0) + std::fabs(ei) < 1e-17) break;
-    }
-    // E1(ix) = exp(-ix) / f
-    const double c = std::cos(ax), s = std::sin(ax);
-    const double fd = fr * fr + fi * fi;
-    const double ir = fr / fd, ii = -fi / fd;
-    const double e1i = c * ii - s * ir;
-    res = e1i + 0.5 * kPi;
-  }
-  return x < 0 ? -res : res;
-}
 
 double tang_toennies(double r, double AA, double BB, double C6, double C8, double C10) {
   const double rbohr = 0.5292, hartree_to_k = 27.21 * 11604.0;
@@ -181,38 +133,6 @@ double v_pair(const char* selec, double r, double r_cutoff, double umax) {
   }
 }
 
-// pi/2 - Si(a x) (fforma.f90 sinint, a > 0)
-double sinint(double a, double x) {
-  const double s = sine_integral(a * x);
-  return a > 0.0 ? 0.5 * kPi - s : 0.5 * kPi + s;
-}
-double sinx11(double a, double x) {
-  const double y = a * x, y2 = y * y;
-  const double d[5] = {1.0, y2, y2 * y2, y2 * y2 * y2, y2 * y2 * y2 * y2};
-  const double b[5] = {40320.0, -720.0, 24.0, -2.0, 1.0};
-  const double c[5] = {362880.0, -5040.0, 120.0, -6.0, 1.0};
-  double bd = 0.0, cd = 0.0;
-  for (int i = 0; i < 5; ++i) {
-    bd += b[i] * d[i];
-    cd += c[i] * d[i];
-  }
-  const double res1 = (a * bd * std::cos(y) + cd * std::sin(y) / x) / (3628800.0 * std::pow(x, 9));
-  const double res2 = -(std::pow(a, 10) * sinint(a, x)) / 3628800.0;
-  return res1 + res2;
-}
-double sinx5(double a, double x) {
-  const double y = a * x, y2 = y * y;
-  const double bd = -2.0 + y2, cd = -6.0 + y2;
-  const double res1 = -(a * bd * std::cos(y) + cd * std::sin(y) / x) / (24.0 * x * x * x);
-  const double res2 = (std::pow(a, 4) * sinint(a, x)) / 24.0;
-  return res1 + res2;
-}
-double bforce_ot(double eps, double sigma, double hc) {
-  const double pi4 = 4.0 * (4.0 * std::atan(1.0)), eps4 = 4.0 * eps;
-  const double s6 = std::pow(sigma, 6), s12 = s6 * s6;
-  return pi4 * eps4 * s12 / (9.0 * std::pow(hc, 9)) - pi4 * eps4 * s6 / (3.0 * std::pow(hc, 3));
-}
-
 // p-grid in FFTW order (DFT4He3d.f90:314-340)
 std::vector<double> pgrid(int n, double h) {
   std::vector<double> p(n);
@@ -277,9 +197,8 @@ extern "C" int he4g_build_tables(const he4g_config* c, const char* selec, double
   const double hx = 2.0 * std::fabs(c->xmax) / nx, hy = 2.0 * std::fabs(c->ymax) / ny,
                hz = 2.0 * std::fabs(c->zmax) / nz;
   const std::vector<double> px = pgrid(nx, hx), py = pgrid(ny, hy), pz = pgrid(nz, hz);
-  const double twopi = 2.0 * kPi;
   const double sigma6 = std::pow(c->sigma4, 6), aux1 = 8.0 * c->eps4;
-  const double bf = bforce_ot(c->eps4, c->sigma4, c->h4);
+  const double bf = he4g_setup::bforce_ot(c->eps4, c->sigma4, c->h4);
   // the form factor depends on |p| only; evaluate each distinct |p| once
   std::unordered_map<unsigned long long, double> cache;
   cache.reserve(1 << 16);
@@ -299,30 +218,13 @@ extern "C" int he4g_build_tables(const he4g_config* c, const char* selec, double
           if (it != cache.end()) {
             v = it->second;
           } else {
-            if (std::fabs(p) < 1e-10) {
-              v = bf;
-            } else {
-              const double a2 = twopi * p;
-              const double t1 = sinx11(a2, c->h4), t2 = sinx5(a2, c->h4);
-              v = (aux1 * sigma6 * (sigma6 * t1 - t2)) / p;
-            }
+            v = he4g_setup::fvlj4_at(p, bf, aux1, sigma6, c->h4);
             cache.emplace(key, v);
           }
           fvlj4[t] = v;
         }
-        if (wcgk) {
-          if (p > 0.0) {
-            const double arg = twopi * p * c->hcg;
-            const double aux = std::sin(arg) - arg * std::cos(arg);
-            wcgk[t] = std::fabs(aux) < 1e-10 ? 1.0 : 3.0 * aux / (arg * arg * arg);
-          } else {
-            wcgk[t] = 1.0;
-          }
-        }
-        if (kalfs) {
-          const double e = kPi * c->l_alpha * p;
-          kalfs[t] = std::exp(-(e * e));
-        }
+        if (wcgk) wcgk[t] = he4g_setup::wcgk_at(p, c->hcg);
+        if (kalfs) kalfs[t] = he4g_setup::kalfs_at(p, c->l_alpha);
       }
     }
   }

@@ -66,19 +66,37 @@ def build_tables(cfg, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463, with_kalf
     return {"fvlj4": fv, "wcgk": wc, "kalfs": ka, "potion": po}
 
 
-class Run:
-    """One GPU-resident run (he4g_run)."""
+def potion_table(cfg, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463):
+    """The radial impurity table alone (potenimpini), for runs whose k-space
+    tables are built on the device."""
+    lib = abi.load()
+    po = np.empty(cfg.npot)
+    rc = lib.he4g_build_tables(C.byref(cfg), selec.encode(), r_cutoff, umax, None, None, None, abi.dptr(po))
+    if rc:
+        raise He4gError(rc, "build_tables")
+    return {"fvlj4": None, "wcgk": None, "kalfs": None, "potion": po}
 
-    def __init__(self, cfg, tables=None, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463):
+
+class Run:
+    """One GPU-resident run (he4g_run). device_tables: build fvlj4, wcgk and
+    kalfs on the device (he4g_create with NULL table pointers) instead of on
+    the host; only the radial impurity table is built here."""
+
+    def __init__(self, cfg, tables=None, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463, device_tables=False):
         self.lib = abi.load()
         self.cfg = cfg
-        self.tables = tables if tables is not None else build_tables(cfg, selec, r_cutoff, umax)
+        if tables is None:
+            tables = (potion_table if device_tables else build_tables)(cfg, selec, r_cutoff, umax)
+        self.tables = tables
         self.shape = (cfg.nz, cfg.ny, cfg.nx)
         h = C.c_void_p()
         t = self.tables
-        rc = self.lib.he4g_create(C.byref(cfg), abi.dptr(t["fvlj4"]), abi.dptr(t["wcgk"]),
-                                  abi.dptr(t["kalfs"]) if t.get("kalfs") is not None else None,
-                                  abi.dptr(t["potion"]), C.byref(h))
+
+        def ptr(name):
+            return abi.dptr(t[name]) if t.get(name) is not None else None
+
+        rc = self.lib.he4g_create(C.byref(cfg), ptr("fvlj4"), ptr("wcgk"), ptr("kalfs"), abi.dptr(t["potion"]),
+                                  C.byref(h))
         if rc:
             raise He4gError(rc, "he4g_create failed")
         self.h = h

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(ROOT, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libhe4g.so")
-SOURCES = ["fft_reg_df.cu", "fft_reg.cu", "fft_xy.cu", "api.cu", "field.cu", "fieldmp.cu", "fielddf.cu", "fft.cu", "setup.cpp", "noalloc.cu"]
+SOURCES = ["fft_reg_df.cu", "fft_reg.cu", "fft_xy.cu", "api.cu", "field.cu", "fieldmp.cu", "fielddf.cu", "fft.cu", "setup.cpp", "setup_dev.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

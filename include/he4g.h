@@ -134,7 +134,12 @@ int he4g_footprint(const he4g_config* cfg, uint64_t* bytes);
 
 /* Allocates the run on the current CUDA device and uploads the tables
  * (replaces dimen.f90, fftini fft.f90:5-76 and the table set-up calls of
- * DFT4He3d.f90:518-596). kalfs is required for core OTC, else may be NULL. */
+ * DFT4He3d.f90:518-596). kalfs is required for core OTC, else may be NULL.
+ * With fvlj4 and wcgk both NULL (kalfs then ignored) the three k-space tables
+ * are computed on the device from cfg instead (fforma.f90:36-60,
+ * initcg.f90:32-49, DFT4He3d.f90:592-596, the formulas of he4g_build_tables,
+ * equal to its tables to a few ulps); potion always comes from the host.
+ * Exactly one of fvlj4 and wcgk NULL is HE4G_EINVAL. */
 int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
                 const double* kalfs, const double* potion, he4g_run** out);
 
