@@ -113,9 +113,47 @@ double alkali_he(double dist, int elem) {
 
 // Select_pot (V_impur.f90): the radial potential named selec, umax inside
 // r_cutoff; -1 when the name is not implemented
+// Ag-He (V_impur.f90:1035-1092): exponential repulsion minus a C6..C12
+// dispersion series, damped by exp(-(D/r - 1)^2) inside r = D. Rows: ground
+// state, Pi, Sigma; columns A, alpha, beta, D, C6, C8, C10, C12.
+double ag_he(double r, int state) {
+  static const double coef[3][8] = {
+      {78741.3877, 0.65299, 0.36367, 12.093, 137042.07, 189386.217, 111358462.0, 1.17670377e10},
+      {0.7095092e6, 1.9928, 0.45500, 4.0562, 0.21661134e6, 123454.7952, 0.307155024e6, 0.740464032e-10},
+      {40005.2, 0.41529, 0.14888, 25.730, 1.97443e-9, 3.37393e-6, 0.00788363, 7.52624e12}};
+  const double* c = coef[state];
+  if (r == 0.0) return c[0];
+  const double damp = r <= c[3] ? std::exp(-(c[3] / r - 1.0) * (c[3] / r - 1.0)) : 1.0;
+  const double r2 = r * r, r6 = r2 * r2 * r2, r8 = r6 * r2, r10 = r8 * r2, r12 = r10 * r2;
+  return c[0] * std::exp(-c[1] * r - c[2] * r2) - damp * (c[4] / r6 + c[5] / r8 + c[6] / r10 + c[7] / r12);
+}
+
+// Ba-He ground state (V_impur.f90:1194-1210): a flat core to 3.7 A, then a
+// fit in the even inverse powers 18 down to 6
+double ba_he(double x) {
+  if (x <= 3.7) return 1297.1;
+  const double x2 = x * x, x6 = x2 * x2 * x2, x8 = x6 * x2, x10 = x8 * x2, x12 = x10 * x2, x14 = x12 * x2,
+               x16 = x14 * x2, x18 = x16 * x2;
+  return -6.146426949008034e14 / x18 + 1.6797251118695925e14 / x16 - 1.6513058293510484e13 / x14 +
+         7.015334514979032e11 / x12 - 1.1066880774828484e10 / x10 + 4.900282758445466e7 / x8 -
+         450294.6878721156 / x6;
+}
+
+// Au-He (V_impur.f90:2476-2497): -De (1 + a1 s + ... + a9 s^9) exp(-a1 s) with
+// s = r - Re, the polynomial evaluated in Horner form as the reference does
+double au_he(double rr) {
+  static const double a[9] = {1.6417, -0.6164, 0.3770, -0.0549, 0.0018, 0.0046, -0.0010, 0.0001, 2.7e-6};
+  const double Re = 4.124, De = 20.301143;
+  const double s = rr - Re;
+  double poly = a[8];
+  for (int k = 7; k >= 0; --k) poly = a[k] + s * poly;
+  return -De * (1.0 + s * poly) * std::exp(-a[0] * s);
+}
+
 int pot_kind(const char* selec) {
-  static const char* names[] = {"Xe_He", "Ar_He", "Aziz_He", "LJ_OT", "LI", "NA", "K", "RB", "CS", "null"};
-  for (int k = 0; k < 10; ++k)
+  static const char* names[] = {"Xe_He", "Ar_He", "Aziz_He", "LJ_OT", "LI",    "NA",     "K",     "RB",
+                                "CS",    "null",  "Ag_gs",   "Ag_Pi", "Ag_Sig", "Ba_gs", "Au"};
+  for (int k = 0; k < 15; ++k)
     if (std::strcmp(selec, names[k]) == 0) return k;
   return -1;
 }
@@ -129,6 +167,9 @@ double v_pair(const char* selec, double r, double r_cutoff, double umax) {
     case 2: return aziz_he(r);
     case 3: return lj_ot(r);
     case 4: case 5: case 6: case 7: case 8: return alkali_he(r, kind - 4);
+    case 10: case 11: case 12: return ag_he(r, kind - 10);
+    case 13: return ba_he(r);
+    case 14: return au_he(r);
     default: return tang_toennies(r, 74.9002, 1.8175, 21.5674, 430.148, 10610.21);
   }
 }

@@ -383,6 +383,43 @@ double orc_v_alkali_he(double dist, int elem) {
   return vimp * evk * hartree;
 }
 
+/* Ag-He (V_impur.f90:1035-1092): A exp(-alpha r - beta r^2) minus the C6..C12
+   dispersion series, damped by exp(-(D/r - 1)^2) for r <= D; state 0: ground
+   state, 1: Pi, 2: Sigma */
+double orc_v_ag_he(double r, int state) {
+  static const double P[3][8] = {
+      {78741.3877, 0.65299, 0.36367, 12.093, 137042.07, 189386.217, 111358462.0, 1.17670377e10},
+      {0.7095092e6, 1.9928, 0.45500, 4.0562, 0.21661134e6, 123454.7952, 0.307155024e6, 0.740464032e-10},
+      {40005.2, 0.41529, 0.14888, 25.730, 1.97443e-9, 3.37393e-6, 0.00788363, 7.52624e12}};
+  const double* q = P[state];
+  if (r == 0.0) return q[0];
+  const double damp = r <= q[3] ? exp(-(q[3] / r - 1.0) * (q[3] / r - 1.0)) : 1.0;
+  const double r2 = r * r, r6 = r2 * r2 * r2, r8 = r6 * r2, r10 = r8 * r2, r12 = r10 * r2;
+  return q[0] * exp(-q[1] * r - q[2] * r2) - damp * (q[4] / r6 + q[5] / r8 + q[6] / r10 + q[7] / r12);
+}
+
+/* Ba-He ground state (V_impur.f90:1194-1210): a constant core up to 3.7 A,
+   then even inverse powers 18 .. 6 */
+double orc_v_ba_he(double x) {
+  if (x <= 3.7) return 1297.1;
+  const double x2 = x * x, x6 = x2 * x2 * x2, x8 = x6 * x2, x10 = x8 * x2, x12 = x10 * x2, x14 = x12 * x2,
+               x16 = x14 * x2, x18 = x16 * x2;
+  return -6.146426949008034e14 / x18 + 1.6797251118695925e14 / x16 - 1.6513058293510484e13 / x14 +
+         7.015334514979032e11 / x12 - 1.1066880774828484e10 / x10 + 4.900282758445466e7 / x8 -
+         450294.6878721156 / x6;
+}
+
+/* Au-He (V_impur.f90:2476-2497): -De (1 + a1 s + ... + a9 s^9) exp(-a1 s),
+   s = r - Re, the polynomial in Horner form */
+double orc_v_au_he(double rr) {
+  static const double a[9] = {1.6417, -0.6164, 0.3770, -0.0549, 0.0018, 0.0046, -0.0010, 0.0001, 2.7e-6};
+  const double Re = 4.124, De = 20.301143;
+  const double s = rr - Re;
+  double poly = a[8];
+  for (int k = 7; k >= 0; --k) poly = a[k] + s * poly;
+  return -De * (1.0 + s * poly) * exp(-a[0] * s);
+}
+
 /* Select_pot (V_impur.f90): umax inside r_cutoff; 'null' is zero everywhere */
 double orc_select_pot(const char* selec, double r, double r_cutoff, double umax) {
   if (strcmp(selec, "null") == 0) return 0.0;
@@ -390,6 +427,11 @@ double orc_select_pot(const char* selec, double r, double r_cutoff, double umax)
   if (strcmp(selec, "Ar_He") == 0) return orc_v_ar_he(r);
   if (strcmp(selec, "Aziz_He") == 0) return orc_v_aziz_he(r);
   if (strcmp(selec, "LJ_OT") == 0) return orc_v_lj_ot(r);
+  if (strcmp(selec, "Ag_gs") == 0) return orc_v_ag_he(r, 0);
+  if (strcmp(selec, "Ag_Pi") == 0) return orc_v_ag_he(r, 1);
+  if (strcmp(selec, "Ag_Sig") == 0) return orc_v_ag_he(r, 2);
+  if (strcmp(selec, "Ba_gs") == 0) return orc_v_ba_he(r);
+  if (strcmp(selec, "Au") == 0) return orc_v_au_he(r);
   static const char* alk[5] = {"LI", "NA", "K", "RB", "CS"};
   for (int k = 0; k < 5; ++k)
     if (strcmp(selec, alk[k]) == 0) return orc_v_alkali_he(r, k);

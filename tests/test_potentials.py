@@ -7,7 +7,7 @@ import pytest
 import he4gpu
 from oracle import oracle
 
-NEW = ["Aziz_He", "LJ_OT", "LI", "NA", "K", "RB", "CS", "null"]
+NEW = ["Aziz_He", "LJ_OT", "LI", "NA", "K", "RB", "CS", "null", "Ag_gs", "Ag_Pi", "Ag_Sig", "Ba_gs", "Au"]
 
 
 def small_cfg():
@@ -60,3 +60,47 @@ def test_alkali_forms(elem):
     r = np.linspace(4.0, 10.0, 601)
     v = np.array([lib.orc_v_alkali_he(x, elem) for x in r])
     assert -5.0 < v.min() < 0.0 and 5.0 < r[v.argmin()] < 9.0
+
+
+def test_au_pins():
+    """V_impur.f90:2476-2497: V(Re) = -De exactly (s = 0); Select_pot's comment
+    for 'Au' (:671-673) gives r_cutoff = 1 A with umax = 6.645232E+04, the
+    form's own value there."""
+    lib = oracle.load()
+    assert lib.orc_v_au_he(4.124) == -20.301143
+    assert lib.orc_v_au_he(1.0) == pytest.approx(6.645232e4, rel=1e-6)
+    r = np.linspace(3.0, 8.0, 2001)
+    v = np.array([lib.orc_v_au_he(x) for x in r])
+    # the fitted polynomial puts the well within 0.1 % of -De and 0.05 A of Re
+    assert v.min() == pytest.approx(-20.301143, rel=1e-3) and r[v.argmin()] == pytest.approx(4.124, abs=0.05)
+
+
+def test_ba_pins():
+    """V_impur.f90:1194-1210: the flat core (1297.1 K up to 3.7 A) meets the
+    inverse-power fit there; a shallow well (a few K) near 7 A; the leading
+    x^-6 and x^-8 terms far out."""
+    lib = oracle.load()
+    assert lib.orc_v_ba_he(3.7) == 1297.1
+    assert lib.orc_v_ba_he(3.7 * (1 + 1e-12)) == pytest.approx(1297.1, rel=1e-5)
+    r = np.linspace(4.0, 12.0, 1601)
+    v = np.array([lib.orc_v_ba_he(x) for x in r])
+    assert -5.0 < v.min() < -2.0 and 6.0 < r[v.argmin()] < 8.0
+    x = 200.0  # the two leading terms; the x^-10 one is 1.5e-5 of them here
+    assert lib.orc_v_ba_he(x) == pytest.approx(-450294.6878721156 / x**6 + 4.900282758445466e7 / x**8, rel=1e-4)
+
+
+@pytest.mark.parametrize("state,c6", [(0, 137042.07), (1, 0.21661134e6), (2, 1.97443e-9)])
+def test_ag_pins(state, c6):
+    """V_impur.f90:1035-1092: A at r = 0; undamped dispersion beyond D, so far
+    out the C6..C12 series alone; an attractive well between the core and
+    the tail."""
+    lib = oracle.load()
+    A = [78741.3877, 0.7095092e6, 40005.2][state]
+    assert lib.orc_v_ag_he(0.0, state) == A
+    c8, c10, c12 = [(189386.217, 111358462.0, 1.17670377e10), (123454.7952, 0.307155024e6, 0.740464032e-10),
+                    (3.37393e-6, 0.00788363, 7.52624e12)][state]
+    r = 40.0
+    assert lib.orc_v_ag_he(r, state) == pytest.approx(-(c6 / r**6 + c8 / r**8 + c10 / r**10 + c12 / r**12), rel=1e-9)
+    rr = np.linspace(2.0, 14.0, 4001)
+    v = np.array([lib.orc_v_ag_he(x, state) for x in rr])
+    assert v.min() < 0.0 and rr[v.argmin()] < 10.0
