@@ -147,6 +147,12 @@ struct he4g_run {
   std::vector<cudaEvent_t> pool;
   double fam_ms[F_COUNT] = {};
   long long fam_launches[F_COUNT] = {};
+  // asynchronous readback of psi (he4g_get_psi_async): a device snapshot,
+  // a copy stream and two events, created on first use
+  double2* psi_stage = nullptr;
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev_snap = nullptr, ev_copied = nullptr;
+  bool copy_pending = false;
 };
 
 namespace {
@@ -1157,6 +1163,12 @@ void he4g_destroy(he4g_run* r) {
   }
   for (auto e : r->pool) cudaEventDestroy(e);
   for (auto& g : r->graphs) cudaGraphExecDestroy(g.exec);
+  if (r->cs) {
+    cudaStreamSynchronize(r->cs);
+    cudaStreamDestroy(r->cs);
+  }
+  if (r->ev_snap) cudaEventDestroy(r->ev_snap);
+  if (r->ev_copied) cudaEventDestroy(r->ev_copied);
   for (void* p : r->allocs) cudaFree(p);
   if (r->s) cudaStreamDestroy(r->s);
   delete r;
@@ -1552,6 +1564,42 @@ int he4g_get_psi(he4g_run* r, double* psi) {
   cudaError_t e = cudaMemcpyAsync(psi, src, sizeof(double2) * r->g.n, cudaMemcpyDeviceToHost, r->s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
   return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "get_psi");
+}
+
+int he4g_get_psi_async(he4g_run* r, double* psi) {
+  if (!r || !psi) return HE4G_EINVAL;
+  cudaError_t e = cudaSuccess;
+  if (!r->cs) {
+    e = cudaStreamCreateWithFlags(&r->cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_snap, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_copied, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(r, e, "get_psi_async");
+  }
+  // an FP64 snapshot that no other call writes (the df64 form converts into it)
+  if (!r->psi_stage && !(r->psi_stage = dalloc<double2>(r, r->g.n, false)))
+    return fail(r, HE4G_ENOMEM, "get_psi_async: no memory for the snapshot of psi");
+  double2* stage = r->psi_stage;
+  // the snapshot may not overwrite a copy still in flight
+  if (r->copy_pending) cudaStreamWaitEvent(r->s, r->ev_copied, 0);
+  if (dfm(r))
+    launch_df_to_f64(reinterpret_cast<const df64*>(r->psi), reinterpret_cast<double*>(stage), 2 * r->g.n, r->s);
+  else
+    e = cudaMemcpyAsync(stage, r->psi, sizeof(double2) * r->g.n, cudaMemcpyDeviceToDevice, r->s);
+  if (e == cudaSuccess) e = cudaEventRecord(r->ev_snap, r->s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(r->cs, r->ev_snap, 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(psi, stage, sizeof(double2) * r->g.n, cudaMemcpyDeviceToHost, r->cs);
+  if (e == cudaSuccess) e = cudaEventRecord(r->ev_copied, r->cs);
+  if (e != cudaSuccess) return cuda_fail(r, e, "get_psi_async");
+  r->copy_pending = true;
+  return HE4G_OK;
+}
+
+int he4g_wait_psi(he4g_run* r) {
+  if (!r) return HE4G_EINVAL;
+  if (!r->copy_pending) return HE4G_OK;
+  const cudaError_t e = cudaEventSynchronize(r->ev_copied);
+  r->copy_pending = false;
+  return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "wait_psi");
 }
 
 int he4g_get_den(he4g_run* r, double* den) {

@@ -208,6 +208,18 @@ class Run:
         self._ck(self.lib.he4g_get_psi(self.h, abi.dptr(out)))
         return out
 
+    def get_psi_async(self, out):
+        """Starts copying psi into `out` (a complex128 array of the grid's
+        shape, pinned for the copy to overlap the next steps) and returns;
+        wait_psi() waits for it. `out` must stay alive until then."""
+        if out.dtype != np.complex128 or out.size != self.cfg.nx * self.cfg.ny * self.cfg.nz or \
+                not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out: a contiguous complex128 array of nx*ny*nz values")
+        self._ck(self.lib.he4g_get_psi_async(self.h, abi.dptr(out)))
+
+    def wait_psi(self):
+        self._ck(self.lib.he4g_wait_psi(self.h))
+
     @property
     def den(self):
         out = np.empty(self.shape)

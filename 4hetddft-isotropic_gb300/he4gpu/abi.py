@@ -94,6 +94,8 @@ SIGNATURES = {
     "he4g_step": (C.c_int, [_P, C.c_int, _D, _D]),
     "he4g_get_trajectory": (C.c_int, [_P, _D, C.c_int, C.POINTER(C.c_int)]),
     "he4g_get_psi": (C.c_int, [_P, _D]),
+    "he4g_get_psi_async": (C.c_int, [_P, _D]),
+    "he4g_wait_psi": (C.c_int, [_P]),
     "he4g_get_den": (C.c_int, [_P, _D]),
     "he4g_get_field": (C.c_int, [_P, C.c_int, _D]),
     "he4g_get_impurity": (C.c_int, [_P, _D, _D, _D]),

@@ -272,6 +272,18 @@ long long he4g_launch_count(const he4g_run* run);
 int he4g_get_trajectory(he4g_run* run, double* rows, int cap, int* n);
 
 int he4g_get_psi(he4g_run* run, double* psi);  /* 2*nx*ny*nz doubles */
+
+/* psi without waiting: a device snapshot of psi is taken in stream order
+ * after the work already issued on the run, and its copy into psi (pinned
+ * host memory, 2*nx*ny*nz doubles, left untouched until the copy lands) runs
+ * on a copy stream while the next steps compute. A later call waits on the
+ * device, not the host, for the previous copy before it takes its snapshot.
+ * The first call allocates the snapshot (16*nx*ny*nz bytes) and the copy
+ * stream. The reference's driver reads psi between steps (the printoutc
+ * dumps of DFT4He3d.f90:972-994); this lets those reads overlap the loop. */
+int he4g_get_psi_async(he4g_run* run, double* psi);
+/* Waits until the copy of the last he4g_get_psi_async has landed. */
+int he4g_wait_psi(he4g_run* run);
 int he4g_get_den(he4g_run* run, double* den);  /* nx*ny*nz doubles   */
 
 /* Field readback for checks: which = 0 pot4, 1 dencg, 2 delj4, 3 uimp,
