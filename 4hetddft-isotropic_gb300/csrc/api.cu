@@ -1060,12 +1060,16 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   }
   if (dev_tables) {
     const double bf = he4g_setup::bforce_ot(c.eps4, c.sigma4, c.h4);
+    // den is not yet in use (set_state fills it): scratch for the radial
+    // form factor of cubic grids, (3 (n/2)^2 + 1) doubles <= n^3 floats
+    void* scratch = r->rs * (size_t)g.n >= radial_scratch_bytes(c.nx) ? r->den : nullptr;
     if (launch_build_tables(dfm(r) ? 2 : mixed(r) ? 1 : 0, c.nx, c.ny, c.nz, g.hx, g.hy, g.hz, bf, 8.0 * c.eps4,
                             std::pow(c.sigma4, 6), c.h4, c.hcg, c.l_alpha, r->fvlj4, r->wcgk,
-                            fn.otc ? r->kalfs : nullptr, r->s) != 0) {
+                            fn.otc ? r->kalfs : nullptr, scratch, r->s) != 0) {
       he4g_destroy(r);
       return HE4G_ECUDA;
     }
+    if (scratch) cudaMemsetAsync(r->den, 0, r->rs * (size_t)g.n, r->s);  // den reads zero until set_state
   } else {
     upload_field(r, r->fvlj4, fvlj4, nh);
     upload_field(r, r->wcgk, wcgk, nh);

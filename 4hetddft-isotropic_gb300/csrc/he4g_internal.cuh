@@ -108,10 +108,13 @@ int launch_finish_pc(const double* partials, int nblocks, const PcFinish& fin, c
 int launch_finish_force(const double* partials, int nblocks, const ForceFinish& fin, cudaStream_t s);
 
 // Device set-up of a run's k-space tables (setup_dev.cu) in the run's table
-// type (prec: 0 FP64, 1 FP32, 2 df64); kalfs may be NULL. 0 on success.
+// type (prec: 0 FP64, 1 FP32, 2 df64); kalfs may be NULL. scratch (device,
+// radial_scratch_bytes(nx) bytes, may be NULL) holds the radial form factor
+// of cubic grids while the kernels run. 0 on success.
+size_t radial_scratch_bytes(int n);
 int launch_build_tables(int prec, int nx, int ny, int nz, double hx, double hy, double hz, double bf, double aux1,
                         double sigma6, double h4, double hcg, double l_alpha, void* fvlj4, void* wcgk, void* kalfs,
-                        cudaStream_t s);
+                        void* scratch, cudaStream_t s);
 
 // Tile shapes of the line passes, chosen per run (he4g_autotune): lines per
 // block of the generic x passes, log2 of the kx columns per generic y/z

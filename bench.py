@@ -192,12 +192,12 @@ class ClockSampler:
 TILES = None  # fixed FFT tiles (profiling runs) instead of autotuning
 
 
-def make_run(prec=FP64):
+def make_run(prec=FP64, device_tables=False):
     import he4gpu
     psi, r, v, meta = he4gpu.collision_case(CASE)
     kw, tk = he4gpu.config_for_case(meta)
     cfg = he4gpu.default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], precision=prec, **kw)
-    run = he4gpu.Run(cfg, selec=tk["selec"], r_cutoff=tk["r_cutoff"], umax=tk["umax"])
+    run = he4gpu.Run(cfg, selec=tk["selec"], r_cutoff=tk["r_cutoff"], umax=tk["umax"], device_tables=device_tables)
     if TILES:
         run.tiles = TILES
     else:
@@ -532,6 +532,32 @@ def form_measure(args, run64, barrier, gpu, prec):
             "clocks": res["clocks"], "vs_fp64": dev}
 
 
+def aux_pass(args):
+    """Profiling runs only: the kernels off the steady predictor-corrector
+    step, once per arithmetic form on the workload's grid: the device set-up
+    of the k-space tables, set_state (conversions, density, first
+    evaluation), the three Runge-Kutta-Gill steps and two predictor-corrector
+    steps, the energies and observables, and an asynchronous psi read. Prints
+    one JSON line of the forms' energies; times nothing."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(0)
+    out = {}
+    for prec in (FP64, MIXED, DF64):
+        run, cfg, psi, r, v, meta = make_run(prec, device_tables=True)
+        run.set_state(psi, r, v)
+        run.step(5)
+        e = run.energy()
+        run.observables(meta["n4"])
+        buf = np.empty(run.shape, dtype=np.complex128)
+        run.get_psi_async(buf)
+        run.wait_psi()
+        out[FORM_NAME[prec]] = {"etot": e["etot"], "steps": run.steps_taken}
+        run.close()
+    print(json.dumps({"aux": out, "workload": CASE}), flush=True)
+    return 0
+
+
 def main():
     if len(sys.argv) >= 2 and sys.argv[1] == "--cpu-sample":
         if len(sys.argv) > 4:
@@ -549,6 +575,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision block")
     ap.add_argument("--no-df64", action="store_true", help="skip the df64 block")
     ap.add_argument("--case", default=CASE, help="workload (profiling runs use smaller ones)")
+    ap.add_argument("--aux", action="store_true",
+                    help="profiling runs: set-up, Runge-Kutta, energy and readback kernels of every form, untimed")
     ap.add_argument("--tiles", default=None,
                     help="FFT tiles lpb_r2c,lpb_c2r,log2cols_y,log2cols_z instead of autotuning (profiling runs)")
     args = ap.parse_args()
@@ -558,6 +586,8 @@ def main():
         TILES = tuple(int(t) for t in args.tiles.split(","))
     if args.impl == "reference":
         return reference_arm(args)
+    if args.aux:
+        return aux_pass(args)
     return ours(args)
 
 
