@@ -16,6 +16,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(ROOT, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libhe4g.so")
+DRIVER_SRC = os.path.join(ROOT, "host", "he4g_driver.cpp")
+DRIVER = os.path.join(OUT_DIR, "he4g_driver")
 SOURCES = ["fft_reg_df.cu", "fft_reg.cu", "fft_xy.cu", "api.cu", "field.cu", "fieldmp.cu", "fielddf.cu", "fft.cu", "setup.cpp", "setup_dev.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -50,9 +52,30 @@ def _stale():
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
+def build_driver(force=False):
+    """The native host driver (host/he4g_driver.cpp), linked against
+    libhe4g.so with an rpath to its directory; returns its path."""
+    if not force and os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(
+            os.path.getmtime(DRIVER_SRC), os.path.getmtime(LIB)):
+        return DRIVER
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("no C++ compiler for the host driver")
+    inc = os.path.join(os.path.dirname(ROOT), "include")
+    cmd = [cxx, "-O2", "-std=c++17", "-I", inc, DRIVER_SRC, "-o", DRIVER + ".tmp", "-L", OUT_DIR, "-lhe4g",
+           "-Wl,-rpath,$ORIGIN", "-Wl,--allow-shlib-undefined"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host driver build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return DRIVER
+
+
 def build(force=False, verbose=False):
-    """Compiles and links libhe4g.so if any source is newer; returns its path."""
+    """Compiles and links libhe4g.so if any source is newer, then the host
+    driver; returns the library's path."""
     if not force and not _stale():
+        build_driver()
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     objdir = os.path.join(OUT_DIR, "obj")
@@ -70,6 +93,7 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver(force=True)
     return LIB
 
 
