@@ -150,10 +150,40 @@ double au_he(double rr) {
   return -De * (1.0 + s * poly) * std::exp(-a[0] * s);
 }
 
+// Alkali ion-He of Koutselos, Mason and Viehland (J. Chem. Phys. 93, 7125,
+// 1990; V_impur.f90:1701-1880): Born-Mayer exchange plus the C4/C6/C8
+// series damped by exp(-(1.28 R_m / x - 1)^2) inside x = 1.28 R_m, in atomic
+// units (x in bohr), returned in K. Rows Na+, K+, Rb+, Cs+: v0, rho, R_m, C4,
+// C6, C8; the reduced Born-Mayer constants and the He polarisabilities are
+// shared.
+double koutselos(double xx, int ion) {
+  static const double P[4][6] = {{0.2063, 0.7640, 4.55, 0.0, 1.424, 13.17},
+                                 {0.2690, 0.8589, 5.49, 0.0, 5.83, 72.05},
+                                 {0.3474, 0.8868, 5.85, 0.0, 8.8, 126.2},
+                                 {0.5092, 0.9241, 6.38, 0.0, 13.69, 236.4}};
+  const double bohr = 0.529177, hartree = 27.2114, ev_to_k = 11604.448;
+  const double A = 146.98, a = 1.5024, B = 70.198, b = 1.4041;
+  const double alpha_d = 1.3831, alpha_q = 2.4434, alpha_o = 10.614;
+  const double* p = P[ion];
+  const double c4 = p[3] + alpha_d / 2.0, c6 = p[4] + alpha_q / 2.0, c8 = p[5] + alpha_o / 2.0;
+  const double x = xx / bohr, rs = x / p[1];
+  const double exch = p[0] * (A * std::exp(-a * rs) - B * std::exp(-b * rs));
+  const double xd = p[2] * 1.28;
+  double damp = 1.0;
+  if (x < xd) damp = x != 0.0 ? std::exp(-(xd / x - 1.0) * (xd / x - 1.0)) : 0.0;
+  double v = exch;
+  if (x != 0.0) {
+    const double x2 = x * x, x4 = x2 * x2, x6 = x4 * x2, x8 = x6 * x2;
+    v = v + (-c4 / x4 - c6 / x6 - c8 / x8) * damp;
+  }
+  return v * hartree * ev_to_k;
+}
+
 int pot_kind(const char* selec) {
-  static const char* names[] = {"Xe_He", "Ar_He", "Aziz_He", "LJ_OT", "LI",    "NA",     "K",     "RB",
-                                "CS",    "null",  "Ag_gs",   "Ag_Pi", "Ag_Sig", "Ba_gs", "Au"};
-  for (int k = 0; k < 15; ++k)
+  static const char* names[] = {"Xe_He", "Ar_He", "Aziz_He", "LJ_OT", "LI", "NA", "K", "RB", "CS", "null",
+                                "Ag_gs", "Ag_Pi", "Ag_Sig", "Ba_gs", "Au", "Na_plus_Koutselos",
+                                "K_plus_Koutselos", "Rb_plus_Koutselos", "Cs_plus_Koutselos"};
+  for (int k = 0; k < 19; ++k)
     if (std::strcmp(selec, names[k]) == 0) return k;
   return -1;
 }
@@ -170,6 +200,7 @@ double v_pair(const char* selec, double r, double r_cutoff, double umax) {
     case 10: case 11: case 12: return ag_he(r, kind - 10);
     case 13: return ba_he(r);
     case 14: return au_he(r);
+    case 15: case 16: case 17: case 18: return koutselos(r, kind - 15);
     default: return tang_toennies(r, 74.9002, 1.8175, 21.5674, 430.148, 10610.21);
   }
 }

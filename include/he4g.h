@@ -123,7 +123,8 @@ void he4g_default_config(he4g_config* cfg, int nx, int ny, int nz, double xmax, 
  * potenimpini.f90:11-27 + V_impur.f90 Select_Pot (radial impurity table).
  * selec (Select_pot names of V_impur.f90): "Xe_He", "Ar_He", "Aziz_He",
  * "LJ_OT", "LI", "NA", "K", "RB", "CS", "Ag_gs", "Ag_Pi", "Ag_Sig", "Ba_gs",
- * "Au" or "null"; others give HE4G_EINVAL.
+ * "Au", "Na_plus_Koutselos", "K_plus_Koutselos", "Rb_plus_Koutselos",
+ * "Cs_plus_Koutselos" or "null"; others give HE4G_EINVAL.
  * Output half-grid arrays hold (nx/2+1)*ny*nz
  * doubles; potion holds cfg->npot doubles; kalfs may be NULL. */
 int he4g_build_tables(const he4g_config* cfg, const char* selec, double r_cutoff, double umax,

@@ -420,6 +420,34 @@ double orc_v_au_he(double rr) {
   return -De * (1.0 + s * poly) * exp(-a[0] * s);
 }
 
+/* alkali ion-He of Koutselos et al., J. Chem. Phys. 93, 7125 (1990)
+   (V_impur.f90:1701-1880): a Born-Mayer exchange term plus the damped
+   C4/C6/C8 induction-dispersion series, atomic units converted to K;
+   ion 0 Na+, 1 K+, 2 Rb+, 3 Cs+ */
+double orc_v_koutselos(double xx, int ion) {
+  static const double P[4][6] = {/* v0, rho, R_m, C4, C6, C8 */
+                                 {0.2063, 0.7640, 4.55, 0.0, 1.424, 13.17},
+                                 {0.2690, 0.8589, 5.49, 0.0, 5.83, 72.05},
+                                 {0.3474, 0.8868, 5.85, 0.0, 8.8, 126.2},
+                                 {0.5092, 0.9241, 6.38, 0.0, 13.69, 236.4}};
+  const double a_bohr = 0.529177, hartree = 27.2114, ev_k = 11604.448;
+  const double A = 146.98, a_a = 1.5024, B = 70.198, b_b = 1.4041;
+  const double a_d = 1.3831, a_q = 2.4434, a_o = 10.614;
+  const double* q = P[ion];
+  const double cc4 = q[3] + a_d / 2.0, cc6 = q[4] + a_q / 2.0, cc8 = q[5] + a_o / 2.0;
+  const double x = xx / a_bohr, rs = x / q[1];
+  const double v_ex = q[0] * (A * exp(-a_a * rs) - B * exp(-b_b * rs));
+  const double aux = q[2] * 1.28;
+  double damp = 1.0;
+  if (x < aux) damp = x != 0.0 ? exp(-(aux / x - 1.0) * (aux / x - 1.0)) : 0.0;
+  double sto = v_ex;
+  if (x != 0.0) {
+    const double x2 = x * x, x4 = x2 * x2, x6 = x4 * x2, x8 = x6 * x2;
+    sto = sto + (-cc4 / x4 - cc6 / x6 - cc8 / x8) * damp;
+  }
+  return sto * hartree * ev_k;
+}
+
 /* Select_pot (V_impur.f90): umax inside r_cutoff; 'null' is zero everywhere */
 double orc_select_pot(const char* selec, double r, double r_cutoff, double umax) {
   if (strcmp(selec, "null") == 0) return 0.0;
@@ -432,6 +460,9 @@ double orc_select_pot(const char* selec, double r, double r_cutoff, double umax)
   if (strcmp(selec, "Ag_Sig") == 0) return orc_v_ag_he(r, 2);
   if (strcmp(selec, "Ba_gs") == 0) return orc_v_ba_he(r);
   if (strcmp(selec, "Au") == 0) return orc_v_au_he(r);
+  static const char* ions[4] = {"Na_plus_Koutselos", "K_plus_Koutselos", "Rb_plus_Koutselos", "Cs_plus_Koutselos"};
+  for (int k = 0; k < 4; ++k)
+    if (strcmp(selec, ions[k]) == 0) return orc_v_koutselos(r, k);
   static const char* alk[5] = {"LI", "NA", "K", "RB", "CS"};
   for (int k = 0; k < 5; ++k)
     if (strcmp(selec, alk[k]) == 0) return orc_v_alkali_he(r, k);

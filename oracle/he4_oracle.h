@@ -33,6 +33,7 @@ double orc_v_alkali_he(double r, int elem);
 double orc_v_ag_he(double r, int state);
 double orc_v_ba_he(double r);
 double orc_v_au_he(double r);
+double orc_v_koutselos(double r, int ion);
 double orc_select_pot(const char* selec, double r, double r_cutoff, double umax);
 double orc_bforce(double eps, double sigma, double hc);
 

@@ -49,6 +49,7 @@ def load():
         "orc_v_ag_he": (C.c_double, [C.c_double, C.c_int]),
         "orc_v_ba_he": (C.c_double, [C.c_double]),
         "orc_v_au_he": (C.c_double, [C.c_double]),
+        "orc_v_koutselos": (C.c_double, [C.c_double, C.c_int]),
         "orc_select_pot": (C.c_double, [C.c_char_p, C.c_double, C.c_double, C.c_double]),
         "orc_bforce": (C.c_double, [C.c_double, C.c_double, C.c_double]),
         "orc_create": (P, [P, _D, _D, _D, _D]),

@@ -7,7 +7,8 @@ import pytest
 import he4gpu
 from oracle import oracle
 
-NEW = ["Aziz_He", "LJ_OT", "LI", "NA", "K", "RB", "CS", "null", "Ag_gs", "Ag_Pi", "Ag_Sig", "Ba_gs", "Au"]
+NEW = ["Aziz_He", "LJ_OT", "LI", "NA", "K", "RB", "CS", "null", "Ag_gs", "Ag_Pi", "Ag_Sig", "Ba_gs", "Au",
+       "Na_plus_Koutselos", "K_plus_Koutselos", "Rb_plus_Koutselos", "Cs_plus_Koutselos"]
 
 
 def small_cfg():
@@ -104,3 +105,23 @@ def test_ag_pins(state, c6):
     rr = np.linspace(2.0, 14.0, 4001)
     v = np.array([lib.orc_v_ag_he(x, state) for x in rr])
     assert v.min() < 0.0 and rr[v.argmin()] < 10.0
+
+
+def test_koutselos_ions_meet_the_reference_values():
+    """Select_pot's comments (V_impur.f90:240-243, 277-280) give the values at
+    the cores the reference ran with: Na+ umax = 9.012825d4 at r_cutoff = 1 A;
+    K+ 1.8628633412d5 at 1 A and 3.2762532479d3 at 2 A."""
+    lib = oracle.load()
+    assert lib.orc_v_koutselos(1.0, 0) == pytest.approx(9.012825e4, rel=1e-7)
+    assert lib.orc_v_koutselos(1.0, 1) == pytest.approx(1.8628633412e5, rel=1e-10)
+    assert lib.orc_v_koutselos(2.0, 1) == pytest.approx(3.2762532479e3, rel=1e-10)
+
+
+@pytest.mark.parametrize("ion", range(4))
+def test_koutselos_wells(ion):
+    """Ion-He wells of a few hundred K between 2 and 4 A (the polarisation
+    attraction of a bare ion), deepest for the smallest ion."""
+    lib = oracle.load()
+    r = np.linspace(1.5, 8.0, 2601)
+    v = np.array([lib.orc_v_koutselos(x, ion) for x in r])
+    assert -500.0 < v.min() < -100.0 and 2.0 < r[v.argmin()] < 4.0
