@@ -78,6 +78,17 @@ module he4g_c
       type(c_ptr), value :: run
       complex(c_double_complex), intent(out) :: psi(*)
     end function
+    ! psi into pinned host memory without waiting (the copy overlaps the next
+    ! steps); psi must not be touched before he4g_wait_psi returns
+    integer(c_int) function he4g_get_psi_async(run, psi) bind(C, name="he4g_get_psi_async")
+      import
+      type(c_ptr), value :: run
+      complex(c_double_complex), intent(inout) :: psi(*)
+    end function
+    integer(c_int) function he4g_wait_psi(run) bind(C, name="he4g_wait_psi")
+      import
+      type(c_ptr), value :: run
+    end function
     integer(c_int) function he4g_get_den(run, den) bind(C, name="he4g_get_den")
       import
       type(c_ptr), value :: run
