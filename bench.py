@@ -539,8 +539,9 @@ def aux_pass(args):
     step, once per arithmetic form on the workload's grid: the device set-up
     of the k-space tables, set_state (conversions, density, first
     evaluation), the three Runge-Kutta-Gill steps and two predictor-corrector
-    steps, the energies and observables, and an asynchronous psi read. Prints
-    one JSON line of the forms' energies; times nothing."""
+    steps, the energies and observables, an asynchronous psi read and (FP64)
+    the allocation-free force on caller-owned arrays. Prints one JSON line of
+    the forms' energies; times nothing."""
     import numpy as np
     import torch
     torch.cuda.set_device(0)
@@ -554,6 +555,17 @@ def aux_pass(args):
         buf = np.empty(run.shape, dtype=np.complex128)
         run.get_psi_async(buf)
         run.wait_psi()
+        if prec == FP64:  # the force on caller-owned arrays, without allocation
+            import ctypes
+            den = torch.from_numpy(run.den).to("cuda")
+            uimp = torch.from_numpy(run.field("uimp")).to("cuda")
+            force = torch.empty(3, dtype=torch.float64, device="cuda")
+            if run.lib.he4g_forceimp_noalloc(ctypes.c_void_p(den.data_ptr()), ctypes.c_void_p(uimp.data_ptr()),
+                                             cfg.nx, cfg.ny, cfg.nz, cfg.xmax, cfg.ymax, cfg.zmax,
+                                             ctypes.c_void_p(force.data_ptr()),
+                                             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)):
+                raise RuntimeError("he4g_forceimp_noalloc failed")
+            torch.cuda.synchronize()
         out[FORM_NAME[prec]] = {"etot": e["etot"], "steps": run.steps_taken}
         run.close()
     print(json.dumps({"aux": out, "workload": CASE}), flush=True)
