@@ -1,8 +1,8 @@
 /*
  * he4_oracle.c — FP64 CPU restatement of the reference time step.
  *
- * TEST INFRASTRUCTURE ONLY (see he4_oracle.h): the checker for the GPU
- * library and the timed CPU baseline. Written from the mathematics of the
+ * TEST INFRASTRUCTURE ONLY (see he4_oracle.h): the reference the GPU
+ * library's results are compared with, and the timed CPU baseline. Written from the mathematics of the
  * cited reference files; each routine names the file:line it restates.
  *
  * Build: oracle/Makefile (gcc -O2 -fopenmp -ffp-contract=off, so that x86

@@ -1,7 +1,8 @@
 """ctypes binding of the FP64 CPU oracle (oracle/he4_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU legs of bench.py as the checker / CPU baseline; the GPU library never
+CPU legs of bench.py, to compare the GPU results with and as the CPU
+baseline; the GPU library never
 uses it. `build()` compiles it with oracle/Makefile into oracle/_build/.
 """
 import ctypes as C
