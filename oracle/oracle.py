@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU legs of bench.py, to compare the GPU results with and as the CPU
-baseline; the GPU library never
-uses it. `build()` compiles it with oracle/Makefile into oracle/_build/.
+baseline; the GPU library never uses it. `build()` compiles it with
+oracle/Makefile into oracle/_build/.
 """
 import ctypes as C
 import os
