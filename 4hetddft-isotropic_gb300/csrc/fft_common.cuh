@@ -582,6 +582,15 @@ __device__ __forceinline__ float penalty_f32(float x, float bd, float cs) {
   return (cs * 2.f * e * inv) * (1.f + 2.f * bd * inv);
 }
 
+// The FP64 tanh branch of the df64 penalty (densities near the solid
+// threshold, which a droplet never reaches), kept out of line: inlined into
+// every unrolled epilogue point it would swell the kernels' code, and the
+// instruction fetches would stall the common FP32 branch.
+static __device__ __noinline__ double penalty_fp64_tanh(double x, double bd, double cs) {
+  const double t = tanh(x);
+  return cs * (1.0 + t + bd * (1.0 - t * t));
+}
+
 template <typename R>
 __device__ __forceinline__ R solid_penalty(R d, R beta, R dm, R cs) {
   const R x = beta * (d - dm);
@@ -595,9 +604,7 @@ __device__ __forceinline__ R solid_penalty(R d, R beta, R dm, R cs) {
       const float bd = (beta * d).hi;
       return df64((cs.hi * 2.f * e * inv) * (1.f + 2.f * bd * inv));
     }
-    const double t = tanh(df_to_double(x));
-    const double p = df_to_double(cs) * (1.0 + t + df_to_double(beta * d) * (1.0 - t * t));
-    return df_split(p);
+    return df_split(penalty_fp64_tanh(df_to_double(x), df_to_double(beta * d), df_to_double(cs)));
   } else {
     if (x < -10.0) {
       const float e = expf(2.f * (float)x);
