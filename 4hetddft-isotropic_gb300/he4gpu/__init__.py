@@ -39,6 +39,19 @@ def default_config(nx, ny, nz, xmax, ymax=None, zmax=None, **overrides):
     return cfg
 
 
+def reference_config(nx, ny, nz, xmax, ymax=None, zmax=None, **overrides):
+    """default_config computed in Python (abi.reference_defaults) without
+    loading libhe4g.so: for processes that only run the CPU oracle."""
+    ymax = xmax if ymax is None else ymax
+    zmax = xmax if zmax is None else zmax
+    cfg = abi.reference_defaults(nx, ny, nz, xmax, ymax, zmax)
+    for k, v in overrides.items():
+        if not hasattr(cfg, k):
+            raise KeyError(k)
+        setattr(cfg, k, v)
+    return cfg
+
+
 def footprint(cfg):
     """Device bytes a run of this configuration allocates (he4g_footprint)."""
     lib = abi.load()

@@ -70,6 +70,30 @@ class Obs(C.Structure):
                 ("ang_im", C.c_double * 3), ("r2", C.c_double * 3)]
 
 
+def reference_defaults(nx, ny, nz, xmax, ymax, zmax):
+    """The values he4g_default_config fills, computed here without loading
+    libhe4g.so, for processes that must not map the GPU library (the CPU
+    timing of the oracle). The module defaults of modules.f90 (he4 :138-148,
+    lenard4 :209-212, deriva :27-33), the absorber of the shipped input
+    (input_files/xe-he1000-hoc-200mps.input:2-4), h_cg = 1.065 h4 for
+    lsolid (DFT4He3d.f90:579-586) and the table size of potenimpini.f90:13-16.
+    tests/test_abi.py holds it equal to the library's, field by field."""
+    c = Config()
+    c.nx, c.ny, c.nz = nx, ny, nz
+    c.npd, c.icon, c.core, c.lsolid, c.lrk, c.precision = 13, 13, CORE_OT, 1, 0, PREC_FP64
+    c.xmax, c.ymax, c.zmax, c.deltat = xmax, ymax, zmax, 0.0
+    c.cp4, c.cpp4, c.h2o2m4 = -2.41186e4, 1.85850e6, 6.05969638298
+    c.alphas, c.l_alpha, c.den0s = 54.31, 1.0, 0.04
+    c.c_solid, c.beta_solid, c.den_m = 3.1577504e4, 40.0, 0.37
+    c.eps4, c.sigma4, c.h4 = 10.22, 2.556, 2.190323
+    c.hcg = 2.190323 * 1.065
+    c.lambdah, c.txmean, c.txsurf, c.tymean, c.tysurf, c.tzmean, c.tzsurf = 2.0, 1000.0, 2.0, 1000.0, 2.0, 49.2, 2.0
+    c.mimpur = 131.29
+    c.npot = 100 * max(nx, ny, nz) + 1
+    c.delinter = 4.0 * max(xmax, ymax, zmax) / float(c.npot - 1)
+    return c
+
+
 _D = C.POINTER(C.c_double)
 _P = C.c_void_p
 

@@ -190,6 +190,7 @@ class ClockSampler:
 
 
 TILES = None  # fixed FFT tiles (profiling runs) instead of autotuning
+CPU_SAMPLE_STEPS = 20  # predictor-corrector steps of the oracle in cpu_baseline (median)
 
 
 def make_run(prec=FP64, device_tables=False):
@@ -241,13 +242,15 @@ def e2e_measure(run, psi, steps):
 
 
 def cpu_sample(kind_steps):
-    """Times predictor-corrector steps of the FP64 CPU oracle at 256^3 (child
-    process, all host cores). Prints one JSON line."""
+    """Times predictor-corrector steps of the FP64 CPU oracle on the workload
+    (child process, all host cores). Prints one JSON line with every step's
+    time. The process never loads libhe4g.so: the configuration comes from
+    he4gpu.reference_config, the Python copy of he4g_default_config."""
     import he4gpu
     from oracle import oracle
     psi, r, v, meta = he4gpu.collision_case(CASE)
     kw, tk = he4gpu.config_for_case(meta)
-    cfg = he4gpu.default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], **kw)
+    cfg = he4gpu.reference_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], **kw)
     tabs = oracle.build_tables(cfg, tk["selec"], tk["r_cutoff"], tk["umax"])
     o = oracle.OracleRun(cfg, tabs)
     o.set_state(psi, r, v)
@@ -267,7 +270,8 @@ def cpu_sample(kind_steps):
         o.poten()
         o.forceimp()
         ts.append(time.perf_counter() - t0)
-    print(json.dumps({"sec_per_step": statistics.median(ts), "steps": steps, "cores": os.cpu_count()}))
+    print(json.dumps({"sec_per_step": statistics.median(ts), "sec_total": sum(ts), "steps": steps, "warmup": warm,
+                      "cores": os.cpu_count()}))
 
 
 def run_cpu_sample(warm, steps):
@@ -307,13 +311,6 @@ def case_grid(case):
     return list(n) if not isinstance(n, int) else [n, n, n]
 
 
-def l2_note(cfg):
-    n = cfg.nx * cfg.ny * cfg.nz
-    return (f"inputs larger than L2 (psi {16 * n / 1e6:.0f} MB, history {7 * 16 * n / 1e9:.2f} GB); no flush"
-            if 16 * n > 129e6 else
-            f"psi {16 * n / 1e6:.0f} MB, history {7 * 16 * n / 1e6:.0f} MB: the step's working set exceeds L2; no flush")
-
-
 def metric_name(case, prec=FP64):
     """The headline metric for the 256^3 collision; the same wording with the
     grid and system of any other workload."""
@@ -327,29 +324,48 @@ def metric_name(case, prec=FP64):
     return m if prec == FP64 else m.replace("FP64", FORM_NAME[prec])
 
 
-def reference_arm(args):
-    ws, rank, _ = dist_env()
-    if rank != 0:
-        return 0
-    # the reference's own Fortran program cannot be built (no Fortran compiler,
-    # no FFTW); its restatement (the FP64 oracle) is timed instead
-    warm = max(0, min(args.warmup, 2))
-    steps = max(1, min(args.steps, 8))
-    s = run_cpu_sample(warm, steps)
-    val = 1.0 / s["sec_per_step"]
+def workload_config(ws, prec=FP64):
+    """The `config` object of the JSON line; both arms print the same one."""
     import he4gpu
     c = he4gpu.initial.CASES[CASE]
     grid = case_grid(CASE)
+    n = grid[0] * grid[1] * grid[2]
+    psi_bytes = 16 * n
+    return {"workload": f"{CASE} {FORM_NAME[prec]} predictor-corrector step",
+            "grid": grid, "h": c["h"], "n4": c["n4"], "impurity": c["imp"],
+            "v_A_per_ps": c["v"], "impact_parameter": f"{c['b_frac']} R",
+            "l2": (f"inputs larger than L2 (psi {psi_bytes / 1e6:.0f} MB, history {7 * psi_bytes / 1e9:.2f} GB); "
+                   "no flush" if psi_bytes > 129e6 else
+                   f"psi {psi_bytes / 1e6:.0f} MB, history {7 * psi_bytes / 1e6:.0f} MB: the step's working set "
+                   "exceeds L2; no flush"),
+            "parallelism": f"replicas x{ws}"}
+
+
+def reference_arm(args):
+    """The reference's path on the host cores: its Fortran program cannot be
+    built (no Fortran compiler, no FFTW/MKL on either machine), so its FP64
+    restatement, the oracle, is timed: exactly args.warmup untimed and
+    args.steps timed predictor-corrector steps (each with the trailing
+    potential and force evaluation) of the same workload as the GPU arm, on
+    every host core. The timing process loads liboracle.so only."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    warm = max(0, args.warmup)
+    steps = max(1, args.steps)
+    s = run_cpu_sample(warm, steps)
+    val = steps / s["sec_total"]
+    grid = case_grid(CASE)
     line = {
         "impl": "reference", "metric": metric_name(CASE), "value": val, "unit": "steps/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * s["sec_per_step"],
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * s["sec_total"] / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Woods-Saxon droplet + Xe)",
-        "config": {"workload": CASE, "grid": grid, "h": c["h"], "n4": c["n4"], "impurity": c["imp"],
-                   "steps_timed": steps},
+        "config": workload_config(args.gpus),
         "cpu_baseline": {"value": val, "unit": "steps/s", "cores": s["cores"], "kind": "port",
-                         "sample": f"{steps} predictor-corrector steps of the FP64 C oracle at "
-                                   f"{'x'.join(map(str, grid))} (median), OpenMP over {s['cores']} cores"},
+                         "sample": f"{steps} predictor-corrector steps (after {warm} untimed) of the FP64 C oracle "
+                                   f"at {'x'.join(map(str, grid))}, OpenMP over {s['cores']} cores; median step "
+                                   f"{1e3 * s['sec_per_step']:.1f} ms"},
         "e2e": {"value": val, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -440,13 +456,27 @@ def ours(args):
             mixed_block = form_measure(args, run, barrier, local, MIXED)
         if prec == FP64 and ws == 1 and not args.no_df64:
             df64_block = form_measure(args, run, barrier, local, DF64)
+        cufft = None
+        if ws == 1 and not args.no_cufft:
+            try:
+                ours64 = fft_ms_per_evaluation(res["roofline"], args.steps) if prec == FP64 else None
+                ours32 = (mixed_block["fft_ms_per_evaluation"] if mixed_block else
+                          fft_ms_per_evaluation(res["roofline"], args.steps) if prec == MIXED else None)
+                cufft = {"what": "2 r2c + 3 c2r + 3 form-factor products per mean-field evaluation "
+                                 "(poten.f90:34-74) through cuFFT (torch.fft), against the library's own "
+                                 "FFT passes of one evaluation; comparison only, not on the library's path",
+                         "fp64": cufft_compare(cfg.nx, cfg.ny, cfg.nz, ours64, torch.float64),
+                         "fp32": cufft_compare(cfg.nx, cfg.ny, cfg.nz, ours32, torch.float32)}
+            except Exception as e:  # reported, not fatal
+                cufft = {"failed": f"{e}"[:300]}
         cpu = None
         if ws == 1 and not args.no_cpu:
             try:
-                s = run_cpu_sample(1, 2)
+                s = run_cpu_sample(1, CPU_SAMPLE_STEPS)
+                grid = "x".join(map(str, case_grid(CASE)))
                 cpu = {"value": 1.0 / s["sec_per_step"], "unit": "steps/s", "cores": s["cores"], "kind": "port",
-                       "sample": "2 predictor-corrector steps of the FP64 C oracle at 256^3 (median of 2, after 1 "
-                                 "warm-up), OpenMP over all host cores"}
+                       "sample": f"median of {CPU_SAMPLE_STEPS} predictor-corrector steps (after 1 untimed) of "
+                                 f"the FP64 C oracle at {grid}, OpenMP over {s['cores']} host cores"}
             except Exception as e:  # reported, not fatal
                 cpu = {"value": None, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
                        "sample": f"failed: {e}"[:300]}
@@ -457,11 +487,8 @@ def ours(args):
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": DTYPE[prec],
             "data": "synthetic (seeded Woods-Saxon droplet + Xe)",
-            "config": {"workload": f"{CASE} {FORM_NAME[prec]} predictor-corrector step",
-                       "grid": [cfg.nx, cfg.ny, cfg.nz], "h": meta["h"], "n4": meta["n4"], "impurity": meta["imp"],
-                       "v_A_per_ps": meta["v"], "impact_parameter": f"{meta['b_frac']} R",
-                       "l2": l2_note(cfg),
-                       "parallelism": f"replicas x{ws}", "fft_tiles": list(run.tiles)},
+            "config": workload_config(ws, prec),
+            "fft_tiles": list(run.tiles),
             "grid_point_updates_per_s": value * cfg.nx * cfg.ny * cfg.nz,
             "hbm_gbs": rf["step_gbs"],
             "roofline": rf,
@@ -477,6 +504,7 @@ def ours(args):
             "wall_s_timed": res["wall_s"],
             "mixed": mixed_block,
             "df64": df64_block,
+            "cufft_compare": cufft,
         }
     if dist:
         dist.barrier()
@@ -528,10 +556,79 @@ def form_measure(args, run64, barrier, gpu, prec):
     run.close()
     rf = res["roofline"]
     return {"value": args.steps / (ms * 1e-3), "unit": "steps/s", "ms_per_step": ms / args.steps,
+            "fft_ms_per_evaluation": fft_ms_per_evaluation(rf, args.steps),
             "dtype": FORM_DTYPE[prec],
             "fft_tiles": tiles,
             "hbm_gbs": rf["step_gbs"], "roofline": rf, "gpu_launches": res["launches"],
             "clocks": res["clocks"], "vs_fp64": dev}
+
+
+def fft_ms_per_evaluation(roofline, steps):
+    """Device time of the 3D FFT line passes of one mean-field evaluation
+    (two per step), from the per-family CUDA-event times of a timed run. The
+    passes include what is fused into them: the correlation prologue, the
+    form-factor products and the pot4 epilogue."""
+    ms = sum(f["ms_total"] for f in roofline["families"] if f["family"].startswith("fft_"))
+    return ms / (2 * steps)
+
+
+def cufft_compare(nx, ny, nz, ours_ms, real_dtype, reps=20):
+    """cuFFT (through torch.fft, timed only as a comparison: it is not on the
+    library's path) doing the transforms of one mean-field evaluation of
+    poten.f90:34-74 at the workload's grid: r2c of den, the products with the
+    coarse-graining and Lennard-Jones form factors and their two c2r, r2c of
+    the correlation field, its product and c2r (2 r2c + 3 c2r + 3 products,
+    the reference's FFTW sequence). CUDA events on torch's stream, after
+    warm-up; the inputs exceed L2 at 256^3. ours_ms: the library's own FFT
+    passes per evaluation (fused prologue/epilogue included)."""
+    import torch
+    dev = torch.device("cuda")
+    cdt = torch.complex128 if real_dtype == torch.float64 else torch.complex64
+    rb = 8 if real_dtype == torch.float64 else 4
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    shape = (nz, ny, nx)
+    den = torch.rand(shape, dtype=real_dtype, device=dev, generator=g)
+    corr = torch.rand(shape, dtype=real_dtype, device=dev, generator=g)
+    hshape = (nz, ny, nx // 2 + 1)
+    wcg = torch.rand(hshape, dtype=real_dtype, device=dev, generator=g)
+    vlj = torch.rand(hshape, dtype=real_dtype, device=dev, generator=g)
+    S = torch.empty(hshape, dtype=cdt, device=dev)
+    T = torch.empty(hshape, dtype=cdt, device=dev)
+    out = [torch.empty(shape, dtype=real_dtype, device=dev) for _ in range(3)]
+
+    def evaluation():
+        torch.fft.rfftn(den, out=S)
+        torch.mul(S, wcg, out=T)
+        torch.fft.irfftn(T, s=shape, out=out[0])
+        torch.mul(S, vlj, out=T)
+        torch.fft.irfftn(T, s=shape, out=out[1])
+        torch.fft.rfftn(corr, out=S)
+        torch.mul(S, wcg, out=T)
+        torch.fft.irfftn(T, s=shape, out=out[2])
+
+    for _ in range(3):
+        evaluation()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        evaluation()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    n, nh = nx * ny * nz, (nx // 2 + 1) * ny * nz
+    cb = 2 * rb
+    # each transform reads its input and writes its output once; each
+    # product reads a spectrum and a table and writes a spectrum
+    alg = 2 * (rb * n + cb * nh) + 3 * (cb * nh + rb * n) + 3 * (2 * cb * nh + rb * nh)
+    peak, kind = read_peaks()
+    del den, corr, wcg, vlj, S, T, out
+    torch.cuda.empty_cache()
+    return {"cufft_ms_per_evaluation": ms, "ours_ms_per_evaluation": ours_ms,
+            "ours_speedup_vs_cufft": ms / ours_ms if ours_ms else None,
+            "cufft_algorithmic_bytes": alg, "cufft_gbs": alg / (ms * 1e-3) / 1e9,
+            "cufft_hbm_frac": alg / (ms * 1e-3) / 1e9 / peak, "peak_source": kind}
 
 
 def aux_pass(args):
@@ -588,6 +685,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass (profiling runs)")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision block")
     ap.add_argument("--no-df64", action="store_true", help="skip the df64 block")
+    ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT comparison")
     ap.add_argument("--case", default=CASE, help="workload (profiling runs use smaller ones)")
     ap.add_argument("--aux", action="store_true",
                     help="profiling runs: set-up, Runge-Kutta, energy and readback kernels of every form, untimed")

@@ -1,6 +1,6 @@
 """Generates the golden fixtures that pin the oracle to the reference's own data.
 
-Run in a checkout that has the reference tree (default path below); the
+Run where the reference source tree is present, giving its path; the
 fixtures it writes are committed, so the tests never need the reference.
 
 * stencil_rows.json: the 13-point first- and second-derivative matrices the
@@ -13,7 +13,7 @@ fixtures it writes are committed, so the tests never need the reference.
   (V_impur.f90 comments for V_Xe_He(2.0) and V_Ar_He(2.0), the shipped input's
   umax = V_Xe_He(2.55), modules.f90's b4 against bforce), each with file:line.
 
-Usage: python tests/golden/make_golden.py [reference_dir]
+Usage: python tests/golden/make_golden.py <reference_dir>
 """
 import json
 import os
@@ -100,7 +100,9 @@ def to_float(entry):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference source tree>")
+    ref = sys.argv[1]
     A = parse_blockds(os.path.join(ref, "blockds.f"))
     out = {"source": "blockds.f via newder.f:99-128 (ICON=1) and redef.f:133-170 (ICON=13)"}
     for K, name in ((1, "d1"), (2, "d2")):

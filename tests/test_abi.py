@@ -43,6 +43,20 @@ def test_default_config_matches_reference_defaults(he4gpu_mod):
     assert cfg.delinter == 4.0 * 38.4 / (cfg.npot - 1)
 
 
+def test_python_defaults_equal_the_library(he4gpu_mod):
+    """abi.reference_defaults (used where libhe4g.so must not be loaded) fills
+    every field exactly as he4g_default_config does."""
+    from he4gpu import abi
+    for dims in ((256, 256, 256, 51.2, 51.2, 51.2), (40, 48, 64, 11.0, 13.2, 17.6), (32, 32, 32, 12.8, 12.8, 12.8)):
+        lib_cfg = he4gpu_mod.default_config(*dims)
+        py_cfg = abi.reference_defaults(*dims)
+        for k, _ in abi.Config._fields_:
+            assert getattr(py_cfg, k) == getattr(lib_cfg, k), k
+    a = he4gpu_mod.reference_config(128, 128, 128, 28.8, deltat=1e-5, mimpur=39.948)
+    b = he4gpu_mod.default_config(128, 128, 128, 28.8, deltat=1e-5, mimpur=39.948)
+    assert bytes(a) == bytes(b)
+
+
 def test_build_tables_match_oracle(he4gpu_mod, oracle_mod):
     for (n, xmax, selec, rc, um) in ((32, 12.8, "Xe_He", 2.55, 2793.9365463), (48, 14.4, "Ar_He", 2.0,
                                                                                  8080.8095081)):

@@ -5,7 +5,8 @@ norm and energy sums, force sum and impurity trajectory.
 Its error against the FP64 oracle is that of FP32 fields (about 1e-7
 relative per evaluation), so the tolerances here are FP32-scale: density and
 energies to 1e-5 relative after a few tens of steps, the impurity position to
-1e-8. Drift statements over long runs are produced by bench.py.
+1e-8. Drift statements over long runs come from he4gpu/drift.py; the
+10^4-step record of the 256^3 collision is tests/records/drift_mixed_he5000_xe_256.json.
 """
 import numpy as np
 import pytest
