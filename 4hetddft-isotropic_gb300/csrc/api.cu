@@ -113,6 +113,8 @@ struct he4g_run {
   void *ualphas = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr,
        *t6 = nullptr;
   float* timec = nullptr;
+  double* uext = nullptr;  // external (surface) potential, energy only; null: none
+  double* uext_buf = nullptr;  // its device array, allocated by the first he4g_set_uext
   // df64 form only: stencil rows, h2o2m4 and grids in df64; FP64 mirrors of
   // psi and the real fields for the FP64 energy and readback kernels
   StencilD std{};
@@ -153,6 +155,11 @@ struct he4g_run {
   cudaStream_t cs = nullptr;
   cudaEvent_t ev_snap = nullptr, ev_copied = nullptr;
   bool copy_pending = false;
+  // health check points inside multi-step calls: the health word copied to
+  // pinned host memory every kHealthEvery steps, one event per copy
+  int* hpin = nullptr;
+  cudaEvent_t hev[2] = {nullptr, nullptr};
+  int hslot = 0, hmarks = 0;
 };
 
 namespace {
@@ -620,10 +627,40 @@ int health_check(he4g_run* r) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
   if (e != cudaSuccess) return cuda_fail(r, e, "step");
   collect_timing(r);
-  if (h.health & 4) return fail(r, HE4G_ETABLE, "impurity distance beyond the potential table");
-  if (h.health & 2) return fail(r, HE4G_ENAN, "non-finite density");
-  if (h.health & 1) return fail(r, HE4G_EDENSITY, "density not > 0 after a Runge-Kutta stage");
+  const std::string at = h.fail_step > 0 ? " (first seen at the end of step " + std::to_string(h.fail_step) +
+                                               " since set_state; the state is that of step " +
+                                               std::to_string(r->iter) + ")"
+                                         : std::string();
+  if (h.health & 4) return fail(r, HE4G_ETABLE, "impurity distance beyond the potential table" + at);
+  if (h.health & 2) return fail(r, HE4G_ENAN, "non-finite density" + at);
+  if (h.health & 1) return fail(r, HE4G_EDENSITY, "density not > 0 after a Runge-Kutta stage" + at);
   return HE4G_OK;
+}
+
+// Health check points inside a multi-step call. The reference STOPs at the
+// step that fails (steprk.f90:89-92); a call here queues its steps without
+// waiting, so every kHealthEvery steps it copies the health word to pinned
+// host memory behind the step and then waits for the copy of the previous
+// check point, which leaves kHealthEvery steps queued on the device while
+// the host looks. A set bit stops the call: it returns with at most
+// 2 * kHealthEvery steps taken after the failing one (health_check reports
+// which step that was).
+constexpr int kHealthEvery = 8;
+
+void health_mark(he4g_run* r) {
+  const int slot = r->hslot;
+  cudaMemcpyAsync(&r->hpin[slot], &r->imp->health, sizeof(int), cudaMemcpyDeviceToHost, r->s);
+  cudaEventRecord(r->hev[slot], r->s);
+  r->hslot ^= 1;
+  r->hmarks += 1;
+}
+
+// true when the check point before the latest one saw a health bit
+bool health_seen(he4g_run* r) {
+  if (r->hmarks < 2) return false;
+  const int prev = r->hslot;  // after the flip: the older of the two slots
+  if (cudaEventSynchronize(r->hev[prev]) != cudaSuccess) return true;  // let the final check report it
+  return r->hpin[prev] != 0;
 }
 
 // steprk (steprk.f90:21-150)
@@ -843,9 +880,14 @@ int one_step(he4g_run* r) {
 
 int step_impl(he4g_run* r, int nsteps, cudaEvent_t stop) {
   if (nsteps < 0) return fail(r, HE4G_EINVAL, "nsteps < 0");
+  r->hmarks = 0;
   for (int s = 0; s < nsteps; ++s) {
     one_step(r);
     if (r->timing && (s % 16) == 15) collect_timing(r);
+    if ((s + 1) % kHealthEvery == 0 && s + 1 < nsteps) {
+      health_mark(r);
+      if (health_seen(r)) break;
+    }
   }
   if (stop) cudaEventRecord(stop, r->s);
   int rc = sync_err(r, "step");
@@ -1054,6 +1096,10 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   chk(r->small = dalloc<double>(r, 64));
   chk(r->imp = dalloc<ImpState>(r, 1));
   chk(r->ring = dalloc<double>(r, (size_t)kRingRows * kRingCols));
+  if (ok && (cudaHostAlloc(reinterpret_cast<void**>(&r->hpin), 2 * sizeof(int), cudaHostAllocDefault) != cudaSuccess ||
+             cudaEventCreateWithFlags(&r->hev[0], cudaEventDisableTiming) != cudaSuccess ||
+             cudaEventCreateWithFlags(&r->hev[1], cudaEventDisableTiming) != cudaSuccess))
+    ok = false;
   if (!ok) {
     he4g_destroy(r);
     return HE4G_ENOMEM;
@@ -1173,6 +1219,9 @@ void he4g_destroy(he4g_run* r) {
   }
   if (r->ev_snap) cudaEventDestroy(r->ev_snap);
   if (r->ev_copied) cudaEventDestroy(r->ev_copied);
+  for (cudaEvent_t e : r->hev)
+    if (e) cudaEventDestroy(e);
+  if (r->hpin) cudaFreeHost(r->hpin);
   for (void* p : r->allocs) cudaFree(p);
   if (r->s) cudaStreamDestroy(r->s);
   delete r;
@@ -1519,9 +1568,19 @@ int he4g_step_many(he4g_run** runs, int n, int nsteps) {
     if (rc) return rc;
   }
   // step by step, run by run: each run's launches go to its own stream, so
-  // the kernels of different runs overlap on the device
+  // the kernels of different runs overlap on the device; a run whose health
+  // check point saw a bit stops there (the others go on)
+  std::vector<char> stopped(n, 0);
+  for (int i = 0; i < n; ++i) runs[i]->hmarks = 0;
   for (int s = 0; s < nsteps; ++s)
-    for (int i = 0; i < n; ++i) one_step(runs[i]);
+    for (int i = 0; i < n; ++i) {
+      if (stopped[i]) continue;
+      one_step(runs[i]);
+      if ((s + 1) % kHealthEvery == 0 && s + 1 < nsteps) {
+        health_mark(runs[i]);
+        if (health_seen(runs[i])) stopped[i] = 1;
+      }
+    }
   int first = HE4G_OK;
   for (int i = 0; i < n; ++i) {
     int rc = sync_err(runs[i], "step_many");
@@ -1660,6 +1719,43 @@ int he4g_get_impurity(he4g_run* r, double rr[3], double v[3], double a[3]) {
   return HE4G_OK;
 }
 
+int he4g_set_timec(he4g_run* r, const double* timec) {
+  if (!r || !timec) return HE4G_EINVAL;
+  const size_t n = r->g.n;
+  std::vector<float> re(n);
+  for (size_t p = 0; p < n; ++p) {
+    const double a = timec[2 * p], b = timec[2 * p + 1];
+    const float f = static_cast<float>(a);
+    if (b != 1.0 || static_cast<double>(f) != a || !std::isfinite(f))
+      return fail(r, HE4G_EINVAL,
+                  "timec(" + std::to_string(p % r->g.nx + 1) + "," + std::to_string(p / r->g.nx % r->g.ny + 1) +
+                      "," + std::to_string(p / ((size_t)r->g.nx * r->g.ny) + 1) +
+                      "): the real part must be a finite single-precision value and the imaginary part 1 "
+                      "(the absorber of real-time evolution, DFT4He3d.f90:689-699)");
+    re[p] = f;
+  }
+  cudaError_t e = cudaMemcpyAsync(r->timec, re.data(), sizeof(float) * n, cudaMemcpyHostToDevice, r->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
+  return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "set_timec");
+}
+
+int he4g_set_uext(he4g_run* r, const double* uext) {
+  if (!r) return HE4G_EINVAL;
+  if (!uext) {
+    r->uext = nullptr;  // the array stays allocated until he4g_destroy
+    return HE4G_OK;
+  }
+  if (!r->uext_buf) {
+    r->uext_buf = static_cast<double*>(dalloc_bytes(r, sizeof(double) * r->g.n, false));
+    if (!r->uext_buf) return fail(r, HE4G_ENOMEM, "set_uext: device allocation failed");
+  }
+  cudaError_t e = cudaMemcpyAsync(r->uext_buf, uext, sizeof(double) * r->g.n, cudaMemcpyHostToDevice, r->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
+  if (e != cudaSuccess) return cuda_fail(r, e, "set_uext");
+  r->uext = r->uext_buf;
+  return HE4G_OK;
+}
+
 int he4g_set_impurity(he4g_run* r, const double rr[3], const double v[3], const double a[3]) {
   int rc = check_ready(r);
   if (rc) return rc;
@@ -1725,6 +1821,11 @@ int he4g_energy(he4g_run* r, he4g_energies* en) {
   cudaMemsetAsync(r->small + 40, 0, sizeof(double) * 3, r->s);
   launch_energy_grad(g, r->st, view.psi, r->xs, r->ys, r->zs, r->small + 40, r->partials, r->s);
   launch_reduce(r->partials, r->pblocks, 7, r->small + 16, r->s);
+  if (r->uext) {
+    launch_dot_ext(g, r->uext, mixed(r) ? nullptr : view.den, mixed(r) ? static_cast<const float*>(r->den) : nullptr,
+                   r->partials, r->s);
+    launch_reduce(r->partials, r->pblocks, 1, r->small + 23, r->s);
+  }
   double v[24];
   ImpState h;
   cudaMemcpyAsync(v, r->small, sizeof v, cudaMemcpyDeviceToHost, r->s);
@@ -1742,7 +1843,8 @@ int he4g_energy(he4g_run* r, he4g_energies* en) {
   en->ecor4 = v[8] * dxyz;
   en->etot4 = en->ekin4 + en->elj4 + en->ecor4 + en->esolid;
   if (otc) en->etot4 = en->etot4 + en->ealphas;
-  en->eext = 0.0;
+  // energy.f90:124: etot4 + sum(uext*den)*dxyz (uext of he4g_set_uext)
+  en->eext = r->uext ? v[23] * dxyz : 0.0;
   en->etot4 = en->etot4 + en->eext;
   const double v2 = h.vimp[0] * h.vimp[0] + h.vimp[1] * h.vimp[1] + h.vimp[2] * h.vimp[2];
   en->ekinx = 0.5 * r->mass * v2;

@@ -487,6 +487,16 @@ __device__ void reduce_cols(const double* partials, int nblocks, int nvals, doub
   }
 }
 
+// sum(uext * den) partials (energy.f90:124); den in FP64 or FP32
+template <typename T>
+__global__ void __launch_bounds__(256) k_dot_ext(Grid g, const double* __restrict__ uext, const T* __restrict__ den,
+                                                  double* partials) {
+  const Pt t = point(g);
+  double v[1] = {0.0};
+  if (t.ok) v[0] = uext[t.p] * static_cast<double>(den[t.p]);
+  block_sum<1>(v, partials);
+}
+
 __global__ void __launch_bounds__(kFinalThreads) k_reduce(const double* partials, int nblocks, int nvals,
                                                        double* out) {
   reduce_cols(partials, nblocks, nvals, out);
@@ -693,6 +703,13 @@ void launch_energy_grad(const Grid& g, const Stencil& st, const double2* psi, co
                         const double* ys, const double* zs, const double* cm, double* partials,
                         cudaStream_t s) {
   k_energy_grad<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, psi, xs, ys, zs, cm, partials);
+}
+void launch_dot_ext(const Grid& g, const double* uext, const double* den64, const float* den32, double* partials,
+                    cudaStream_t s) {
+  if (den64)
+    k_dot_ext<double><<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, uext, den64, partials);
+  else
+    k_dot_ext<float><<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, uext, den32, partials);
 }
 void launch_reduce(const double* partials, int nblocks, int nvals, double* out, cudaStream_t s) {
   k_reduce<<<1, kFinalThreads, 0, s>>>(partials, nblocks, nvals, out);

@@ -79,7 +79,7 @@ struct ImpState {
   double errHe, errimp;
   long long ring_head;  // rows written to the trajectory ring
   int health;           // bit 0: den <= 0, bit 1: non-finite, bit 2: table overflow
-  int pad1;
+  int fail_step;        // first step (since set_state) whose end saw a health bit; 0: none
 };
 
 constexpr int kRingRows = 8192;
@@ -234,6 +234,9 @@ void launch_energy_grad(const Grid& g, const Stencil& st, const double2* psi, co
                         const double* ys, const double* zs, const double* cm, double* partials,
                         cudaStream_t s);
 void launch_reduce(const double* partials, int nblocks, int nvals, double* out, cudaStream_t s);
+// per-block partials of sum(uext * den) (one of den64 / den32 non-null)
+void launch_dot_ext(const Grid& g, const double* uext, const double* den64, const float* den32, double* partials,
+                    cudaStream_t s);
 int pc_blocks(const Grid& g);
 void launch_density(const Grid& g, const double2* psi, double* den, cudaStream_t s);
 

@@ -102,6 +102,7 @@ __device__ __forceinline__ void imp_record_body(ImpState* s, double* ring) {
     r[7 + a] = s->aimp[a];
   }
   s->ring_head += 1;
+  if (s->health != 0 && s->fail_step == 0) s->fail_step = (int)s->ring_head;
 }
 
 // Fixed-order sum over the 32 lanes of a warp; the result is in lane 0.

@@ -13,6 +13,7 @@
 // that packs many runs into HBM by footprint) and calls the force inside its
 // time loop. cudaMalloc there would synchronise the whole device on every
 // step and can fail once co-resident runs have filled the GPU's memory.
+#include <cuda.h>  // CUcontext and the driver-call types; the calls are resolved through cudart
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -25,7 +26,7 @@ namespace {
 
 constexpr int kBX = 64, kBY = 4;  // 256-thread blocks of 64 x 4 points
 constexpr int kThreads = kBX * kBY;
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;  // cached (context, address) pairs
 
 // Largest block count accepted: ceil(nx/64) * ceil(ny/4) * nz, which is
 // 5 * 80 * 320 = 128000 for the largest 320^3 grid. 3 partial sums each:
@@ -34,8 +35,23 @@ constexpr long long kMaxBlocks = 131072;
 
 __device__ __align__(256) double g_force_scratch[kMaxBlocks * 3];
 
-double* g_scratch_addr[kMaxDevices] = {};
+// The device address of g_force_scratch belongs to the CUDA context it was
+// looked up in: each context loads its own copy of this module, and a
+// context re-created after cudaDeviceReset may place it elsewhere. So the
+// cache is keyed by the context's unique ID (cuCtxGetId: never reused within
+// a process), not by the device number.
+struct ScratchEntry {
+  unsigned long long ctx_id;
+  double* addr;
+};
+ScratchEntry g_scratch_cache[kMaxContexts] = {};
+int g_scratch_next = 0;
 std::mutex g_scratch_mu;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
 
 struct ForceArgs {
   int nx, ny, nz;
@@ -113,25 +129,64 @@ __global__ void __launch_bounds__(256) k_force_finish(const double* __restrict__
   }
 }
 
-// Device address of g_force_scratch on the current device, looked up once
-// per device with that device current.
-int scratch_for_current_device(double** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return HE4G_ECUDA;
-  if (dev < 0 || dev >= kMaxDevices) return HE4G_EINVAL;
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_force_scratch);
-    if (e != cudaSuccess) {
-      std::fprintf(stderr, "he4g_forceimp_noalloc: cudaGetSymbolAddress failed on device %d: %s\n", dev,
-                   cudaGetErrorString(e));
+int lookup_symbol(double** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_force_scratch);
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "he4g_forceimp_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+    return HE4G_ECUDA;
+  }
+  *out = static_cast<double*>(p);
+  return HE4G_OK;
+}
+
+// ID of the context current on this thread (the runtime's primary context of
+// the current device unless the host bound its own with cuCtxSetCurrent).
+int current_context_id(unsigned long long* id) {
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess) {
+      std::fprintf(stderr, "he4g_forceimp_noalloc: the driver does not provide cuCtxGetCurrent/cuCtxGetId\n");
       return HE4G_ECUDA;
     }
-    g_scratch_addr[dev] = static_cast<double*>(p);
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
   }
-  *out = g_scratch_addr[dev];
+  CUcontext ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return HE4G_ECUDA;
+  return g_ctx_get_id(ctx, id) == CUDA_SUCCESS ? HE4G_OK : HE4G_ECUDA;
+}
+
+// Device address of g_force_scratch in the current context. The first call
+// in a context looks it up (cudaGetSymbolAddress, with that context
+// current) and caches it under the context's ID.
+int scratch_for_current_context(double** out) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  unsigned long long id = 0;
+  if (current_context_id(&id) != HE4G_OK) {
+    // no context bound yet: the symbol lookup initialises the runtime's
+    // primary context of the current device, then the ID exists
+    double* p = nullptr;
+    int rc = lookup_symbol(&p);
+    if (rc) return rc;
+    rc = current_context_id(&id);
+    if (rc) return rc;
+  }
+  for (const ScratchEntry& c : g_scratch_cache)
+    if (c.addr && c.ctx_id == id) {
+      *out = c.addr;
+      return HE4G_OK;
+    }
+  double* p = nullptr;
+  const int rc = lookup_symbol(&p);
+  if (rc) return rc;
+  g_scratch_cache[g_scratch_next] = {id, p};
+  g_scratch_next = (g_scratch_next + 1) % kMaxContexts;
+  *out = p;
   return HE4G_OK;
 }
 
@@ -143,7 +198,13 @@ extern "C" int he4g_forceimp_noalloc(const double* den, const double* uimp, int 
     std::fprintf(stderr, "he4g_forceimp_noalloc: null array or grid axis shorter than the 13-point stencil\n");
     return HE4G_EINVAL;
   }
-  const long long nblocks = (long long)((nx + kBX - 1) / kBX) * ((ny + kBY - 1) / kBY) * nz;
+  if (!(std::isfinite(xmax) && std::isfinite(ymax) && std::isfinite(zmax)) || xmax == 0.0 || ymax == 0.0 ||
+      zmax == 0.0) {
+    std::fprintf(stderr, "he4g_forceimp_noalloc: box half-extents must be finite and nonzero\n");
+    return HE4G_EINVAL;
+  }
+  const long long bx = ((long long)nx + kBX - 1) / kBX, by = ((long long)ny + kBY - 1) / kBY;
+  const long long nblocks = bx * by * (long long)nz;
   if (nblocks > kMaxBlocks) {
     std::fprintf(stderr,
                  "he4g_forceimp_noalloc: grid %dx%dx%d needs %lld partial-sum slots, more than the %lld "
@@ -152,7 +213,7 @@ extern "C" int he4g_forceimp_noalloc(const double* den, const double* uimp, int 
     return HE4G_EINVAL;
   }
   double* scratch = nullptr;
-  int rc = scratch_for_current_device(&scratch);
+  int rc = scratch_for_current_context(&scratch);
   if (rc) return rc;
   ForceArgs a{};
   a.nx = nx;
@@ -166,7 +227,7 @@ extern "C" int he4g_forceimp_noalloc(const double* den, const double* uimp, int 
   }
   const double dxyz = h[0] * h[1] * h[2];
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  dim3 grid((nx + kBX - 1) / kBX, (ny + kBY - 1) / kBY, nz);
+  dim3 grid((unsigned)bx, (unsigned)by, (unsigned)nz);
   k_force_partials<<<grid, dim3(kBX, kBY), 0, s>>>(a, den, uimp, scratch);
   k_force_finish<<<1, 256, 0, s>>>(scratch, (int)nblocks, dxyz, F);
   cudaError_t e = cudaGetLastError();

@@ -10,8 +10,12 @@
 //    Xe–He / Ar–He potentials of V_impur.f90:2678-2772.
 //
 // Compiled with -ffp-contract=off so that every host platform rounds the same.
+#include <cctype>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <unordered_map>
 #include <vector>
 
@@ -307,4 +311,123 @@ extern "C" int he4g_build_tables(const he4g_config* c, const char* selec, double
     }
   }
   return HE4G_OK;
+}
+
+namespace {
+
+// He-TiO2 surface of morse.f90, in K. The laterally averaged Morse form
+// (Morse_HeTiO2_1D, morse.f90:1-16): De (exp(2 alpha (Re - r)) -
+// 2 exp(alpha (Re - r))) with De = 39.95 cm^-1, alpha = 1.721 A^-1,
+// Re = 4.3619 A and the cm^-1 -> K factor 1.4387752, which the reference
+// writes as a default-kind (single-precision) literal: its value is the
+// FP32 number nearest to 1.4387752, widened.
+double morse_tio2_1d(double r) {
+  const double De = 39.95, alpha = 1.721, Re = 4.3619;
+  const double cm_to_k = static_cast<double>(1.4387752f);
+  return De * (std::exp(2.0 * alpha * (Re - r)) - 2.0 * std::exp(alpha * (Re - r))) * cm_to_k;
+}
+
+// The corrugated form (Morse_HeTiO2_3D, morse.f90:37-97): De, alpha and Ze
+// are Fourier series in x (period a, cosines of orders 0-2) and y (period b,
+// orders 0-3), each the bilinear form Lx^T M Ly of a 3x4 coefficient matrix;
+// V = De (exp(-2 alpha (z - Ze)) - 2 exp(-alpha (z - Ze))).
+double morse_tio2_3d(double x, double y, double z) {
+  static const double kDe[3][4] = {{54.671500, -2.228480, 0.585194, 13.211000},
+                                   {4.842040, 0.363525, 4.614530, -1.182030},
+                                   {3.747220, 3.222690, 0.333350, 0.587320}};
+  static const double kAl[3][4] = {{1.492420, -0.010921, 0.003189, -0.168927},
+                                   {-0.097618, -0.024780, 0.062441, 0.016801},
+                                   {-0.034535, 0.030015, 0.012846, -0.011699}};
+  static const double kZe[3][4] = {{4.073990, 0.057537, -0.001500, -0.568990},
+                                   {-0.115578, -0.018127, -0.090046, 0.008590},
+                                   {-0.075153, -0.051210, -0.023349, -0.017931}};
+  const double pi = std::acos(-1.0), a = 2.9850, b = 6.49548;
+  double lx[3], ly[4];
+  for (int i = 0; i < 3; ++i) lx[i] = std::cos(2.0 * pi * static_cast<double>(i) * x / a);
+  for (int j = 0; j < 4; ++j) ly[j] = std::cos(2.0 * pi * static_cast<double>(j) * y / b);
+  auto form = [&](const double (&m)[3][4]) {
+    double out = 0.0;
+    for (int j = 0; j < 4; ++j) {  // (Lx^T M) first, then the product with Ly
+      double t = 0.0;
+      for (int i = 0; i < 3; ++i) t += lx[i] * m[i][j];
+      out += t * ly[j];
+    }
+    return out;
+  };
+  const double De = form(kDe), al = form(kAl), Ze = form(kZe);
+  return De * (std::exp(-2.0 * al * (z - Ze)) - 2.0 * std::exp(-al * (z - Ze)));
+}
+
+}  // namespace
+
+// uext of DFT4He3d.f90:760-784: min(3000 K, surface potential at z - zsurf)
+// on the grid x(ix) = -xmax + hx*(ix-1) etc. (DFT4He3d.f90:274-290)
+extern "C" int he4g_build_uext(const he4g_config* c, int lsurf3d, double zsurf, double* uext) {
+  if (!c || !uext || c->nx <= 0 || c->ny <= 0 || c->nz <= 0) return HE4G_EINVAL;
+  const int nx = c->nx, ny = c->ny, nz = c->nz;
+  const double hx = 2.0 * std::fabs(c->xmax) / nx, hy = 2.0 * std::fabs(c->ymax) / ny,
+               hz = 2.0 * std::fabs(c->zmax) / nz;
+  for (int k = 0; k < nz; ++k) {
+    const double z = -c->zmax + hz * static_cast<double>(k);
+    for (int j = 0; j < ny; ++j) {
+      const double y = -c->ymax + hy * static_cast<double>(j);
+      for (int i = 0; i < nx; ++i) {
+        const double x = -c->xmax + hx * static_cast<double>(i);
+        const double v = lsurf3d ? morse_tio2_3d(x, y, z - zsurf) : morse_tio2_1d(z - zsurf);
+        uext[(static_cast<size_t>(k) * ny + j) * nx + i] = std::fmin(3000.0, v);
+      }
+    }
+  }
+  return HE4G_OK;
+}
+
+// Integer `name = value` of a namelist file (case-insensitive name, the
+// first assignment of it outside quotes). The Fortran wrappers read the
+// driver's own echo of its &input group (DFT4He3d.namelist.read,
+// DFT4He3d.f90:195-196) for the loop cadence, so the driver's source stays
+// unchanged.
+extern "C" int he4g_read_namelist_int(const char* path, const char* name, int* value) {
+  if (!path || !name || !value || !*name) return HE4G_EINVAL;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return HE4G_EINVAL;
+  std::string text;
+  char buf[4096];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, got);
+  std::fclose(f);
+  auto low = [](char ch) { return static_cast<char>(std::tolower(static_cast<unsigned char>(ch))); };
+  const size_t nlen = std::strlen(name);
+  char quote = 0;
+  for (size_t i = 0; i < text.size(); ++i) {
+    const char ch = text[i];
+    if (quote) {
+      if (ch == quote) quote = 0;
+      continue;
+    }
+    if (ch == '\'' || ch == '"') {
+      quote = ch;
+      continue;
+    }
+    if (ch == '!') {  // comment to the end of the line
+      while (i < text.size() && text[i] != '\n') ++i;
+      continue;
+    }
+    const bool start = i == 0 || std::isspace(static_cast<unsigned char>(text[i - 1])) || text[i - 1] == ',' ||
+                       text[i - 1] == '&';
+    if (!start || i + nlen > text.size()) continue;
+    size_t k = 0;
+    while (k < nlen && low(text[i + k]) == low(name[k])) ++k;
+    if (k != nlen) continue;
+    size_t j = i + nlen;
+    while (j < text.size() && std::isspace(static_cast<unsigned char>(text[j]))) ++j;
+    if (j >= text.size() || text[j] != '=') continue;
+    ++j;
+    while (j < text.size() && std::isspace(static_cast<unsigned char>(text[j]))) ++j;
+    char* end = nullptr;
+    const long v = std::strtol(text.c_str() + j, &end, 10);
+    if (end == text.c_str() + j) return HE4G_EINVAL;
+    *value = static_cast<int>(v);
+    return HE4G_OK;
+  }
+  return HE4G_EINVAL;
 }

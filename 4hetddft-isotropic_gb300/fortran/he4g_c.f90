@@ -18,12 +18,17 @@ module he4g_c
     real(c_double) :: etot4, ekin4, elj4, ecor4, ealphas, esolid, eext, ekinx, eHeX, eimpu, etot
   end type
   type(c_ptr), save :: he4g_run = c_null_ptr
+  ! loop cadence of the driver, read from its namelist echo (DFT4He3d.f90:195-196):
+  ! the wrappers copy psi and den back only on the steps where the driver reads them
+  logical, save :: he4g_lazy = .false.
+  integer(c_int), save :: he4g_iter0 = 0, he4g_niter = 0, he4g_pener = 1, he4g_pcurr = 1
+  integer, save :: he4g_k = 0                ! steps taken through the wrappers (iteraux)
+  logical, save :: he4g_loop_state_sent = .false.
   interface
     integer(c_int) function he4g_create(cfg, fvlj4, wcgk, kalfs, potion, out) bind(C, name="he4g_create")
       import
       type(he4g_config), intent(in) :: cfg
-      real(c_double), intent(in) :: fvlj4(*), wcgk(*), potion(*)
-      type(c_ptr), value :: kalfs
+      real(c_double), intent(in) :: fvlj4(*), wcgk(*), kalfs(*), potion(*)   ! kalfs: read for core OTC only
       type(c_ptr), intent(out) :: out
     end function
     integer(c_int) function he4g_set_state(run, psi, rimp, vimp) bind(C, name="he4g_set_state")
@@ -100,12 +105,55 @@ module he4g_c
       integer(c_int), value :: which
       real(c_double), intent(out) :: out(*)
     end function
+    ! the driver's absorber array timec (grid module, modules.f90:101)
+    integer(c_int) function he4g_set_timec(run, timec) bind(C, name="he4g_set_timec")
+      import
+      type(c_ptr), value :: run
+      complex(c_double_complex), intent(in) :: timec(*)
+    end function
+    ! the driver's external potential uext (field module, modules.f90:54)
+    integer(c_int) function he4g_set_uext(run, uext) bind(C, name="he4g_set_uext")
+      import
+      type(c_ptr), value :: run
+      real(c_double), intent(in) :: uext(*)
+    end function
+    integer(c_int) function he4g_read_namelist_int(path, name, val) bind(C, name="he4g_read_namelist_int")
+      import
+      character(kind=c_char), intent(in) :: path(*), name(*)
+      integer(c_int), intent(out) :: val
+    end function
     type(c_ptr) function he4g_last_error(run) bind(C, name="he4g_last_error")
       import
       type(c_ptr), value :: run
     end function
   end interface
 contains
+  ! iter = iter0 + iteraux (DFT4He3d.f90:833-836): psi is read by the driver
+  ! every pener iterations (angular momentum, :869-926), every pcurr
+  ! (printoutc, :972-994) and after the last one (:1006-1010)
+  logical function he4g_psi_wanted()
+    he4g_psi_wanted = .not. he4g_lazy
+    if (he4g_lazy) he4g_psi_wanted = mod(he4g_iter0 + he4g_k, he4g_pener) == 0 .or. &
+        (he4g_pcurr > 0 .and. mod(he4g_k, max(he4g_pcurr, 1)) == 0) .or. he4g_iter0 + he4g_k >= he4g_niter
+  end function
+  ! den is read every pener iterations, after poten (:869, r_cm :875)
+  logical function he4g_den_wanted()
+    he4g_den_wanted = .not. he4g_lazy
+    if (he4g_lazy) he4g_den_wanted = he4g_k > 0 .and. mod(he4g_iter0 + he4g_k, he4g_pener) == 0
+  end function
+  subroutine he4g_read_cadence()
+    character(*), parameter :: f = 'DFT4He3d.namelist.read'
+    logical :: op
+    integer :: u
+    inquire(file=f, opened=op, number=u)
+    if (op) flush(u)                         ! the driver leaves the unit open
+    he4g_lazy = he4g_read_namelist_int(f//c_null_char, 'iter0'//c_null_char, he4g_iter0) == 0 .and. &
+                he4g_read_namelist_int(f//c_null_char, 'niter'//c_null_char, he4g_niter) == 0 .and. &
+                he4g_read_namelist_int(f//c_null_char, 'pener'//c_null_char, he4g_pener) == 0 .and. &
+                he4g_read_namelist_int(f//c_null_char, 'pcurr'//c_null_char, he4g_pcurr) == 0
+    if (he4g_lazy) he4g_lazy = he4g_pener > 0
+    if (.not. he4g_lazy) write(0,'(A)') 'he4g: no loop cadence in '//f//'; psi and den are copied every step'
+  end subroutine
   subroutine he4g_check(rc, where)
     integer(c_int), intent(in) :: rc
     character(*), intent(in) :: where

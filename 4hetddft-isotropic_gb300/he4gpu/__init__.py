@@ -79,6 +79,25 @@ def build_tables(cfg, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463, with_kalf
     return {"fvlj4": fv, "wcgk": wc, "kalfs": ka, "potion": po}
 
 
+def build_uext(cfg, lsurf3d=False, zsurf=-25.0):
+    """The TiO2 surface potential of DFT4He3d.f90:760-784 (morse.f90) on the
+    run's grid, shape (nz, ny, nx); zsurf defaults to the driver's -25 A."""
+    lib = abi.load()
+    out = np.empty((cfg.nz, cfg.ny, cfg.nx))
+    rc = lib.he4g_build_uext(C.byref(cfg), 1 if lsurf3d else 0, float(zsurf), abi.dptr(out))
+    if rc:
+        raise He4gError(rc, "build_uext")
+    return out
+
+
+def read_namelist_int(path, name):
+    """he4g_read_namelist_int: an integer of a namelist file, or None."""
+    lib = abi.load()
+    v = C.c_int()
+    rc = lib.he4g_read_namelist_int(str(path).encode(), name.encode(), C.byref(v))
+    return int(v.value) if rc == 0 else None
+
+
 def potion_table(cfg, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463):
     """The radial impurity table alone (potenimpini), for runs whose k-space
     tables are built on the device."""
@@ -274,6 +293,20 @@ class Run:
         r, v, a = np.zeros(3), np.zeros(3), np.zeros(3)
         self._ck(self.lib.he4g_get_impurity(self.h, abi.dptr(r), abi.dptr(v), abi.dptr(a)))
         return r, v, a
+
+    def set_timec(self, timec):
+        """he4g_set_timec: the absorber from a complex128 (nz, ny, nx) array
+        shaped like the driver's timec module array."""
+        t = np.ascontiguousarray(timec, dtype=np.complex128).reshape(self.shape)
+        self._ck(self.lib.he4g_set_timec(self.h, abi.dptr(t)))
+
+    def set_uext(self, uext):
+        """he4g_set_uext: the external potential of the energy (None: none)."""
+        if uext is None:
+            self._ck(self.lib.he4g_set_uext(self.h, None))
+            return
+        u = np.ascontiguousarray(uext, dtype=np.float64).reshape(self.shape)
+        self._ck(self.lib.he4g_set_uext(self.h, abi.dptr(u)))
 
     def set_impurity(self, r, v, a):
         r, v, a = (np.ascontiguousarray(x, dtype=np.float64) for x in (r, v, a))

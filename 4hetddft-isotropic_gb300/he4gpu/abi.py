@@ -137,6 +137,10 @@ SIGNATURES = {
     "he4g_steps_taken": (C.c_int, [_P]),
     "he4g_kernel_times": (C.c_int, [_P, C.POINTER(C.c_char_p), _D, C.POINTER(C.c_int), C.c_int]),
     "he4g_enable_timing": (C.c_int, [_P, C.c_int]),
+    "he4g_set_timec": (C.c_int, [_P, _D]),
+    "he4g_set_uext": (C.c_int, [_P, _D]),
+    "he4g_build_uext": (C.c_int, [C.POINTER(Config), C.c_int, C.c_double, _D]),
+    "he4g_read_namelist_int": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_int)]),
 }
 
 _lib = None

@@ -12,7 +12,9 @@
 //    7015 and <Lx,Ly,Lz> (DFT4He3d.f90:844-926, 1128-1140);
 //  - every pcurr steps density.NNNN.dat in the printoutc layout
 //    (printoutc.f90:52-77; DFT4He3d.f90:972-994), psi read back with
-//    he4g_get_psi_async so that the copy overlaps the next steps.
+//    he4g_get_psi_async so that the copy overlaps the next steps;
+//  - with lsurf, the TiO2 surface potential (lsurf3D, Zsurf;
+//    DFT4He3d.f90:760-784) in the energy blocks.
 //
 //   he4g_driver input.nml [--precision fp64|mixed|df64] [--parse]
 //
@@ -345,6 +347,13 @@ int main(int argc, char** argv) {
   he4g_run* run = nullptr;
   check(he4g_create(&c, nullptr, nullptr, nullptr, potion.data(), &run), "he4g_create", nullptr);
   check(he4g_set_state(run, psi.data(), rimp, vimp), "he4g_set_state", run);
+  // the TiO2 surface (DFT4He3d.f90:760-784): uext enters the energy only
+  if (has("lsurf") && flog(nl.at("lsurf"))) {
+    std::vector<double> uext(n);
+    const bool l3d = has("lsurf3d") && flog(nl.at("lsurf3d"));
+    check(he4g_build_uext(&c, l3d ? 1 : 0, num("zsurf", -25.0), uext.data()), "he4g_build_uext", run);
+    check(he4g_set_uext(run, uext.data()), "he4g_set_uext", run);
+  }
 
   std::FILE* fo[3] = {std::fopen(str("filerimp", "rimp.out").c_str(), "w"),
                       std::fopen(str("filevimp", "vimp.out").c_str(), "w"),

@@ -130,13 +130,31 @@ void he4g_default_config(he4g_config* cfg, int nx, int ny, int nz, double xmax, 
 int he4g_build_tables(const he4g_config* cfg, const char* selec, double r_cutoff, double umax,
                       double* fvlj4, double* wcgk, double* kalfs, double* potion);
 
+/* The external (surface) potential uext of DFT4He3d.f90:760-784 on the
+ * grid x(ix) = -xmax + hx*(ix-1) etc.: min(3000 K, V(z - zsurf)) with V the
+ * laterally averaged He-TiO2 Morse potential (lsurf3d = 0,
+ * Morse_HeTiO2_1D, morse.f90:1-16) or its corrugated form (lsurf3d = 1,
+ * Morse_HeTiO2_3D, morse.f90:37-97). uext holds nx*ny*nz doubles (Fortran
+ * order). Host arithmetic only; hand the result to he4g_set_uext. */
+int he4g_build_uext(const he4g_config* cfg, int lsurf3d, double zsurf, double* uext);
+
+/* Reads the integer `name = value` of a namelist file (first assignment,
+ * name case-insensitive) into *value; HE4G_EINVAL when the file or the name
+ * is missing. The Fortran wrappers read the loop cadence (iter0, niter,
+ * pener, pcurr) from the echo of its &input group that the driver writes at
+ * start-up (DFT4He3d.namelist.read, DFT4He3d.f90:195-196), so that they copy
+ * psi and den back only on the steps where the driver reads them. Host
+ * only. */
+int he4g_read_namelist_int(const char* path, const char* name, int* value);
+
 /* Device bytes he4g_create allocates for cfg (admission by HBM footprint);
  * host arithmetic only. */
 int he4g_footprint(const he4g_config* cfg, uint64_t* bytes);
 
 /* Allocates the run on the current CUDA device and uploads the tables
  * (replaces dimen.f90, fftini fft.f90:5-76 and the table set-up calls of
- * DFT4He3d.f90:518-596). kalfs is required for core OTC, else may be NULL.
+ * DFT4He3d.f90:518-596). kalfs is required for core OTC, else ignored (may
+ * be NULL).
  * With fvlj4 and wcgk both NULL (kalfs then ignored) the three k-space tables
  * are computed on the device from cfg instead (fforma.f90:36-60,
  * initcg.f90:32-49, DFT4He3d.f90:592-596, the formulas of he4g_build_tables,
@@ -153,6 +171,25 @@ const char* he4g_last_error(const he4g_run* run);
  * of q, pc, qr, qv and the impurity history: dimen.f90:117-118,
  * DFT4He3d.f90:796-800). den = |psi|^2 (:637). */
 int he4g_set_state(he4g_run* run, const double* psi, const double rimp[3], const double vimp[3]);
+
+/* Replaces the run's absorber with the driver's own module array timec
+ * (modules.f90:101, built at DFT4He3d.f90:689-699): complex(8), Fortran
+ * order, 2*nx*ny*nz doubles. The real part of every point must be a
+ * single-precision value (the reference builds it with a default-kind
+ * CMPLX, which rounds it to FP32) and the imaginary part exactly 1 (real-time
+ * evolution); anything else is HE4G_EINVAL with the offending point in
+ * he4g_last_error. Until the first call the run uses the absorber of its
+ * config (lambdah, t*mean, t*surf), built the same way. Applies to the next
+ * step; captured step graphs stay valid. */
+int he4g_set_timec(he4g_run* run, const double* timec);
+
+/* Sets the external potential uext (module array of modules.f90:54; real(8),
+ * Fortran order, nx*ny*nz doubles), which enters the energy only:
+ * eext = sum(uext*den)*dxyz is added to etot4 (energy.f90:124) and reported
+ * in he4g_energies.eext. NULL removes it (eext = 0, the driver's
+ * uext = 0 without lsurf, DFT4He3d.f90:782-784). The first non-NULL call
+ * allocates 8*nx*ny*nz device bytes, beyond he4g_footprint. */
+int he4g_set_uext(he4g_run* run, const double* uext);
 
 /* ---------------------------------------------- reference-routine mirrors */
 
@@ -209,9 +246,14 @@ int he4g_step(he4g_run* run, int nsteps, double* errHe, double* errimp);
  *    built-in device array of 3 MiB that every GPU which loads the library
  *    holds until the process exits. It fits 131072 blocks of 64x4 points,
  *    i.e. ceil(nx/64)*ceil(ny/4)*nz <= 131072 (every grid up to 320^3);
- *    larger grids are rejected with HE4G_EINVAL and a message on stderr.
- *  - The first call on a device looks up that array's device address with
- *    the device current; make that first call before any stream capture.
+ *    larger grids, zero or non-finite extents are rejected with HE4G_EINVAL
+ *    and a message on stderr.
+ *  - The array's device address belongs to the CUDA context current at the
+ *    call (the runtime's primary context of the current device, or a context
+ *    the host made current itself). The first call in each context looks it
+ *    up (cudaGetSymbolAddress) and caches it under the context's unique ID,
+ *    so a context re-created after cudaDeviceReset gets a fresh lookup; make
+ *    that first call before any stream capture.
  *  - All calls share the array, which keeps the last call's partial sums;
  *    no part of it needs zeroing (each call writes every slot it reads), but
  *    calls that overlap on the GPU (e.g. on two streams at once) race on it.
@@ -277,7 +319,10 @@ int he4g_get_psi(he4g_run* run, double* psi);  /* 2*nx*ny*nz doubles */
 /* psi without waiting: a device snapshot of psi is taken in stream order
  * after the work already issued on the run, and its copy into psi (pinned
  * host memory, 2*nx*ny*nz doubles, left untouched until the copy lands) runs
- * on a copy stream while the next steps compute. A later call waits on the
+ * on a copy stream while the next steps compute. The buffer must be pinned
+ * (page-locked: cudaHostAlloc, cudaHostRegister) for the copy to overlap;
+ * into pageable memory the CUDA runtime completes the copy before the call
+ * returns, which is correct but blocks the host for the copy. A later call waits on the
  * device, not the host, for the previous copy before it takes its snapshot.
  * The first call allocates the snapshot (16*nx*ny*nz bytes) and the copy
  * stream. The reference's driver reads psi between steps (the printoutc

@@ -174,6 +174,7 @@ struct orc_run {
   double ucenter[3];
   int iter;
   int have_state;
+  double* uext; /* external potential of the energy (modules.f90:54); NULL: zero */
 };
 
 void orc_set_threads(int n) {
@@ -685,7 +686,7 @@ void orc_destroy(orc_run* o) {
                   o->pc, o->sto1c, o->sto4c, o->den, o->pot4, o->dencg, o->delj4, o->uimp,
                   o->dxden, o->dyden, o->dzden, o->penalty, o->sto1, o->fden, o->wk1, o->denalf,
                   o->falfs, o->intx, o->inty, o->intz, o->ualphas, o->sto2, o->sto3, o->sto4,
-                  o->sto5, o->sto6, o->wk2, o->wk3};
+                  o->sto5, o->sto6, o->wk2, o->wk3, o->uext};
   for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; ++i) free(ptrs[i]);
   free(o);
 }
@@ -1309,6 +1310,7 @@ int orc_energy(orc_run* o, he4g_energies* e) {
     ksum s[8];
     memset(s, 0, sizeof s);
     const oc* f = (const oc*)o->psi;
+    const double* ux = o->uext;
     for (int j = 0; j < ny; ++j)
       for (int i = 0; i < nx; ++i) {
         size_t p = ((size_t)k * ny + j) * nx + i;
@@ -1333,6 +1335,7 @@ int orc_energy(orc_run* o, he4g_energies* e) {
         kadd(&s[2], d * cg * cg * (aux1 + aux2 * cg));
         if (c->lsolid) kadd(&s[3], d * (1.0 + tanh(c->beta_solid * (d - c->den_m))));
         kadd(&s[4], o->uimp[p] * d);
+        if (ux) kadd(&s[6], ux[p] * d);
         if (otc)
           kadd(&s[5], o->falfs[p] * (o->dxden[p] * o->intx[p] + o->dyden[p] * o->inty[p] +
                                      o->dzden[p] * o->intz[p]));
@@ -1355,7 +1358,9 @@ int orc_energy(orc_run* o, he4g_energies* e) {
   e->ecor4 = tot[2] * dxyz;
   e->etot4 = e->ekin4 + e->elj4 + e->ecor4 + e->esolid;
   if (otc) e->etot4 = e->etot4 + e->ealphas;
-  e->eext = 0.0; /* uext = 0 without lsurf (DFT4He3d.f90:782-785) */
+  /* energy.f90:124: etot4 + sum(uext*den)*dxyz; uext = 0 without lsurf
+   * (DFT4He3d.f90:782-784) */
+  e->eext = o->uext ? tot[6] * dxyz : 0.0;
   e->etot4 = e->etot4 + e->eext;
   double v2 = o->vimp[0] * o->vimp[0] + o->vimp[1] * o->vimp[1] + o->vimp[2] * o->vimp[2];
   e->ekinx = 0.5 * o->mass * v2;
@@ -1493,4 +1498,70 @@ int orc_get_impurity(orc_run* o, double r[3], double v[3], double a[3]) {
 }
 double orc_get_timec(orc_run* o, int ix, int iy, int iz) {
   return o->timec[((size_t)iz * o->ny + iy) * o->nx + ix];
+}
+
+/* the whole timec module array as the driver holds it (DFT4He3d.f90:689-699):
+ * complex(8), real part rounded to single precision, imaginary part 1 */
+void orc_timec_array(orc_run* o, double* out) {
+  for (size_t p = 0; p < o->n; ++p) {
+    out[2 * p] = o->timec[p];
+    out[2 * p + 1] = 1.0;
+  }
+}
+
+/* external potential of the energy; NULL removes it */
+int orc_set_uext(orc_run* o, const double* uext) {
+  if (!uext) {
+    free(o->uext);
+    o->uext = NULL;
+    return 0;
+  }
+  if (!o->uext) o->uext = (double*)malloc(sizeof(double) * o->n);
+  memcpy(o->uext, uext, sizeof(double) * o->n);
+  return 0;
+}
+
+/* He-TiO2 Morse surface of morse.f90. 1D (Morse_HeTiO2_1D, :1-16): the
+ * laterally averaged well in cm^-1 times 1.4387752 K/cm^-1, a
+ * default-kind (FP32) literal in the reference. 3D (Morse_HeTiO2_3D,
+ * :37-97): depth, range and position are cosine series in x (period
+ * 2.9850 A, orders 0-2) and y (6.49548 A, orders 0-3), each the product
+ * row(x) * M * column(y) of a 3x4 table. */
+double orc_morse_1d(double r) {
+  const double de = 39.95, al = 1.721, re = 4.3619;
+  return de * (exp(2.0 * al * (re - r)) - 2.0 * exp(al * (re - r))) * (double)1.4387752f;
+}
+double orc_morse_3d(double x, double y, double z) {
+  static const double tab[3][3][4] = {
+      {{54.671500, -2.228480, 0.585194, 13.211000}, {4.842040, 0.363525, 4.614530, -1.182030},
+       {3.747220, 3.222690, 0.333350, 0.587320}},
+      {{1.492420, -0.010921, 0.003189, -0.168927}, {-0.097618, -0.024780, 0.062441, 0.016801},
+       {-0.034535, 0.030015, 0.012846, -0.011699}},
+      {{4.073990, 0.057537, -0.001500, -0.568990}, {-0.115578, -0.018127, -0.090046, 0.008590},
+       {-0.075153, -0.051210, -0.023349, -0.017931}}};
+  const double pi = acos(-1.0);
+  double cx[3], cy[4], v[3];
+  for (int m = 0; m < 3; ++m) cx[m] = cos(2.0 * pi * (double)m * x / 2.9850);
+  for (int m = 0; m < 4; ++m) cy[m] = cos(2.0 * pi * (double)m * y / 6.49548);
+  for (int t = 0; t < 3; ++t) {
+    double acc = 0.0;
+    for (int b = 0; b < 4; ++b) {
+      double row = 0.0;
+      for (int a = 0; a < 3; ++a) row += cx[a] * tab[t][a][b];
+      acc += row * cy[b];
+    }
+    v[t] = acc;
+  }
+  return v[0] * (exp(-2.0 * v[1] * (z - v[2])) - 2.0 * exp(-v[1] * (z - v[2])));
+}
+/* uext of DFT4He3d.f90:760-784 on the grid of cfg */
+void orc_build_uext(const he4g_config* c, int lsurf3d, double zsurf, double* uext) {
+  const double hx = 2.0 * fabs(c->xmax) / c->nx, hy = 2.0 * fabs(c->ymax) / c->ny, hz = 2.0 * fabs(c->zmax) / c->nz;
+  for (int k = 0; k < c->nz; ++k)
+    for (int j = 0; j < c->ny; ++j)
+      for (int i = 0; i < c->nx; ++i) {
+        const double x = -c->xmax + hx * (double)i, y = -c->ymax + hy * (double)j, z = -c->zmax + hz * (double)k;
+        const double v = lsurf3d ? orc_morse_3d(x, y, z - zsurf) : orc_morse_1d(z - zsurf);
+        uext[((size_t)k * c->ny + j) * c->nx + i] = v < 3000.0 ? v : 3000.0;
+      }
 }

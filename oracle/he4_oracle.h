@@ -57,6 +57,11 @@ int orc_get_den(orc_run* o, double* den);
 int orc_get_field(orc_run* o, int which, double* out);
 int orc_get_impurity(orc_run* o, double r[3], double v[3], double a[3]);
 double orc_get_timec(orc_run* o, int ix, int iy, int iz);
+void orc_timec_array(orc_run* o, double* out);
+int orc_set_uext(orc_run* o, const double* uext);
+double orc_morse_1d(double r);
+double orc_morse_3d(double x, double y, double z);
+void orc_build_uext(const he4g_config* c, int lsurf3d, double zsurf, double* uext);
 
 /* raw building blocks, exposed for the unit checks */
 void orc_r2c(orc_run* o, const double* in, double* out_cplx);

@@ -70,6 +70,11 @@ def load():
         "orc_get_field": (C.c_int, [P, C.c_int, _D]),
         "orc_get_impurity": (C.c_int, [P, _D, _D, _D]),
         "orc_get_timec": (C.c_double, [P, C.c_int, C.c_int, C.c_int]),
+        "orc_timec_array": (None, [P, _D]),
+        "orc_set_uext": (C.c_int, [P, _D]),
+        "orc_morse_1d": (C.c_double, [C.c_double]),
+        "orc_morse_3d": (C.c_double, [C.c_double, C.c_double, C.c_double]),
+        "orc_build_uext": (None, [P, C.c_int, C.c_double, _D]),
         "orc_r2c": (None, [P, _D, _D]),
         "orc_c2r": (None, [P, _D, _D]),
         "orc_deriv_real": (None, [P, C.c_int, C.c_int, _D, _D]),
@@ -82,6 +87,14 @@ def load():
         f.argtypes = args
     _lib = lib
     return lib
+
+
+def build_uext(cfg, lsurf3d=False, zsurf=-25.0):
+    """The oracle's own surface potential on cfg's grid, (nz, ny, nx)."""
+    lib = load()
+    out = np.empty((cfg.nz, cfg.ny, cfg.nx))
+    lib.orc_build_uext(C.addressof(cfg), 1 if lsurf3d else 0, float(zsurf), _dp(out))
+    return out
 
 
 FIELDS = {"pot4": 0, "dencg": 1, "delj4": 2, "uimp": 3, "dxden": 4, "dyden": 5, "dzden": 6, "ualphas": 7,
@@ -195,6 +208,19 @@ class OracleRun:
 
     def timec(self, ix, iy, iz):
         return self.lib.orc_get_timec(self.h, ix, iy, iz)
+
+    def timec_array(self):
+        """The driver's timec module array, complex128 (nz, ny, nx)."""
+        out = np.empty(self.shape, dtype=np.complex128)
+        self.lib.orc_timec_array(self.h, _dp(out.view(np.float64)))
+        return out
+
+    def set_uext(self, uext):
+        if uext is None:
+            self.lib.orc_set_uext(self.h, None)
+        else:
+            u = np.ascontiguousarray(uext, dtype=np.float64)
+            self.lib.orc_set_uext(self.h, _dp(u))
 
     def r2c(self, a):
         a = np.ascontiguousarray(a, dtype=float)

@@ -12,6 +12,8 @@ fixtures it writes are committed, so the tests never need the reference.
 * reference_kats.json: known answers quoted in the reference source
   (V_impur.f90 comments for V_Xe_He(2.0) and V_Ar_He(2.0), the shipped input's
   umax = V_Xe_He(2.55), modules.f90's b4 against bforce), each with file:line.
+* reference_modules.json: the variables each module of modules.f90 declares,
+  which the Fortran wrappers may use (tests/test_fortran_binding.py).
 
 Usage: python tests/golden/make_golden.py <reference_dir>
 """
@@ -86,6 +88,42 @@ def redef13(mat):
     return m
 
 
+def module_variables(path):
+    """{module: sorted variable names} of modules.f90: the names each module
+    declares at module level (entity lists of its declaration statements,
+    initialisers and array specs removed; components of derived types
+    excluded)."""
+    mods, cur, in_type = {}, None, False
+    for line in open(path, encoding="latin-1").read().splitlines():
+        code = line.split("!")[0]
+        if re.match(r"\s*module\s+\w+\s*$", code, re.I):
+            cur = code.split()[1].lower()
+            mods[cur] = set()
+            continue
+        if re.match(r"\s*end\s*module", code, re.I):
+            cur = None
+            continue
+        if cur is None:
+            continue
+        if re.match(r"\s*type\s*(,|::|\s+\w+\s*$)", code, re.I) and "(" not in code.split("::")[0][4:]:
+            in_type = True
+            continue
+        if re.match(r"\s*end\s*type", code, re.I):
+            in_type = False
+            continue
+        if in_type or "::" not in code:
+            continue
+        rhs = code.split("::", 1)[1]
+        while re.search(r"\([^()]*\)", rhs):
+            rhs = re.sub(r"\([^()]*\)", "", rhs)
+        rhs = re.sub(r"'[^']*'|\"[^\"]*\"", "", rhs)
+        for part in rhs.split(","):
+            name = part.split("=")[0].strip()
+            if re.match(r"^[A-Za-z_]\w*$", name):
+                mods[cur].add(name.lower())
+    return {k: sorted(v) for k, v in mods.items()}
+
+
 def signed_decimal(entry):
     s, sg = entry
     if sg > 0:
@@ -139,7 +177,10 @@ def main():
                  "abs_tol": 0.005, "source": f"modules.f90:{ln}"})
     with open(os.path.join(HERE, "reference_kats.json"), "w") as f:
         json.dump(kats, f, indent=1)
-    print("wrote stencil_rows.json and reference_kats.json")
+    with open(os.path.join(HERE, "reference_modules.json"), "w") as f:
+        json.dump({"source": "modules.f90", "modules": module_variables(os.path.join(ref, "modules.f90"))}, f,
+                  indent=1)
+    print("wrote stencil_rows.json, reference_kats.json and reference_modules.json")
 
 
 if __name__ == "__main__":

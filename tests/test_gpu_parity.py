@@ -164,6 +164,22 @@ def test_zero_density_stops_like_steprk():
     assert e.value.code == he4gpu.abi.HE4G_EDENSITY
 
 
+def test_zero_density_stops_a_long_call_near_the_failing_step():
+    """A he4g_step call of many steps stops within 2 * 8 steps of the step
+    whose density check failed, and names that step (the reference STOPs in
+    that step, steprk.f90:89-92)."""
+    import he4gpu
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    psi = psi.copy()
+    psi[0:8, :, :] = 0.0
+    run = gpu_run(cfg, tk, psi, r, v)
+    with pytest.raises(he4gpu.He4gError) as e:
+        run.step(200)
+    assert e.value.code == he4gpu.abi.HE4G_EDENSITY
+    assert 1 <= run.steps_taken <= 1 + 2 * 8
+    assert "end of step 1 " in str(e.value)
+
+
 def test_impurity_beyond_table_is_an_error():
     import he4gpu
     cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
