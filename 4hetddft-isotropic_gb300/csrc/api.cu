@@ -160,6 +160,31 @@ struct he4g_run {
   int* hpin = nullptr;
   cudaEvent_t hev[2] = {nullptr, nullptr};
   int hslot = 0, hmarks = 0;
+  // batches (he4g_batch_create) this run belongs to: their graphs hold the
+  // run's buffers and launch shapes
+  std::vector<he4g_batch*> batches;
+};
+
+// A fixed set of runs stepped together, one CUDA graph per batch step: the
+// graph forks from the batch's stream into one branch per run (that run's
+// predictor-corrector step and trailing evaluation) and joins back. The
+// graph for a tuple of the runs' history arrangements is captured on first
+// use and replayed afterwards (each run's arrangement recurs every 10 steps).
+struct BatchGraph {
+  std::vector<GraphKey> keys;
+  std::vector<long long> nlaunch;
+  cudaGraphExec_t exec;
+};
+struct he4g_batch {
+  std::vector<he4g_run*> runs;
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  std::vector<cudaEvent_t> join;
+  std::vector<BatchGraph> graphs;
+  bool dead = false;       // a member run was destroyed
+  bool no_graphs = false;  // capture failed once: per-run launches from then on
+  int hslot = 0, hmarks = 0;
+  cudaEvent_t hev[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -793,6 +818,11 @@ void steppc_dev(he4g_run* r, double dt) {
 
 int step_impl(he4g_run* r, int nsteps, cudaEvent_t stop);
 
+void drop_batch_graphs(he4g_batch* b) {
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  b->graphs.clear();
+}
+
 int check_ready(he4g_run* r) {
   if (!r) return HE4G_EINVAL;
   if (!r->have_state) return fail(r, HE4G_ESTATE, "set_state has not been called");
@@ -1207,6 +1237,13 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
 void he4g_destroy(he4g_run* r) {
   if (!r) return;
   if (r->s) cudaStreamSynchronize(r->s);
+  for (he4g_batch* b : r->batches) {
+    if (b->s) cudaStreamSynchronize(b->s);
+    drop_batch_graphs(b);
+    b->dead = true;
+    for (auto& m : b->runs)
+      if (m == r) m = nullptr;
+  }
   for (auto& p : r->pending) {
     cudaEventDestroy(p.second.first);
     cudaEventDestroy(p.second.second);
@@ -1376,6 +1413,7 @@ void apply_tiles(he4g_run* r, const FftTiles& t) {
   fft_prepare(r->prec, r->plan);
   for (auto& e : r->graphs) cudaGraphExecDestroy(e.exec);
   r->graphs.clear();
+  for (he4g_batch* b : r->batches) drop_batch_graphs(b);
 }
 
 // device time per launch of fn: one untimed launch, then `reps` timed ones
@@ -1589,6 +1627,177 @@ int he4g_step_many(he4g_run** runs, int n, int nsteps) {
   }
   return first;
 }
+
+int he4g_batch_create(he4g_run** runs, int n, he4g_batch** out) {
+  if (!runs || n <= 0 || !out) return HE4G_EINVAL;
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!runs[i]) return HE4G_EINVAL;
+    for (int j = 0; j < i; ++j)
+      if (runs[j] == runs[i]) return fail(runs[i], HE4G_EINVAL, "he4g_batch_create: a run is listed twice");
+  }
+  he4g_batch* b = new he4g_batch();
+  b->runs.assign(runs, runs + n);
+  b->join.assign(n, nullptr);
+  bool ok = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->hev[0], cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->hev[1], cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; ok && i < n; ++i) ok = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    he4g_batch_destroy(b);
+    return HE4G_ECUDA;
+  }
+  for (he4g_run* r : b->runs) r->batches.push_back(b);
+  *out = b;
+  return HE4G_OK;
+}
+
+void he4g_batch_destroy(he4g_batch* b) {
+  if (!b) return;
+  if (b->s) cudaStreamSynchronize(b->s);
+  drop_batch_graphs(b);
+  for (he4g_run* r : b->runs)
+    if (r) r->batches.erase(std::remove(r->batches.begin(), r->batches.end(), b), r->batches.end());
+  for (cudaEvent_t e : b->join)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : {b->fork, b->done, b->hev[0], b->hev[1]})
+    if (e) cudaEventDestroy(e);
+  if (b->s) cudaStreamDestroy(b->s);
+  delete b;
+}
+
+extern "C++" {
+namespace {
+// One batch step of all runs from a graph on the batch's stream; false when
+// capture failed (the runs' roles are then unchanged).
+bool batch_step_graph(he4g_batch* b) {
+  const size_t n = b->runs.size();
+  std::vector<GraphKey> keys(n);
+  for (size_t i = 0; i < n; ++i) keys[i] = current_key(b->runs[i]);
+  for (auto& g : b->graphs) {
+    if (g.keys != keys) continue;
+    if (cudaGraphLaunch(g.exec, b->s) != cudaSuccess) return false;
+    for (size_t i = 0; i < n; ++i) {
+      advance_pc_roles(b->runs[i]);
+      b->runs[i]->launches += g.nlaunch[i];
+    }
+    return true;
+  }
+  std::vector<long long> l0(n);
+  for (size_t i = 0; i < n; ++i) l0[i] = b->runs[i]->launches;
+  bool ok = cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess &&
+            cudaEventRecord(b->fork, b->s) == cudaSuccess;
+  size_t captured = 0;
+  for (size_t i = 0; ok && i < n; ++i) {
+    he4g_run* r = b->runs[i];
+    ok = cudaStreamWaitEvent(r->s, b->fork, 0) == cudaSuccess;
+    if (!ok) break;
+    pc_step_launches(r);
+    ++captured;
+    ok = cudaEventRecord(b->join[i], r->s) == cudaSuccess && cudaStreamWaitEvent(b->s, b->join[i], 0) == cudaSuccess;
+  }
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->s, &graph);
+  cudaGraphExec_t exec = nullptr;
+  if (ok && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (!ok || e != cudaSuccess || cudaGraphLaunch(exec, b->s) != cudaSuccess) {
+    cudaGetLastError();
+    if (exec) cudaGraphExecDestroy(exec);
+    // capture recorded the launches without running them: undo the role changes
+    for (size_t i = 0; i < captured; ++i) {
+      he4g_run* r = b->runs[i];
+      const GraphKey& k = keys[i];
+      r->psi = static_cast<double2*>(const_cast<void*>(k.p[0]));
+      r->scratch = static_cast<double2*>(const_cast<void*>(k.p[1]));
+      for (int j = 0; j < 3; ++j) r->old[j] = static_cast<double2*>(const_cast<void*>(k.p[2 + j]));
+      r->h[0] = const_cast<void*>(k.p[5]);
+      r->h[1] = const_cast<void*>(k.p[6]);
+      r->cur32 = k.cur32;
+      r->launches = l0[i];
+    }
+    b->no_graphs = true;
+    return false;
+  }
+  BatchGraph g{keys, std::vector<long long>(n), exec};
+  for (size_t i = 0; i < n; ++i) g.nlaunch[i] = b->runs[i]->launches - l0[i];
+  b->graphs.push_back(std::move(g));
+  return true;
+}
+
+// the health words of all runs copied behind the batch's work (see health_mark)
+void batch_health_mark(he4g_batch* b) {
+  const int slot = b->hslot;
+  for (he4g_run* r : b->runs)
+    cudaMemcpyAsync(&r->hpin[slot], &r->imp->health, sizeof(int), cudaMemcpyDeviceToHost, b->s);
+  cudaEventRecord(b->hev[slot], b->s);
+  b->hslot ^= 1;
+  b->hmarks += 1;
+}
+bool batch_health_seen(he4g_batch* b) {
+  if (b->hmarks < 2) return false;
+  const int prev = b->hslot;
+  if (cudaEventSynchronize(b->hev[prev]) != cudaSuccess) return true;
+  for (he4g_run* r : b->runs)
+    if (r->hpin[prev] != 0) return true;
+  return false;
+}
+}  // namespace
+}  // extern "C++"
+
+int he4g_batch_step(he4g_batch* b, int nsteps) {
+  if (!b || nsteps < 0) return HE4G_EINVAL;
+  if (b->dead) return HE4G_ESTATE;
+  for (he4g_run* r : b->runs) {
+    const int rc = check_ready(r);
+    if (rc) return rc;
+  }
+  // the batch stream starts after the work already issued on every run
+  for (size_t i = 0; i < b->runs.size(); ++i) {
+    cudaEventRecord(b->join[i], b->runs[i]->s);
+    cudaStreamWaitEvent(b->s, b->join[i], 0);
+  }
+  b->hmarks = 0;
+  for (int s = 0; s < nsteps; ++s) {
+    bool graph_ok = false;
+    bool pc = !b->no_graphs;
+    for (he4g_run* r : b->runs)
+      if (r->iter + 1 <= 3 || r->cfg.lrk || r->timing) pc = false;
+    if (pc) graph_ok = batch_step_graph(b);
+    if (!graph_ok) {
+      // Runge-Kutta start (or no graph): each run's step on its own stream,
+      // between the batch stream's fork and join
+      cudaEventRecord(b->fork, b->s);
+      for (size_t i = 0; i < b->runs.size(); ++i) {
+        he4g_run* r = b->runs[i];
+        cudaStreamWaitEvent(r->s, b->fork, 0);
+        one_step(r);
+        cudaEventRecord(b->join[i], r->s);
+        cudaStreamWaitEvent(b->s, b->join[i], 0);
+      }
+    } else {
+      for (he4g_run* r : b->runs) r->iter += 1;
+    }
+    if ((s + 1) % kHealthEvery == 0 && s + 1 < nsteps) {
+      batch_health_mark(b);
+      if (batch_health_seen(b)) break;
+    }
+  }
+  // every run's stream continues after the batch's work
+  cudaEventRecord(b->done, b->s);
+  for (he4g_run* r : b->runs) cudaStreamWaitEvent(r->s, b->done, 0);
+  int first = HE4G_OK;
+  for (he4g_run* r : b->runs) {
+    int rc = sync_err(r, "batch_step");
+    if (!rc) rc = health_check(r);
+    if (rc && first == HE4G_OK) first = rc;
+  }
+  return first;
+}
+
+int he4g_batch_graphs(const he4g_batch* b) { return b ? static_cast<int>(b->graphs.size()) : -1; }
 
 int he4g_steps_taken(const he4g_run* r) { return r ? r->iter : -1; }
 

@@ -346,3 +346,39 @@ def step_many(runs, nsteps):
     if rc:
         msgs = [r.lib.he4g_last_error(r.h) for r in runs]
         raise He4gError(rc, "; ".join(m.decode() for m in msgs if m))
+
+
+class Batch:
+    """he4g_batch: a fixed set of runs advanced together, one CUDA graph per
+    batch step (every run's step in one graph launch)."""
+
+    def __init__(self, runs):
+        self.runs = list(runs)
+        self.lib = abi.load()
+        arr = (C.c_void_p * len(self.runs))(*[r.h.value if isinstance(r.h, C.c_void_p) else r.h for r in self.runs])
+        h = C.c_void_p()
+        rc = self.lib.he4g_batch_create(arr, len(self.runs), C.byref(h))
+        if rc:
+            raise He4gError(rc, "he4g_batch_create failed")
+        self.h = h
+
+    def step(self, nsteps):
+        rc = self.lib.he4g_batch_step(self.h, nsteps)
+        if rc:
+            msgs = [r.lib.he4g_last_error(r.h) for r in self.runs if getattr(r, "h", None)]
+            raise He4gError(rc, "; ".join(m.decode() for m in msgs if m))
+
+    @property
+    def graphs(self):
+        return int(self.lib.he4g_batch_graphs(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.he4g_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

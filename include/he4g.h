@@ -277,6 +277,31 @@ int he4g_enable_graphs(he4g_run* run, int on);
  * Returns the first error of any run. */
 int he4g_step_many(he4g_run** runs, int n, int nsteps);
 
+/* A fixed set of runs stepped together with one CUDA graph per batch step.
+ * No counterpart in the reference (it runs one collision per process). The
+ * graph forks from the batch's own stream into one branch per run (its
+ * predictor-corrector step and trailing evaluation, as he4g_step) and joins
+ * back; the graph for each tuple of the runs' history-slot arrangements is
+ * captured on first use and replayed afterwards, so a batch step costs one
+ * graph launch however many runs it holds. Steps in which any run is still in
+ * its Runge-Kutta start (or has kernel timing on) launch run by run between a
+ * fork and a join of the batch's stream instead. Each run's results are
+ * those of he4g_step on the run alone, bit for bit.
+ *  - he4g_batch_create: runs (distinct, n >= 1) stay owned by the caller.
+ *  - he4g_batch_step: advances every run by nsteps; the batch's stream waits
+ *    for the work already issued on each run, and each run's stream waits for
+ *    the batch's work before its later calls. Health check points as in
+ *    he4g_step (all runs stop at the first one that saw a bit). Returns the
+ *    first run's error; HE4G_ESTATE once a member run has been destroyed.
+ *  - Destroying a member run drops the batch's graphs and leaves the batch
+ *    usable only for he4g_batch_destroy. Changing a run's tiles drops them too.
+ *  - he4g_batch_graphs: graphs currently captured (diagnostics). */
+typedef struct he4g_batch he4g_batch;
+int he4g_batch_create(he4g_run** runs, int n, he4g_batch** out);
+int he4g_batch_step(he4g_batch* batch, int nsteps);
+int he4g_batch_graphs(const he4g_batch* batch);
+void he4g_batch_destroy(he4g_batch* batch);
+
 /* Tile shapes of the FFT line passes, HE4G_NTILES ints: tiles[0] lines per
  * block of the generic forward x pass, tiles[1] of the generic inverse x
  * pass, tiles[2] log2 of the kx columns per block of the generic y pass,

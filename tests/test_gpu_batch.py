@@ -48,6 +48,42 @@ def test_runs_in_the_mix_match_runs_alone(precision):
         assert x.energy() == y.energy()
 
 
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_batch_graph_matches_runs_alone(precision):
+    """he4g_batch_step: all runs' predictor-corrector steps in one graph per
+    batch step; 3 Runge-Kutta steps run run by run, then 24 predictor-
+    corrector steps cover the 10 arrangements of every run twice. The runs
+    start at different phases (one has 2 steps more), so the batch graphs
+    key on mixed arrangements. Each run ends bit for bit where it ends alone."""
+    import he4gpu
+    cases = ["he100_xe_32", "he300_ar_48", "he200_xe_40x48x64"]
+    alone, members, pre = [], [], [0, 2, 0]
+    for c, k in zip(cases, pre):
+        cfg, tk, psi, r, v, meta = make_case(c, precision=precision)
+        x = gpu_run(cfg, tk, psi, r, v)
+        x.step(27 + k)
+        alone.append(x)
+        y = gpu_run(cfg, tk, psi, r, v)
+        y.enable_graphs(True)
+        y.step(k)
+        members.append(y)
+    b = he4gpu.Batch(members)
+    b.step(27)
+    assert 1 <= b.graphs <= 10
+    for x, y in zip(alone, members):
+        assert x.steps_taken == y.steps_taken
+        assert np.array_equal(x.psi, y.psi)
+        assert all(np.array_equal(p, q) for p, q in zip(x.impurity(), y.impurity()))
+        assert np.array_equal(x.trajectory(), y.trajectory())
+        assert x.energy() == y.energy()
+    # a member run is destroyed: the batch refuses to step and can be freed
+    members[1].close()
+    with pytest.raises(he4gpu.He4gError) as e:
+        b.step(1)
+    assert e.value.code == he4gpu.abi.HE4G_ESTATE
+    b.close()
+
+
 @pytest.mark.parametrize("engine", [0, 15])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_tile_shapes_give_identical_results(precision, engine):

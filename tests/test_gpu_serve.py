@@ -1,0 +1,37 @@
+"""GPU check of the serving loop (he4gpu.serve) on a small stream: five jobs
+on 32^3 and 48^3 grids arrive while others run, the HBM budget admits at most
+two at a time (admission by he4g_footprint, eviction on completion), every
+job's result in the mix equals its result alone bit for bit, and every job's
+final energy and norm in the mixed form stay within |dE/E| < 1e-6 and 1e-8
+of its plain-FP64 twin served one job at a time."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _stream():
+    from he4gpu.initial import make_meta
+    jobs = []
+    spec = [(32, 100, "Xe", 12), (48, 300, "Ar", 9), (32, 150, "Ar", 14), (48, 200, "Xe", 10), (32, 120, "Xe", 8)]
+    for i, (g, n4, imp, steps) in enumerate(spec):
+        h = 0.8 if g == 32 else 0.6
+        meta = make_meta(g, h, n4, imp, 0.3, 3.0, steps=steps, gap=2.0, seed=100 + i)
+        jobs.append((0.05 * i, meta))
+    return jobs
+
+
+def test_serving_loop_admits_evicts_and_matches_runs_alone():
+    import he4gpu
+    from he4gpu import serve as S
+    stream = _stream()
+    need = max(he4gpu.footprint(S.job_config(m, S.MIXED)) for _, m in stream)
+    rep, kept = S.serve(stream, 2 * need, chunk=4, keep_results=tuple(range(len(stream))))
+    assert rep["jobs"] == len(stream)
+    assert 1 <= rep["max_resident"] <= 2
+    check = S.alone_vs_mix(stream, kept)
+    assert all(v["identical"] for v in check.values()), check
+    base = S.one_at_a_time_measured(stream)
+    assert base["jobs"] == len(stream)
+    drift = S.compare_finals(rep["finals"], base["finals"])
+    assert drift["jobs_compared"] == len(stream)
+    assert drift["dE_rel_max"] < 1e-6 and drift["norm_rel_max"] < 1e-8, drift
