@@ -528,11 +528,14 @@ void poten_dev(he4g_run* r) {
     }
   }
   {
-    // rho-hat -> coarse-grained density (spec0), Lennard-Jones (spec1), alpha_s density (spec2)
+    // rho-hat -> coarse-grained density (spec0) and alpha_s density (spec2);
+    // the forward z spectrum of rho stays in spec1 for the Lennard-Jones
+    // term, which joins the correlation convolution below
     Tick t(r, F_FFT_Z_CONV);
-    void* outs[3] = {r->spec0, r->spec1, r->spec2};
-    const void* facs[3] = {r->wcgk, r->fvlj4, r->kalfs};
-    t.launched(fft_z_conv(g, r->plan, prec, r->spec0, outs, facs, otc ? 3 : 2, 0.5 * g.renor, nullptr, r->s));
+    void* outs[2] = {r->spec0, r->spec2};
+    const void* facs[2] = {r->wcgk, r->kalfs};
+    t.launched(fft_z_conv(g, r->plan, prec, r->spec0, outs, facs, otc ? 2 : 1, 0.5 * g.renor, nullptr, r->s,
+                          r->spec1));
   }
   // inverse y, dencg and the correlation prologue, forward y: one fused
   // plane kernel, else the y passes around one fused row pass on the
@@ -573,10 +576,13 @@ void poten_dev(he4g_run* r) {
     }
   }
   {
-    // correlation convolution, plus the Lennard-Jones field already in spec1
+    // correlation and Lennard-Jones convolutions: W g-hat + V_LJ rho-hat in
+    // the z spectrum, one inverse transform of the sum (poten.f90:46-74 sums
+    // the two fields after their inverse transforms; the transform is linear)
     Tick t(r, F_FFT_Z_CONV);
     const void* f1[1] = {r->wcgk};
-    t.launched(fft_z_conv(g, r->plan, prec, r->spec0, sp0, f1, 1, 0.5 * g.renor, r->spec1, r->s));
+    t.launched(fft_z_conv(g, r->plan, prec, r->spec0, sp0, f1, 1, 0.5 * g.renor, nullptr, r->s, nullptr, r->spec1,
+                          r->fvlj4));
   }
   bool inv = false;
   if (xy) {
@@ -1509,9 +1515,8 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
     sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r, ENGINE_C2R);
   } else {
     // the fused z convolution against the split passes, on an evaluation's
-    // two z convolutions (two products, then one product plus a spectrum)
-    void* zo2[2] = {r->spec0, r->spec1};
-    const void* zf2[2] = {r->wcgk, r->fvlj4};
+    // two z convolutions (one product keeping the forward spectrum, then the
+    // sum of two products)
     const void* zf1[1] = {r->wcgk};
     float ms[2] = {0.f, 0.f};
     for (int split = 0; split < 2; ++split) {
@@ -1520,8 +1525,9 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
       r->plan.tiles = trial;
       fft_prepare(prec, r->plan);
       ms[split] = per_launch_ms(r, a, b, reps, [&] {
-        fft_z_conv(g, r->plan, prec, r->spec0, zo2, zf2, 2, 0.5 * g.renor, nullptr, r->s);
-        fft_z_conv(g, r->plan, prec, r->spec0, sp, zf1, 1, 0.5 * g.renor, r->spec1, r->s);
+        fft_z_conv(g, r->plan, prec, r->spec0, sp, zf1, 1, 0.5 * g.renor, nullptr, r->s, r->spec1);
+        fft_z_conv(g, r->plan, prec, r->spec0, sp, zf1, 1, 0.5 * g.renor, nullptr, r->s, nullptr, r->spec1,
+                   r->fvlj4);
       });
     }
     best.engine = ms[1] < ms[0] ? (best.engine | ENGINE_ZSPLIT) : (best.engine & ~ENGINE_ZSPLIT);
@@ -1536,8 +1542,6 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
     void* out = r->delj4;
     const void* cin[1] = {r->spec0};
     void* cout[1] = {out};
-    void* zouts[2] = {r->spec0, r->spec1};
-    const void* zfacs[2] = {r->wcgk, r->fvlj4};
     const void* zf1[1] = {r->wcgk};
     float best_ms = 0.f;
     int best_opt = 0;
@@ -1552,7 +1556,7 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
           fft_x_r2c(g, r->plan, prec, r->den, r->spec0, r->s);
           fft_y(g, r->plan, prec, sp, 1, -1, r->s);
         }
-        fft_z_conv(g, r->plan, prec, r->spec0, zouts, zfacs, 2, 0.5 * g.renor, nullptr, r->s);
+        fft_z_conv(g, r->plan, prec, r->spec0, sp, zf1, 1, 0.5 * g.renor, nullptr, r->s, r->spec1);
         if (!(xy && !otc && xy_mid(g, r->plan, r->spec0, out, r->den, cp4, cpp4, r->s))) {
           fft_y(g, r->plan, prec, sp, 1, +1, r->s);
           if (!fft_x_c2r_corr(g, r->plan, prec, r->spec0, out, r->den, cp4, cpp4, r->s)) {
@@ -1561,7 +1565,8 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
           }
           fft_y(g, r->plan, prec, sp, 1, -1, r->s);
         }
-        fft_z_conv(g, r->plan, prec, r->spec0, sp, zf1, 1, 0.5 * g.renor, r->spec1, r->s);
+        fft_z_conv(g, r->plan, prec, r->spec0, sp, zf1, 1, 0.5 * g.renor, nullptr, r->s, nullptr, r->spec1,
+                   r->fvlj4);
         if (!(xy && xy_inv_pot4(g, r->plan, r->spec0, r->dencg, r->den, r->fn, out, r->s))) {
           fft_y(g, r->plan, prec, sp, 1, +1, r->s);
           fft_x_c2r_pot4(g, r->plan, prec, r->spec0, r->dencg, r->den, r->fn, out, r->s);

@@ -216,9 +216,17 @@ __global__ void __launch_bounds__(kThreads) k_y(Grid g, FftAxis ax, SpecList<R> 
 }
 
 
+// the loads of one point of a two-term product (FactorList::add2)
+template <typename R>
+struct ZTerm {
+  R f, f2;
+  C2<R> a;
+};
+
 // Forward z transform, product with each factor table (times scale), inverse
 // z transform; output 0 may alias the input. `add` (nullable) is a spectrum
-// in the same (kx, ky, z) space that is added to output 0.
+// in the same (kx, ky, z) space that is added to output 0; fl.keep and
+// fl.add2 as FactorList describes.
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C2<R>* in, FactorList<R> fl,
                                                      int nout, R scale, const C2<R>* __restrict__ add, int ltx) {
@@ -249,22 +257,58 @@ __global__ void __launch_bounds__(kThreads) k_z_conv(Grid g, FftAxis ax, const C
   __syncthreads();
   C2<R>* fwd = fft_smem<R, -1>(a, b, ncol, ld, ax, tws);
   C2<R>* s1 = fwd == a ? b : a;
-  for (int o = 0; o < nout; ++o) {
-    const R* fac = o == 0 ? fl.f[0] : (o == 1 ? fl.f[1] : fl.f[2]);  // selected: no local copy
+  if (fl.keep) {  // the forward spectrum, unscaled
     staged_loop<R>(
         TX * n,
         [&](int w) {
           const int cc = w & (TX - 1), k = w >> ltx;
-          return cc < ncol ? __ldg(&fac[base + (long long)k * plane + cc]) : (R)0;
+          return cc < ncol ? fwd[cc * ld + pidx<R>(k)] : mk<R>(0, 0);
         },
-        [&](int w, R f0) {
+        [&](int w, C2<R> v) {
           const int cc = w & (TX - 1), k = w >> ltx;
-          if (cc < ncol) {
-            const R f = f0 * scale;
-            const C2<R> v = fwd[cc * ld + pidx<R>(k)];
-            s1[cc * ld + pidx<R>(k)] = mk<R>(v.x * f, v.y * f);
-          }
+          if (cc < ncol) fl.keep[base + (long long)k * plane + cc] = v;
         });
+  }
+  for (int o = 0; o < nout; ++o) {
+    const R* fac = o == 0 ? fl.f[0] : (o == 1 ? fl.f[1] : fl.f[2]);  // selected: no local copy
+    if (o == 0 && fl.add2) {
+      // (fwd f0 + add2 fac2) scale: the second convolution's spectrum joins
+      // before the one inverse transform
+      staged_loop<R>(
+          TX * n,
+          [&](int w) {
+            const int cc = w & (TX - 1), k = w >> ltx;
+            ZTerm<R> t{(R)0, (R)0, mk<R>(0, 0)};
+            if (cc < ncol) {
+              const long long e = base + (long long)k * plane + cc;
+              t = ZTerm<R>{__ldg(&fac[e]), __ldg(&fl.fac2[e]), fl.add2[e]};
+            }
+            return t;
+          },
+          [&](int w, ZTerm<R> t) {
+            const int cc = w & (TX - 1), k = w >> ltx;
+            if (cc < ncol) {
+              const R f = t.f * scale, f2 = t.f2 * scale;
+              const C2<R> v = fwd[cc * ld + pidx<R>(k)];
+              s1[cc * ld + pidx<R>(k)] = mk<R>(fma(t.a.x, f2, v.x * f), fma(t.a.y, f2, v.y * f));
+            }
+          });
+    } else {
+      staged_loop<R>(
+          TX * n,
+          [&](int w) {
+            const int cc = w & (TX - 1), k = w >> ltx;
+            return cc < ncol ? __ldg(&fac[base + (long long)k * plane + cc]) : (R)0;
+          },
+          [&](int w, R f0) {
+            const int cc = w & (TX - 1), k = w >> ltx;
+            if (cc < ncol) {
+              const R f = f0 * scale;
+              const C2<R> v = fwd[cc * ld + pidx<R>(k)];
+              s1[cc * ld + pidx<R>(k)] = mk<R>(v.x * f, v.y * f);
+            }
+          });
+    }
     __syncthreads();
     C2<R>* r = fft_smem<R, 1>(s1, c, ncol, ld, ax, tws);
     C2<R>* dst = o == 0 ? fl.out[0] : (o == 1 ? fl.out[1] : fl.out[2]);
@@ -343,8 +387,8 @@ void y_impl(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int 
 
 template <typename R>
 void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors,
-                int nout, double scale, const void* add, cudaStream_t s) {
-  if ((p.tiles.engine & ENGINE_Z) && reg_z<R>(g, p, in, outs, factors, nout, scale, add, s)) return;
+                int nout, double scale, const void* add, const ZExtra& zx, cudaStream_t s) {
+  if ((p.tiles.engine & ENGINE_Z) && reg_z<R>(g, p, in, outs, factors, nout, scale, add, zx, s)) return;
   const int ltx = p.tiles.ltx_z;
   const int TX = 1 << ltx;
   FactorList<R> fl{};
@@ -352,6 +396,9 @@ void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* ou
     fl.f[i] = static_cast<const R*>(factors[i]);
     fl.out[i] = static_cast<C2<R>*>(outs[i]);
   }
+  fl.keep = static_cast<C2<R>*>(zx.keep);
+  fl.add2 = static_cast<const C2<R>*>(zx.add2);
+  fl.fac2 = static_cast<const R*>(zx.fac2);
   const size_t smem = smem_of<R>(PASS_Z, p, ltx);
   set_smem(k_z_conv<R>, smem);
   dim3 grid((g.nxh + TX - 1) / TX, g.ny);
@@ -444,16 +491,19 @@ void fft_y(const Grid& g, const FftPlan& p, int prec, void* const* specs, int ns
     y_impl<float>(g, p, specs, nspec, sign, s);
 }
 int fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* const* outs,
-               const void* const* factors, int nout, double scale, const void* add, cudaStream_t s) {
+               const void* const* factors, int nout, double scale, const void* add, cudaStream_t s, void* keep,
+               const void* add2, const void* fac2) {
+  const ZExtra zx{keep, add2, fac2};
   if (prec == HE4G_PREC_FP64) {
-    zconv_impl<double>(g, p, in, outs, factors, nout, scale, add, s);
+    zconv_impl<double>(g, p, in, outs, factors, nout, scale, add, zx, s);
     return 1;
   }
   if (prec == HE4G_PREC_DF64) {
-    reg_z<df64>(g, p, in, outs, factors, nout, scale, add, s);
-    return (p.tiles.engine & ENGINE_ZSPLIT) ? 1 + nout : 1;
+    reg_z<df64>(g, p, in, outs, factors, nout, scale, add, zx, s);
+    if (!(p.tiles.engine & ENGINE_ZSPLIT)) return 1;
+    return add2 ? 2 : 1 + nout;
   }
-  zconv_impl<float>(g, p, in, outs, factors, nout, scale, add, s);
+  zconv_impl<float>(g, p, in, outs, factors, nout, scale, add, zx, s);
   return 1;
 }
 void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins, void* const* outs, int nspec,
@@ -514,7 +564,7 @@ void prepare_reg(const FftPlan& p) {
   for (int pro : {PRO_PLAIN, PRO_CORR, PRO_PROD})
     reg_r2c<R>(g, p, nullptr, pro, nullptr, nullptr, (R)0, (R)0, nullptr, nullptr, false);
   for (int sign : {-1, 1}) reg_y<R>(g, p, sp, 1, sign, nullptr, false);
-  reg_z<R>(g, p, nullptr, sp, f, 1, 1.0, nullptr, nullptr, false);
+  reg_z<R>(g, p, nullptr, sp, f, 1, 1.0, nullptr, ZExtra{}, nullptr, false);
   for (int epi : {EPI_STORE, EPI_POT4})
     reg_c2r<R>(g, p, nullptr, epi, nullptr, nullptr, nullptr, nullptr, 1, pa, nullptr, false);
   reg_c2r_corr<R>(g, p, nullptr, nullptr, nullptr, nullptr, (R)0, (R)0, nullptr, false);

@@ -637,10 +637,18 @@ struct SpecList {
   C2<R>* p[4];
 };
 
+// The tables and outputs of a z convolution. keep (nullable) receives the
+// forward z spectrum of the input, unscaled. add2 (nullable, with its table
+// fac2) is a spectrum in that same forward layout whose product joins output
+// 0's product before the inverse transform: output 0 = Z^-1((Z(in) f0 +
+// add2 fac2) scale), one inverse transform for the sum of two convolutions.
 template <typename R>
 struct FactorList {
   const Fld<R>* f[3];
   C2<R>* out[3];
+  C2<R>* keep;
+  const C2<R>* add2;
+  const Fld<R>* fac2;
 };
 
 // Raises a kernel's dynamic shared-memory limit once per (kernel, device) to
@@ -667,9 +675,15 @@ void set_smem(K kernel, size_t bytes) {
 template <typename R>
 bool reg_y(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int sign, cudaStream_t s,
            bool launch = true);
+// keep / add2 / fac2 of a z convolution (FactorList), untyped
+struct ZExtra {
+  void* keep;
+  const void* add2;
+  const void* fac2;
+};
 template <typename R>
 bool reg_z(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors, int nout,
-           double scale, const void* add, cudaStream_t s, bool launch = true);
+           double scale, const void* add, const ZExtra& zx, cudaStream_t s, bool launch = true);
 template <typename R>
 bool reg_r2c(const Grid& g, const FftPlan& p, const C2<R>* twx, int pro, const Fld<R>* a, const Fld<R>* b, R c0,
              R c1, C2<R>* out, cudaStream_t s, bool launch = true);

@@ -21,9 +21,9 @@ template bool reg_c2r_corr<float>(const Grid&, const FftPlan&, const float2*, fl
 template bool reg_y<double>(const Grid&, const FftPlan&, void* const*, int, int, cudaStream_t, bool);
 template bool reg_y<float>(const Grid&, const FftPlan&, void* const*, int, int, cudaStream_t, bool);
 template bool reg_z<double>(const Grid&, const FftPlan&, const void*, void* const*, const void* const*, int, double,
-                            const void*, cudaStream_t, bool);
+                            const void*, const ZExtra&, cudaStream_t, bool);
 template bool reg_z<float>(const Grid&, const FftPlan&, const void*, void* const*, const void* const*, int, double,
-                           const void*, cudaStream_t, bool);
+                           const void*, const ZExtra&, cudaStream_t, bool);
 template bool reg_r2c<double>(const Grid&, const FftPlan&, const double2*, int, const double*, const double*, double,
                               double, double2*, cudaStream_t, bool);
 template bool reg_r2c<float>(const Grid&, const FftPlan&, const float2*, int, const float*, const float*, float,

@@ -138,6 +138,10 @@ __global__ void __launch_bounds__(kRegThreads, std::is_same<R, double>::value ? 
     RegDft<R, Q, -1>::run(X);
 #pragma unroll
     for (int j = 0; j < Q; ++j) xbuf[(kp * Q + j) * L + cb] = X[j];
+    if (fl.keep) {  // the forward spectrum, unscaled
+#pragma unroll
+      for (int j = 0; j < Q; ++j) fl.keep[base + (kp + P * j) * stride + cb] = X[j];
+    }
   }
   for (int o = 0; o < nout; ++o) {
     C2<R> y[Q];
@@ -147,9 +151,15 @@ __global__ void __launch_bounds__(kRegThreads, std::is_same<R, double>::value ? 
       const Fld<R>* fac = o == 0 ? fl.f[0] : (o == 1 ? fl.f[1] : fl.f[2]);
 #pragma unroll
       for (int j = 0; j < Q; ++j) {
-        const R f = ldf<R>(&fac[base + (kp + P * j) * stride + cb]) * scale;
+        const long long e = base + (kp + P * j) * stride + cb;
+        const R f = ldf<R>(&fac[e]) * scale;
         const C2<R> x = xbuf[(kp * Q + j) * L + cb];
         y[j] = mk<R>(x.x * f, x.y * f);
+        if (o == 0 && fl.add2) {  // the second convolution joins before the inverse
+          const R f2 = ldf<R>(&fl.fac2[e]) * scale;
+          const C2<R> a = fl.add2[e];
+          y[j] = mk<R>(fma(a.x, f2, y[j].x), fma(a.y, f2, y[j].y));
+        }
       }
       RegDft<R, Q, 1>::run(y);
 #pragma unroll
@@ -201,10 +211,17 @@ __host__ __device__ constexpr size_t zcol_smem(bool with_factor) {
          (with_factor ? sizeof(Fld<R>) * P * Q * reg_lines<P, Q>() : 0);
 }
 
+// ofac (nullable) multiplies the output instead (times scale), and oadd *
+// oaddfac (nullable, times scale) is added to that product: the forward pass
+// of a convolution whose product, or sum of two products, is stored for a
+// plain inverse pass.
 template <typename R, int P, int Q, int SIGN>
 __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, const C2<R>* in, C2<R>* out,
                                                           const Fld<R>* __restrict__ fac, R scale,
-                                                          const C2<R>* __restrict__ add) {
+                                                          const C2<R>* __restrict__ add,
+                                                          const Fld<R>* __restrict__ ofac,
+                                                          const C2<R>* __restrict__ oadd,
+                                                          const Fld<R>* __restrict__ oaddfac) {
   static_assert(sizeof(C2<R>) == 16 && sizeof(Fld<R>) == 8, "asynchronous copies of 16-byte values, 8-byte factors");
   constexpr int N = P * Q;
   constexpr int L = reg_lines<P, Q>();
@@ -261,6 +278,15 @@ __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, co
     for (int j = 0; j < Q; ++j) {
       const long long e = base + (kp + P * j) * stride + c2;
       C2<R> r = w[j];
+      if (ofac) {
+        const R f = ldf<R>(&ofac[e]) * scale;
+        r = mk<R>(r.x * f, r.y * f);
+        if (oadd) {
+          const R f2 = ldf<R>(&oaddfac[e]) * scale;
+          const C2<R> a = oadd[e];
+          r = mk<R>(fma(a.x, f2, r.x), fma(a.y, f2, r.y));
+        }
+      }
       if (add) r = cadd<R>(r, add[e]);
       out[e] = r;
     }
@@ -634,6 +660,9 @@ void run_z(const Grid& g, const FftPlan& p, const C2<R>* in, const FactorList<R>
 // The split z convolution: the forward pass transforms `in` in place, then
 // each output gets its product-and-inverse pass; an output that aliases the
 // input goes last, so that every product reads the forward spectrum.
+// With fl.add2 (one output): a forward pass that stores (Z(in) f0 + add2
+// fac2) scale into output 0, then a plain inverse pass in place there. With
+// fl.keep the forward pass writes the spectrum there instead of over `in`.
 template <typename R, int P, int Q>
 void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>& fl, int nout, R scale,
                  const C2<R>* add, cudaStream_t s, bool launch) {
@@ -643,16 +672,25 @@ void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>
   set_smem(k_zcol_reg<R, P, Q, 1>, smem_f);
   if (!launch) return;
   dim3 grid((g.nxh + L - 1) / L, g.ny);
-  k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, in, nullptr, scale, nullptr);
+  if (fl.add2) {
+    k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, fl.out[0], nullptr, scale, nullptr, fl.f[0],
+                                                            fl.add2, fl.fac2);
+    k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, smem, s>>>(g, p.z, fl.out[0], fl.out[0], nullptr, scale, add,
+                                                           nullptr, nullptr, nullptr);
+    return;
+  }
+  C2<R>* fwd = fl.keep ? fl.keep : in;
+  k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, fwd, nullptr, scale, nullptr, nullptr, nullptr,
+                                                          nullptr);
   int order[3], n = 0;
   for (int o = 0; o < nout; ++o)
-    if (fl.out[o] != in) order[n++] = o;
+    if (fl.out[o] != fwd) order[n++] = o;
   for (int o = 0; o < nout; ++o)
-    if (fl.out[o] == in) order[n++] = o;
+    if (fl.out[o] == fwd) order[n++] = o;
   for (int i = 0; i < nout; ++i) {
     const int o = order[i];
-    k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, fl.f[o] ? smem_f : smem, s>>>(g, p.z, in, fl.out[o], fl.f[o], scale,
-                                                            o == 0 ? add : nullptr);
+    k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, fl.f[o] ? smem_f : smem, s>>>(
+        g, p.z, fwd, fl.out[o], fl.f[o], scale, o == 0 ? add : nullptr, nullptr, nullptr, nullptr);
   }
 }
 
@@ -733,12 +771,15 @@ bool reg_y(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int s
 
 template <typename R>
 bool reg_z(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors, int nout,
-           double scale, const void* add, cudaStream_t s, bool launch) {
+           double scale, const void* add, const ZExtra& zx, cudaStream_t s, bool launch) {
   FactorList<R> fl{};
   for (int i = 0; i < nout; ++i) {
     fl.f[i] = static_cast<const Fld<R>*>(factors[i]);
     fl.out[i] = static_cast<C2<R>*>(outs[i]);
   }
+  fl.keep = static_cast<C2<R>*>(zx.keep);
+  fl.add2 = static_cast<const C2<R>*>(zx.add2);
+  fl.fac2 = static_cast<const Fld<R>*>(zx.fac2);
   const C2<R>* ip = static_cast<const C2<R>*>(in);
   const C2<R>* ap = static_cast<const C2<R>*>(add);
   // df64: the split passes when ENGINE_ZSPLIT is set (launch == false

@@ -10,7 +10,7 @@ template bool reg_c2r_corr<df64>(const Grid&, const FftPlan&, const df2*, df2*, 
                                  cudaStream_t, bool);
 template bool reg_y<df64>(const Grid&, const FftPlan&, void* const*, int, int, cudaStream_t, bool);
 template bool reg_z<df64>(const Grid&, const FftPlan&, const void*, void* const*, const void* const*, int, double,
-                          const void*, cudaStream_t, bool);
+                          const void*, const ZExtra&, cudaStream_t, bool);
 template bool reg_r2c<df64>(const Grid&, const FftPlan&, const df2*, int, const df64*, const df64*, df64, df64,
                             df2*, cudaStream_t, bool);
 template bool reg_c2r<df64>(const Grid&, const FftPlan&, const df2*, int, const df2*, const df2*, df64*, df64*,

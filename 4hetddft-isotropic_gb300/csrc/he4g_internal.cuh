@@ -181,12 +181,18 @@ void fft_x_r2c_prod(const Grid& g, const FftPlan& p, int prec, const void* a, co
                     cudaStream_t s);
 void fft_y(const Grid& g, const FftPlan& p, int prec, void* const* specs, int nspec, int sign, cudaStream_t s);
 // forward z, multiply by nout tables (each scaled by `scale`), inverse z;
-// `add` (nullable) is added to output 0. Returns the kernels launched: one
-// fused kernel, or in the df64 form a forward pass that transforms `in` in
-// place (it is overwritten even when no output aliases it) and one
-// product-and-inverse pass per output.
+// `add` (nullable) is added to output 0. keep (nullable) receives the
+// forward z spectrum of `in` (unscaled); add2 (nullable) is such a forward
+// spectrum whose product with fac2 joins output 0's product before its
+// inverse transform (one inverse for the sum of two convolutions; used with
+// nout = 1). Returns the kernels launched: one fused kernel, or in the df64
+// split form a forward pass (into keep, else in place: `in` is overwritten
+// even when no output aliases it) and one product-and-inverse pass per
+// output; with add2 a forward pass that stores the product sum into output 0
+// and an inverse pass there.
 int fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* const* outs,
-               const void* const* factors, int nout, double scale, const void* add, cudaStream_t s);
+               const void* const* factors, int nout, double scale, const void* add, cudaStream_t s,
+               void* keep = nullptr, const void* add2 = nullptr, const void* fac2 = nullptr);
 void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins, void* const* outs, int nspec,
                cudaStream_t s);
 // c2r of the coarse-grained density spectrum (stored to dencg) fused with the

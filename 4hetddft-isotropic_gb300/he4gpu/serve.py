@@ -79,8 +79,12 @@ def pct(xs, q):
 
 
 def final_state(run, meta):
-    """The job's last total energy and norm (energy.f90, sum(den)*dxyz)."""
-    return {"etot": run.energy()["etot"], "norm": run.observables(meta["n4"])["npart"]}
+    """The job's last total energy, the sum of its components' magnitudes
+    (the energy scale: etot is a difference of large terms and can be small)
+    and its norm (energy.f90, sum(den)*dxyz)."""
+    e = run.energy()
+    scale = sum(abs(e[k]) for k in ("ekin4", "elj4", "ecor4", "ealphas", "esolid", "eext", "ekinx", "eHeX"))
+    return {"etot": e["etot"], "escale": scale, "norm": run.observables(meta["n4"])["npart"]}
 
 
 def serve(stream, hbm_budget, max_active=64, chunk=16, precision=MIXED, keep_results=(0,)):
@@ -212,10 +216,15 @@ def pretune(stream, precision, shared=True):
 
 
 def compare_finals(mixed, fp64):
-    """Per job: |E_mixed - E_fp64| / |E_fp64| and |N_mixed - N_fp64| / N_fp64."""
-    de = {j: abs(mixed[j]["etot"] - fp64[j]["etot"]) / abs(fp64[j]["etot"]) for j in fp64 if j in mixed}
-    dn = {j: abs(mixed[j]["norm"] - fp64[j]["norm"]) / abs(fp64[j]["norm"]) for j in fp64 if j in mixed}
+    """Per job: |E_mixed - E_fp64| / |E_fp64|, the same difference over the
+    job's energy scale (sum of the components' magnitudes), and
+    |N_mixed - N_fp64| / N_fp64."""
+    jobs = [j for j in fp64 if j in mixed]
+    de = {j: abs(mixed[j]["etot"] - fp64[j]["etot"]) / abs(fp64[j]["etot"]) for j in jobs}
+    ds = {j: abs(mixed[j]["etot"] - fp64[j]["etot"]) / fp64[j]["escale"] for j in jobs}
+    dn = {j: abs(mixed[j]["norm"] - fp64[j]["norm"]) / abs(fp64[j]["norm"]) for j in jobs}
     return {"jobs_compared": len(de), "dE_rel_max": max(de.values()) if de else None,
+            "dE_rel_p50": pct(list(de.values()), 50), "dE_over_scale_max": max(ds.values()) if ds else None,
             "norm_rel_max": max(dn.values()) if dn else None,
             "jobs_within_dE_1e-6": sum(1 for v in de.values() if v < 1e-6),
             "jobs_within_norm_1e-8": sum(1 for v in dn.values() if v < 1e-8)}
