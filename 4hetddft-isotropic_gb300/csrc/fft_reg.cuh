@@ -211,17 +211,15 @@ __host__ __device__ constexpr size_t zcol_smem(bool with_factor) {
          (with_factor ? sizeof(Fld<R>) * P * Q * reg_lines<P, Q>() : 0);
 }
 
-// ofac (nullable) multiplies the output instead (times scale), and oadd *
-// oaddfac (nullable, times scale) is added to that product: the forward pass
-// of a convolution whose product, or sum of two products, is stored for a
-// plain inverse pass.
+// in2 * fac2 (nullable, times scale; read directly, not staged) is added to
+// the product of a product pass before the transform: the sum of two
+// convolutions in one inverse pass.
 template <typename R, int P, int Q, int SIGN>
 __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, const C2<R>* in, C2<R>* out,
                                                           const Fld<R>* __restrict__ fac, R scale,
                                                           const C2<R>* __restrict__ add,
-                                                          const Fld<R>* __restrict__ ofac,
-                                                          const C2<R>* __restrict__ oadd,
-                                                          const Fld<R>* __restrict__ oaddfac) {
+                                                          const C2<R>* __restrict__ in2,
+                                                          const Fld<R>* __restrict__ fac2) {
   static_assert(sizeof(C2<R>) == 16 && sizeof(Fld<R>) == 8, "asynchronous copies of 16-byte values, 8-byte factors");
   constexpr int N = P * Q;
   constexpr int L = reg_lines<P, Q>();
@@ -256,6 +254,12 @@ __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, co
       if (fac) {
         const R f = fs[(Q * p + u) * L + c1] * scale;
         v[p] = mk<R>(v[p].x * f, v[p].y * f);
+        if (in2) {
+          const long long e = base + (Q * p + u) * stride + c1;
+          const R f2 = ldf<R>(&fac2[e]) * scale;
+          const C2<R> a = in2[e];
+          v[p] = mk<R>(fma(a.x, f2, v[p].x), fma(a.y, f2, v[p].y));
+        }
       }
     }
   }
@@ -278,15 +282,6 @@ __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, co
     for (int j = 0; j < Q; ++j) {
       const long long e = base + (kp + P * j) * stride + c2;
       C2<R> r = w[j];
-      if (ofac) {
-        const R f = ldf<R>(&ofac[e]) * scale;
-        r = mk<R>(r.x * f, r.y * f);
-        if (oadd) {
-          const R f2 = ldf<R>(&oaddfac[e]) * scale;
-          const C2<R> a = oadd[e];
-          r = mk<R>(fma(a.x, f2, r.x), fma(a.y, f2, r.y));
-        }
-      }
       if (add) r = cadd<R>(r, add[e]);
       out[e] = r;
     }
@@ -660,8 +655,8 @@ void run_z(const Grid& g, const FftPlan& p, const C2<R>* in, const FactorList<R>
 // The split z convolution: the forward pass transforms `in` in place, then
 // each output gets its product-and-inverse pass; an output that aliases the
 // input goes last, so that every product reads the forward spectrum.
-// With fl.add2 (one output): a forward pass that stores (Z(in) f0 + add2
-// fac2) scale into output 0, then a plain inverse pass in place there. With
+// With fl.add2 (one output): the forward pass in place, then one product
+// pass that adds add2 fac2 to the product before its inverse transform. With
 // fl.keep the forward pass writes the spectrum there instead of over `in`.
 template <typename R, int P, int Q>
 void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>& fl, int nout, R scale,
@@ -673,15 +668,13 @@ void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>
   if (!launch) return;
   dim3 grid((g.nxh + L - 1) / L, g.ny);
   if (fl.add2) {
-    k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, fl.out[0], nullptr, scale, nullptr, fl.f[0],
-                                                            fl.add2, fl.fac2);
-    k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, smem, s>>>(g, p.z, fl.out[0], fl.out[0], nullptr, scale, add,
-                                                           nullptr, nullptr, nullptr);
+    k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, in, nullptr, scale, nullptr, nullptr, nullptr);
+    k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, smem_f, s>>>(g, p.z, in, fl.out[0], fl.f[0], scale, add, fl.add2,
+                                                             fl.fac2);
     return;
   }
   C2<R>* fwd = fl.keep ? fl.keep : in;
-  k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, fwd, nullptr, scale, nullptr, nullptr, nullptr,
-                                                          nullptr);
+  k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, fwd, nullptr, scale, nullptr, nullptr, nullptr);
   int order[3], n = 0;
   for (int o = 0; o < nout; ++o)
     if (fl.out[o] != fwd) order[n++] = o;
@@ -690,7 +683,7 @@ void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>
   for (int i = 0; i < nout; ++i) {
     const int o = order[i];
     k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, fl.f[o] ? smem_f : smem, s>>>(
-        g, p.z, fwd, fl.out[o], fl.f[o], scale, o == 0 ? add : nullptr, nullptr, nullptr, nullptr);
+        g, p.z, fwd, fl.out[o], fl.f[o], scale, o == 0 ? add : nullptr, nullptr, nullptr);
   }
 }
 

@@ -188,8 +188,8 @@ void fft_y(const Grid& g, const FftPlan& p, int prec, void* const* specs, int ns
 // nout = 1). Returns the kernels launched: one fused kernel, or in the df64
 // split form a forward pass (into keep, else in place: `in` is overwritten
 // even when no output aliases it) and one product-and-inverse pass per
-// output; with add2 a forward pass that stores the product sum into output 0
-// and an inverse pass there.
+// output; with add2 the forward pass in place and one product pass that
+// adds add2 fac2 before its inverse transform.
 int fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* const* outs,
                const void* const* factors, int nout, double scale, const void* add, cudaStream_t s,
                void* keep = nullptr, const void* add2 = nullptr, const void* fac2 = nullptr);

@@ -84,8 +84,9 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64, fused_corr=False, fused_xy
         "fft_x_r2c": ev * ((r * n + c * nh) + (2 * r * n + c * nh)),
         # fwd 1, inv 1, fwd 1, inv 1 spectrum: read + write each
         "fft_y": ev * 4 * 2 * c * nh,
-        # product 1: R spectrum + 2 tables | W 2 spectra; product 2: R spectrum + table + added spectrum | W
-        "fft_z_conv": ev * ((c + 2 * r + 2 * c) * nh + (c + r + c + c) * nh),
+        # 1: R spectrum + table | W output + kept forward spectrum; 2: R spectrum + table + kept spectrum +
+        # table | W output (the Lennard-Jones product joins the correlation product before the inverse)
+        "fft_z_conv": ev * ((c + r + 2 * c) * nh + (c + r + c + r + c) * nh),
         # spectrum -> dencg
         "fft_x_c2r": ev * (c * nh + r * n),
         # spectrum + dencg + den -> pot4
