@@ -211,9 +211,10 @@ __host__ __device__ constexpr size_t zcol_smem(bool with_factor) {
          (with_factor ? sizeof(Fld<R>) * P * Q * reg_lines<P, Q>() : 0);
 }
 
-// in2 * fac2 (nullable, times scale; read directly, not staged) is added to
-// the product of a product pass before the transform: the sum of two
-// convolutions in one inverse pass.
+// in2 * fac2 (nullable, times scale) is added to the product of a product
+// pass before the transform: the sum of two convolutions in one inverse
+// pass. Its tiles reach the same shared slots by a second round of
+// asynchronous copies once the first product is in registers.
 template <typename R, int P, int Q, int SIGN>
 __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, const C2<R>* in, C2<R>* out,
                                                           const Fld<R>* __restrict__ fac, R scale,
@@ -254,16 +255,31 @@ __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, co
       if (fac) {
         const R f = fs[(Q * p + u) * L + c1] * scale;
         v[p] = mk<R>(v[p].x * f, v[p].y * f);
-        if (in2) {
-          const long long e = base + (Q * p + u) * stride + c1;
-          const R f2 = ldf<R>(&fac2[e]) * scale;
-          const C2<R> a = in2[e];
-          v[p] = mk<R>(fma(a.x, f2, v[p].x), fma(a.y, f2, v[p].y));
-        }
       }
     }
   }
-  __syncthreads();
+  __syncthreads();  // every slot has been read: the second round may overwrite them
+  if (in2 && fac) {
+    // each thread copies the slots it alone reads back, so no further barrier
+    if (act1) {
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const long long e = base + (Q * p + u) * stride + c1;
+        cp_async16(&buf[(Q * p + u) * L + c1], &in2[e]);
+        cp_async8(&fs[(Q * p + u) * L + c1], &fac2[e]);
+      }
+    }
+    cp_async_wait_all();
+    if (act1) {
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        const R f2 = fs[(Q * p + u) * L + c1] * scale;
+        const C2<R> a = buf[(Q * p + u) * L + c1];
+        v[p] = mk<R>(fma(a.x, f2, v[p].x), fma(a.y, f2, v[p].y));
+      }
+    }
+    __syncthreads();  // the slots are read before the exchange below overwrites them
+  }
   if (act1) {
     RegDft<R, P, SIGN>::run(v);
 #pragma unroll

@@ -113,9 +113,10 @@ def algorithmic_bytes_per_step(nx, ny, nz, prec=FP64, fused_corr=False, fused_xy
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of each
 # kernel family at 256^3, mean over the captured launches; from the ncu
 # captures summarised in profiles/fp64_step_he5000_xe_256_kernels.md and
-# profiles/mixed_step_he5000_xe_256_kernels.md.
+# profiles/mixed_step_he5000_xe_256_kernels.md (FP64 z convolution: the
+# capture after the Lennard-Jones product joined the correlation product).
 TRAFFIC_256 = {
-    FP64: {"potenimp": 71.7e6, "fft_x_r2c": 293.2e6, "fft_y": 216.6e6, "fft_z_conv": 470.7e6,
+    FP64: {"potenimp": 71.7e6, "fft_x_r2c": 293.2e6, "fft_y": 216.6e6, "fft_z_conv": 466.8e6,
            "fft_x_c2r": 218.4e6, "fft_x_c2r_pot4": 511.3e6, "force": 268.8e6, "pc_predict": 2581.7e6,
            "pc_correct": 2600.8e6},
     MIXED: {"fft_x_r2c": 126.0e6, "fft_y": 81.5e6, "fft_z_conv": 212.1e6, "fft_x_c2r": 85.9e6,
