@@ -1069,6 +1069,10 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
       c2 += q2[0] / (h * h);
     }
     r->std.d2c = df_of(c2);
+    r->std.cubic = 1;
+    for (int k = 1; k <= kStencilHalf; ++k)
+      for (int a = 1; a < 3; ++a)
+        if (r->std.d2[a][k].hi != r->std.d2[0][k].hi || r->std.d2[a][k].lo != r->std.d2[0][k].lo) r->std.cubic = 0;
     r->h2d = df_of(static_cast<long double>(c.h2o2m4));
   }
   Functional& fn = r->fn;

@@ -502,18 +502,29 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_reg(Grid g, FftAxis ax, c
     C2<R> w[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) w[q] = buf[rb * LD + xpad<Q>(kp * Q + q)];
-    RegDft<R, Q, 1>::run(w);
     const long long rowe = (row0 + rb) * g.nx;
+    // the epilogue's loads go out before the Q-point DFT, so that their
+    // latency overlaps its arithmetic
+    C2<R> cgv[EPI == EPI_POT4 ? Q : 1], dv[EPI == EPI_POT4 ? Q : 1];
+    if (EPI == EPI_POT4) {
+#pragma unroll
+      for (int j = 0; j < Q; ++j) {
+        const long long e = rowe + 2 * (kp + P * j);
+        cgv[j] = ld_pair<R>(pa.dencg + e);
+        if (pa.fn.lsolid) dv[j] = ld_pair<R>(pa.den + e);
+      }
+    }
+    RegDft<R, Q, 1>::run(w);
 #pragma unroll
     for (int j = 0; j < Q; ++j) {
       const long long e = rowe + 2 * (kp + P * j);
       C2<R> val = w[j];
       if (EPI == EPI_POT4) {
-        const C2<R> cg = ld_pair<R>(pa.dencg + e);
+        const C2<R> cg = cgv[j];
         R p0 = fma(cg.x * cg.x, fma(kc[1], cg.x, kc[0]), val.x);
         R p1 = fma(cg.y * cg.y, fma(kc[1], cg.y, kc[0]), val.y);
         if (pa.fn.lsolid) {
-          const C2<R> d = ld_pair<R>(pa.den + e);
+          const C2<R> d = dv[j];
           p0 += solid_penalty<R>(d.x, kc[2], kc[3], kc[4]);
           p1 += solid_penalty<R>(d.y, kc[2], kc[3], kc[4]);
         }
@@ -588,16 +599,21 @@ __global__ void __launch_bounds__(kRegThreads) k_x_c2r_corr_reg(Grid g, FftAxis 
     const bool actB = tid < RB * P && rb < nrows;
     C2<R> w[Q];
     if (actB) {
+      const long long rowe = (row0 + rb) * g.nx;
+      // the prologue's den loads go out before the Q-point DFT, so that
+      // their latency overlaps its arithmetic
+      C2<R> dv[Q];
+#pragma unroll
+      for (int j = 0; j < Q; ++j) dv[j] = ld_pair<R>(den + rowe + 2 * (kp + P * j));
 #pragma unroll
       for (int q = 0; q < Q; ++q) w[q] = buf[rb * LD + xpad<Q>(kp * Q + q)];
       RegDft<R, Q, 1>::run(w);
-      const long long rowe = (row0 + rb) * g.nx;
 #pragma unroll
       for (int j = 0; j < Q; ++j) {
         const long long e = rowe + 2 * (kp + P * j);
         const C2<R> cg = w[j];
         st_pair<R>(dencg + e, cg);
-        const C2<R> d = ld_pair<R>(den + e);
+        const C2<R> d = dv[j];
         w[j] = mk<R>(d.x * cg.x * fma(c1, cg.x, c0), d.y * cg.y * fma(c1, cg.y, c0));
       }
       RegDft<R, Q, -1>::run(w);

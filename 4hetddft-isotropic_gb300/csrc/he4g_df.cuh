@@ -13,6 +13,7 @@ struct StencilD {
   df64 d1[3][kStencilHalf + 1];
   df64 d2[3][kStencilHalf + 1];
   df64 d2c;
+  int cubic;  // 1: the second-derivative rows of the three axes are equal (hx = hy = hz)
 };
 
 // the radial impurity table and the grid coordinates in df64
