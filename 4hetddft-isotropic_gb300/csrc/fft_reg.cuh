@@ -42,6 +42,39 @@ __device__ __forceinline__ void stage_tw(C2<R>* tws, const C2<R>* tw, int n) {
   for (int t = threadIdx.x; t < n; t += blockDim.x) tws[t] = __ldg(&tw[t]);
 }
 
+// The kx columns a y or z block transforms. The half spectrum has nx/2 + 1
+// columns; when that is k*L + 1 (L a divisor of nx/2), a last tile of one
+// column per plane would keep a whole block for 1/L of its work. Then the
+// blocks past the k full tiles take that last (Nyquist) column of L
+// consecutive planes instead (planes: z for the y pass, ky for the z pass;
+// column c at plane stride cs), and grid.x is k + 1 with the extra blocks'
+// planes grouped by L. Returns false for a block with no columns.
+struct ColTile {
+  long long base;  // element of column 0, line index 0
+  long long cs;    // element stride between the tile's columns
+  int ncol;
+};
+__host__ __device__ constexpr bool nyquist_tiles(int nxh, int L) { return L > 1 && nxh % L == 1; }
+__host__ __device__ inline int col_blocks(int nxh, int L) {
+  return nyquist_tiles(nxh, L) ? nxh / L + 1 : (nxh + L - 1) / L;
+}
+template <int L>
+__device__ __forceinline__ bool col_tile(int nxh, int nouter, long long outer_stride, ColTile& t) {
+  const int bx = blockIdx.x, by = blockIdx.y;
+  if (nyquist_tiles(nxh, L) && bx == nxh / L) {
+    const int o0 = by * L;
+    if (o0 >= nouter) return false;
+    t.base = (long long)o0 * outer_stride + (nxh - 1);
+    t.cs = outer_stride;
+    t.ncol = min(L, nouter - o0);
+    return true;
+  }
+  t.base = (long long)by * outer_stride + (long long)bx * L;
+  t.cs = 1;
+  t.ncol = min(L, nxh - bx * L);
+  return true;
+}
+
 // ------------------------------------------------------------- y pass
 // In-place transform along y of L kx columns of one z plane per block.
 // Shared memory: the exchange buffer [N][L] (column fastest, so that the
@@ -54,9 +87,10 @@ __global__ void __launch_bounds__(kRegThreads) k_y_reg(Grid g, FftAxis ax, SpecL
   C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
   C2<R>* tws = buf + N * L;
   C2<R>* sp = specs.p[blockIdx.z];
-  const int kx0 = blockIdx.x * L;
-  const int ncol = min(L, g.nxh - kx0);
-  const long long base = (long long)blockIdx.y * g.ny * g.nxh + kx0;
+  ColTile ct;
+  if (!col_tile<L>(g.nxh, g.nz, (long long)g.ny * g.nxh, ct)) return;
+  const int ncol = ct.ncol;
+  const long long base = ct.base, cs = ct.cs;
   const long long stride = g.nxh;
   const int tid = threadIdx.x;
   const int c1 = tid % L, u = tid / L;
@@ -64,7 +98,7 @@ __global__ void __launch_bounds__(kRegThreads) k_y_reg(Grid g, FftAxis ax, SpecL
   C2<R> v[P];
   if (act1) {
 #pragma unroll
-    for (int p = 0; p < P; ++p) v[p] = sp[base + (Q * p + u) * stride + c1];
+    for (int p = 0; p < P; ++p) v[p] = sp[base + (Q * p + u) * stride + c1 * cs];
   }
   stage_tw<R>(tws, twiddles<R>(ax), N);
   __syncthreads();
@@ -83,7 +117,7 @@ __global__ void __launch_bounds__(kRegThreads) k_y_reg(Grid g, FftAxis ax, SpecL
     for (int q = 0; q < Q; ++q) w[q] = buf[(kp * Q + q) * L + c2];
     RegDft<R, Q, SIGN>::run(w);
 #pragma unroll
-    for (int j = 0; j < Q; ++j) sp[base + (kp + P * j) * stride + c2] = w[j];
+    for (int j = 0; j < Q; ++j) sp[base + (kp + P * j) * stride + c2 * cs] = w[j];
   }
 }
 
@@ -103,9 +137,10 @@ __global__ void __launch_bounds__(kRegThreads, std::is_same<R, double>::value ? 
   C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
   C2<R>* xbuf = buf + N * L;
   C2<R>* tws = xbuf + N * L;
-  const int kx0 = blockIdx.x * L;
-  const int ncol = min(L, g.nxh - kx0);
-  const long long base = (long long)blockIdx.y * g.nxh + kx0;
+  ColTile ct;
+  if (!col_tile<L>(g.nxh, g.ny, g.nxh, ct)) return;
+  const int ncol = ct.ncol;
+  const long long base = ct.base, cs = ct.cs;
   const long long stride = (long long)g.ny * g.nxh;
   const int tid = threadIdx.x;
   // layout A: thread (c, u), u < Q, holds x[Q*p + u]
@@ -118,7 +153,7 @@ __global__ void __launch_bounds__(kRegThreads, std::is_same<R, double>::value ? 
     C2<R> v[P];
     if (actA) {
 #pragma unroll
-      for (int p = 0; p < P; ++p) v[p] = in[base + (Q * p + u) * stride + ca];
+      for (int p = 0; p < P; ++p) v[p] = in[base + (Q * p + u) * stride + ca * cs];
     }
     stage_tw<R>(tws, twiddles<R>(ax), N);
     __syncthreads();
@@ -140,7 +175,7 @@ __global__ void __launch_bounds__(kRegThreads, std::is_same<R, double>::value ? 
     for (int j = 0; j < Q; ++j) xbuf[(kp * Q + j) * L + cb] = X[j];
     if (fl.keep) {  // the forward spectrum, unscaled
 #pragma unroll
-      for (int j = 0; j < Q; ++j) fl.keep[base + (kp + P * j) * stride + cb] = X[j];
+      for (int j = 0; j < Q; ++j) fl.keep[base + (kp + P * j) * stride + cb * cs] = X[j];
     }
   }
   for (int o = 0; o < nout; ++o) {
@@ -151,7 +186,7 @@ __global__ void __launch_bounds__(kRegThreads, std::is_same<R, double>::value ? 
       const Fld<R>* fac = o == 0 ? fl.f[0] : (o == 1 ? fl.f[1] : fl.f[2]);
 #pragma unroll
       for (int j = 0; j < Q; ++j) {
-        const long long e = base + (kp + P * j) * stride + cb;
+        const long long e = base + (kp + P * j) * stride + cb * cs;
         const R f = ldf<R>(&fac[e]) * scale;
         const C2<R> x = xbuf[(kp * Q + j) * L + cb];
         y[j] = mk<R>(x.x * f, x.y * f);
@@ -180,7 +215,7 @@ __global__ void __launch_bounds__(kRegThreads, std::is_same<R, double>::value ? 
       RegDft<R, P, 1>::run(w);
 #pragma unroll
       for (int j = 0; j < P; ++j) {
-        const long long e = base + (u + Q * j) * stride + ca;
+        const long long e = base + (u + Q * j) * stride + ca * cs;
         C2<R> r = w[j];
         if (addo) r = cadd<R>(r, addo[e]);
         dst[e] = r;
@@ -228,9 +263,10 @@ __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, co
   C2<R>* buf = reinterpret_cast<C2<R>*>(smraw);
   C2<R>* tws = buf + N * L;
   Fld<R>* fs = reinterpret_cast<Fld<R>*>(tws + N);  // factor tile, product passes only
-  const int kx0 = blockIdx.x * L;
-  const int ncol = min(L, g.nxh - kx0);
-  const long long base = (long long)blockIdx.y * g.nxh + kx0;
+  ColTile ct;
+  if (!col_tile<L>(g.nxh, g.ny, g.nxh, ct)) return;
+  const int ncol = ct.ncol;
+  const long long base = ct.base, cs = ct.cs;
   const long long stride = (long long)g.ny * g.nxh;
   const int tid = threadIdx.x;
   const int c1 = tid % L, u = tid / L;
@@ -238,12 +274,12 @@ __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, co
   if (act1) {
 #pragma unroll
     for (int p = 0; p < P; ++p) {
-      const long long e = base + (Q * p + u) * stride + c1;
+      const long long e = base + (Q * p + u) * stride + c1 * cs;
       cp_async16(&buf[(Q * p + u) * L + c1], &in[e]);
       if (fac) cp_async8(&fs[(Q * p + u) * L + c1], &fac[e]);
     }
   }
-  if (add && tid < N && ncol > 0)  // row tid of the added tile: ncol values, 16-byte aligned
+  if (add && cs == 1 && tid < N && ncol > 0)  // row tid of the added tile: ncol values, 16-byte aligned
     prefetch_l2(&add[base + (long long)tid * stride], (unsigned)(ncol * sizeof(C2<R>)));
   stage_tw<R>(tws, twiddles<R>(ax), N);
   cp_async_wait_all();
@@ -264,7 +300,7 @@ __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, co
     if (act1) {
 #pragma unroll
       for (int p = 0; p < P; ++p) {
-        const long long e = base + (Q * p + u) * stride + c1;
+        const long long e = base + (Q * p + u) * stride + c1 * cs;
         cp_async16(&buf[(Q * p + u) * L + c1], &in2[e]);
         cp_async8(&fs[(Q * p + u) * L + c1], &fac2[e]);
       }
@@ -296,7 +332,7 @@ __global__ void __launch_bounds__(kRegThreads) k_zcol_reg(Grid g, FftAxis ax, co
     RegDft<R, Q, SIGN>::run(w);
 #pragma unroll
     for (int j = 0; j < Q; ++j) {
-      const long long e = base + (kp + P * j) * stride + c2;
+      const long long e = base + (kp + P * j) * stride + c2 * cs;
       C2<R> r = w[j];
       if (add) r = cadd<R>(r, add[e]);
       out[e] = r;
@@ -669,7 +705,7 @@ void run_y(const Grid& g, const FftPlan& p, const SpecList<R>& sl, int nspec, cu
   const size_t smem = sizeof(C2<R>) * (P * Q * L + P * Q);
   set_smem(k_y_reg<R, P, Q, SIGN>, smem);
   if (!launch) return;
-  dim3 grid((g.nxh + L - 1) / L, g.nz, nspec);
+  dim3 grid(col_blocks(g.nxh, L), g.nz, nspec);
   k_y_reg<R, P, Q, SIGN><<<grid, kRegThreads, smem, s>>>(g, p.y, sl);
 }
 
@@ -680,7 +716,7 @@ void run_z(const Grid& g, const FftPlan& p, const C2<R>* in, const FactorList<R>
   const size_t smem = sizeof(C2<R>) * (2 * P * Q * L + P * Q);
   set_smem(k_z_conv_reg<R, P, Q>, smem);
   if (!launch) return;
-  dim3 grid((g.nxh + L - 1) / L, g.ny);
+  dim3 grid(col_blocks(g.nxh, L), g.ny);
   k_z_conv_reg<R, P, Q><<<grid, kRegThreads, smem, s>>>(g, p.z, in, fl, nout, scale, add);
 }
 
@@ -698,7 +734,7 @@ void run_z_split(const Grid& g, const FftPlan& p, C2<R>* in, const FactorList<R>
   set_smem(k_zcol_reg<R, P, Q, -1>, smem);
   set_smem(k_zcol_reg<R, P, Q, 1>, smem_f);
   if (!launch) return;
-  dim3 grid((g.nxh + L - 1) / L, g.ny);
+  dim3 grid(col_blocks(g.nxh, L), g.ny);
   if (fl.add2) {
     k_zcol_reg<R, P, Q, -1><<<grid, kRegThreads, smem, s>>>(g, p.z, in, in, nullptr, scale, nullptr, nullptr, nullptr);
     k_zcol_reg<R, P, Q, 1><<<grid, kRegThreads, smem_f, s>>>(g, p.z, in, fl.out[0], fl.f[0], scale, add, fl.add2,
