@@ -541,12 +541,12 @@ int orc_build_tables(const he4g_config* c, const char* selec, double r_cutoff, d
       kalfs[t] = exp(-(e * e));
     }
   }
-  /* potenimpini (potenimpini.f90:11-27) */
+  /* potenimpini (potenimpini.f90:11-27): nodes at (i-1)*delinter with
+     delinter = 4 max(xmax, ymax, zmax) / (npot - 1), the value the config
+     carries (he4g_default_config computes it so) and the one potenimp's
+     interpolation divides by; table and lookup use the same spacing */
   if (potion) {
-    double mx = c->xmax > c->ymax ? c->xmax : c->ymax;
-    if (c->zmax > mx) mx = c->zmax;
-    double rmax = 4.0 * mx;
-    double del = rmax / (double)(c->npot - 1);
+    double del = c->delinter;
     for (int i = 1; i <= c->npot; ++i) {
       double r = (double)(i - 1) * del;
       potion[i - 1] = select_pot(selec, r, r_cutoff, umax);

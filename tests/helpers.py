@@ -2,13 +2,16 @@
 import numpy as np
 
 
-def make_case(case, seed=0, **over):
+def make_case(case, seed=0, extents=None, **over):
+    """Configuration, table keys, state and metadata of a named collision
+    workload; extents = (xmax, ymax, zmax) replaces the box half-extents before
+    the defaults that depend on them (the impurity table spacing) are set."""
     import he4gpu
     psi, r, v, meta = he4gpu.collision_case(case, seed=seed)
     kw, tk = he4gpu.config_for_case(meta)
     kw.update(over)
-    cfg = he4gpu.default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], meta["ymax"], meta["zmax"],
-                                **kw)
+    ext = extents or (meta["xmax"], meta["ymax"], meta["zmax"])
+    cfg = he4gpu.default_config(meta["nx"], meta["ny"], meta["nz"], *ext, **kw)
     return cfg, tk, psi, r, v, meta
 
 

@@ -46,10 +46,10 @@ def test_unequal_spacings_take_the_per_axis_stencil():
     """A grid with hx, hy, hz all different (the y and z half-extents
     stretched) runs the per-axis stencil sums, where equal spacings run the
     six-neighbour sums of a cubic grid; both meet the oracle."""
-    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", precision=DF64)
-    c64, *_ = make_case("he100_xe_32")
-    for c in (cfg, c64):
-        c.ymax, c.zmax = 0.9 * meta["ymax"], 1.1 * meta["zmax"]
+    ext = (12.8, 0.9 * 12.8, 1.1 * 12.8)
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", extents=ext, precision=DF64)
+    c64, *_ = make_case("he100_xe_32", extents=ext)
+    assert meta["xmax"] == 12.8
     assert len({2 * cfg.xmax / cfg.nx, 2 * cfg.ymax / cfg.ny, 2 * cfg.zmax / cfg.nz}) == 3
     g = gpu_run(cfg, tk, psi, r, v)
     o = oracle_run(c64, tk, psi, r, v)
