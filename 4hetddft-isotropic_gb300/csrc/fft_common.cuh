@@ -9,6 +9,7 @@
 #include <utility>
 
 #include "df64.cuh"
+#include "fpconv.cuh"
 #include "he4g_internal.cuh"
 
 namespace he4g {
@@ -606,11 +607,18 @@ __device__ __forceinline__ R solid_penalty(R d, R beta, R dm, R cs) {
     }
     return df_split(penalty_fp64_tanh(df_to_double(x), df_to_double(beta * d), df_to_double(cs)));
   } else {
-    if (x < -10.0) {
-      const float e = expf(2.f * (float)x);
+    // The test x < -10 on x's bits (negative, |x| > 10, not NaN) and the
+    // FP32 conversions by integer operations (fpconv.cuh): comparisons and
+    // conversions of doubles issue on the FP64 pipe, which bounds this form.
+    // fpconv flushes binary32 subnormals, which only a penalty below
+    // 1.2e-38 K would meet.
+    const long long b = __double_as_longlong(x);
+    const long long mag = b & 0x7FFFFFFFFFFFFFFFLL;
+    if (b < 0 && mag > 0x4024000000000000LL && mag <= 0x7FF0000000000000LL) {
+      const float e = expf(2.f * d2f(x));
       const float inv = 1.f / (1.f + e);
-      const float bd = (float)(beta * d);
-      return (R)(((float)cs * 2.f * e * inv) * (1.f + 2.f * bd * inv));
+      const float bd = d2f(beta * d);
+      return f2d((d2f(cs) * 2.f * e * inv) * (1.f + 2.f * bd * inv));
     }
     const R t = tanh(x);
     return cs * ((R)1 + t + beta * d * ((R)1 - t * t));

@@ -254,16 +254,39 @@ __device__ __forceinline__ double div_rn(double a, double d, double inv) {
   return __fma_rn(e, inv, q0);
 }
 
+// trunc(q) of a non-negative q, as an integer (returned) and as a double
+// (qt), from q's bits: the conversion instructions (and comparisons) of
+// doubles issue on the FP64 pipe, which bounds this kernel, and integer
+// operations do not. Negative, NaN, infinite and q >= 2^62 return -1, which
+// the table check rejects (a saturated conversion could overflow ir + 1).
+__device__ __forceinline__ long long trunc_nonneg(double q, double& qt) {
+  const long long b = __double_as_longlong(q);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;  // unbiased exponent
+  qt = 0.0;
+  if ((b << 1) == 0) return 0;  // +0 and -0
+  if (b < 0 || e >= 62) return -1;
+  if (e < 0) return 0;  // 0 < q < 1
+  const long long m = (b & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL;
+  if (e >= 52) {
+    qt = q;
+    return m << (e - 52);
+  }
+  qt = __longlong_as_double(b & ~((1LL << (52 - e)) - 1));
+  return m >> (52 - e);
+}
+
 // updatepoten (potenimp.f90:71-95): linear interpolation of the radial
 // table at r = |x - center|. Every rounding step is explicit so that uimp
-// matches a CPU evaluation of the same expression bit for bit.
+// matches a CPU evaluation of the same expression bit for bit. A thread
+// evaluates kPX points of one x row, kBX apart, sharing dy^2 + dz^2.
+constexpr int kPX = 4;
+
 __global__ void __launch_bounds__(256) k_potenimp(Grid g, const double* __restrict__ xs,
                                                    const double* __restrict__ ys,
                                                    const double* __restrict__ zs,
                                                    const double* __restrict__ potion, int npot,
                                                    double delinter, double inv, ImpState* imp, int center_sel,
                                                    double* uimp) {
-  const Pt t = point(g);
   const double* c = center_sel == 0 ? imp->rimp : imp->center;
   const double c0 = c[0], c1 = c[1], c2 = c[2];
   if (center_sel == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 &&
@@ -272,28 +295,39 @@ __global__ void __launch_bounds__(256) k_potenimp(Grid g, const double* __restri
     imp->center[1] = c1;
     imp->center[2] = c2;
   }
-  if (!t.ok) return;
-  const double dz = __dadd_rn(__ldg(zs + t.k), -c2);
-  const double dy = __dadd_rn(__ldg(ys + t.j), -c1);
-  const double dx = __dadd_rn(__ldg(xs + t.i), -c0);
+  const int j = blockIdx.y * kBY + threadIdx.y, k = blockIdx.z;
+  if (j >= g.ny) return;
+  const double dz = __dadd_rn(__ldg(zs + k), -c2);
+  const double dy = __dadd_rn(__ldg(ys + j), -c1);
   const double zt = __dmul_rn(dz, dz);
   const double yt = __dadd_rn(__dmul_rn(dy, dy), zt);
-  const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), yt));
-  const long long ir = (long long)div_rn(r, delinter, inv);
-  // mod(r, delinter) exactly: r - ir*delinter is representable and one FMA
-  // gives it, except when r/delinter rounded up onto an integer; then the
-  // true remainder (in [delinter/2, delinter)) is that negative value plus
-  // delinter, again exact
-  double rem = __fma_rn(-(double)ir, delinter, r);
-  if (rem < 0.0) rem = __dadd_rn(rem, delinter);
-  const double w = div_rn(rem, delinter, inv);
-  double u = 0.0;
-  if (ir >= 0 && ir + 1 < npot) {
-    u = __dadd_rn(__dmul_rn(__ldg(potion + ir), __dadd_rn(1.0, -w)), __dmul_rn(__ldg(potion + ir + 1), w));
-  } else {
-    atomicOr(&imp->health, 4);
+  const long long row = ((long long)k * g.ny + j) * g.nx;
+  bool bad = false;
+#pragma unroll
+  for (int q = 0; q < kPX; ++q) {
+    const int i = (blockIdx.x * kPX + q) * kBX + threadIdx.x;
+    if (i >= g.nx) break;
+    const double dx = __dadd_rn(__ldg(xs + i), -c0);
+    const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), yt));
+    double irf;
+    const long long ir = trunc_nonneg(div_rn(r, delinter, inv), irf);
+    // mod(r, delinter) exactly: r - ir*delinter is representable and one FMA
+    // gives it, except when r/delinter rounded up onto an integer; then the
+    // true remainder (in [delinter/2, delinter)) is that negative value plus
+    // delinter, again exact. The FMA's exact zero is +0, so the sign bit
+    // alone marks a negative remainder.
+    double rem = __fma_rn(-irf, delinter, r);
+    if (__double_as_longlong(rem) < 0) rem = __dadd_rn(rem, delinter);
+    const double w = div_rn(rem, delinter, inv);
+    double u = 0.0;
+    if (ir >= 0 && ir < npot - 1) {
+      u = __dadd_rn(__dmul_rn(__ldg(potion + ir), __dadd_rn(1.0, -w)), __dmul_rn(__ldg(potion + ir + 1), w));
+    } else {
+      bad = true;
+    }
+    uimp[row + i] = u;
   }
-  uimp[t.p] = u;
+  if (bad) atomicOr(&imp->health, 4);
 }
 
 // derden (derden.f90:26-28) fused with the force sums of forceimp
@@ -675,7 +709,8 @@ void launch_potenimp(const Grid& g, const double* x, const double* y, const doub
                      int npot, double delinter, const ImpState* imp, int center_sel, double* uimp,
                      cudaStream_t s) {
   const double inv = 1.0 / delinter;  // correctly rounded (IEEE division)
-  k_potenimp<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, x, y, z, potion, npot, delinter, inv,
+  const dim3 grid((g.nx + kBX * kPX - 1) / (kBX * kPX), (g.ny + kBY - 1) / kBY, g.nz);
+  k_potenimp<<<grid, dim3(kBX, kBY), 0, s>>>(g, x, y, z, potion, npot, delinter, inv,
                                                       const_cast<ImpState*>(imp), center_sel, uimp);
 }
 int launch_force(const Grid& g, const Stencil& st, const double* den, const double* uimp, double* dx,
