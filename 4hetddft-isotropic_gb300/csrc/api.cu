@@ -1010,9 +1010,6 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   if (c.npot < 2 || !(c.delinter > 0)) return bad("bad potential table");
   if (c.precision != HE4G_PREC_FP64 && c.precision != HE4G_PREC_MIXED && c.precision != HE4G_PREC_DF64)
     return bad("unsupported precision");
-  if (c.precision == HE4G_PREC_DF64 &&
-      !(fft_reg_supported(c.nx / 2) && fft_reg_supported(c.ny) && fft_reg_supported(c.nz)))
-    return bad("HE4G_PREC_DF64 needs nx/2, ny and nz in {16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 256}");
   if (c.precision == HE4G_PREC_DF64 && c.core == HE4G_CORE_OTC)
     return bad("HE4G_PREC_DF64 supports core OT (the alpha_s term of core OTC runs in FP64 or mixed precision)");
   r->prec = c.precision;
@@ -1409,8 +1406,6 @@ constexpr int kMaxLtx = 5;
 
 bool tiles_fit(const he4g_run* r, const FftTiles& t) {
   if (t.engine & ~fft_reg_engines(r->prec, r->plan)) return false;
-  const int all = ENGINE_R2C | ENGINE_C2R | ENGINE_Y | ENGINE_Z;
-  if (r->prec == HE4G_PREC_DF64 && (t.engine & all) != all) return false;  // register engine only
   if (t.lpb_r2c < 1 || t.lpb_r2c > kMaxLpb || t.lpb_c2r < 1 || t.lpb_c2r > kMaxLpb) return false;
   if (t.ltx_y < 0 || t.ltx_y > kMaxLtx || t.ltx_z < 0 || t.ltx_z > kMaxLtx) return false;
   return fft_smem_bytes(r->prec, PASS_R2C, r->plan, t.lpb_r2c) && fft_smem_bytes(r->prec, PASS_C2R, r->plan, t.lpb_c2r) &&
@@ -1512,12 +1507,11 @@ int he4g_autotune(he4g_run* r, int reps, int tiles[HE4G_NTILES]) {
     best.*field = best_tile;
     best.engine = best_reg ? (best.engine | bit) : (best.engine & ~bit);
   };
-  if (prec != HE4G_PREC_DF64) {  // df64 has the register engine only
-    sweep(PASS_R2C, 1, kMaxLpb, true, &FftTiles::lpb_r2c, ENGINE_R2C);
-    sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y, ENGINE_Y);
-    sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z, ENGINE_Z);
-    sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r, ENGINE_C2R);
-  } else {
+  sweep(PASS_R2C, 1, kMaxLpb, true, &FftTiles::lpb_r2c, ENGINE_R2C);
+  sweep(PASS_Y, 0, kMaxLtx, false, &FftTiles::ltx_y, ENGINE_Y);
+  sweep(PASS_Z, 0, kMaxLtx, false, &FftTiles::ltx_z, ENGINE_Z);
+  sweep(PASS_C2R, 1, kMaxLpb, true, &FftTiles::lpb_c2r, ENGINE_C2R);
+  if (prec == HE4G_PREC_DF64 && (best.engine & ENGINE_Z)) {
     // the fused z convolution against the split passes, on an evaluation's
     // two z convolutions (one product keeping the forward spectrum, then the
     // sum of two products)

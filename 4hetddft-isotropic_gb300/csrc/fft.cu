@@ -164,12 +164,22 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Grid g, FftAxis ax, const C2
     if (EPI == EPI_POT4) {
       const Functional& fn = pa.fn;
       const C2<R> cg = in.cg;
-      const R a0 = (R)fn.a0, a1 = (R)fn.a1;
+      R k[5];
+      if constexpr (std::is_same<R, df64>::value) {
+        for (int i = 0; i < 5; ++i) k[i] = pa.k[i];  // split on the host
+      } else {
+        k[0] = (R)fn.a0;
+        k[1] = (R)fn.a1;
+        k[2] = (R)fn.beta_solid;
+        k[3] = (R)fn.den_m;
+        k[4] = (R)fn.c_solid;
+      }
+      const R a0 = k[0], a1 = k[1];
       R p0 = fma(cg.x * cg.x, fma(a1, cg.x, a0), v.x);
       R p1 = fma(cg.y * cg.y, fma(a1, cg.y, a0), v.y);
       if (fn.lsolid) {
         const C2<R> d = in.d;
-        const R beta = (R)fn.beta_solid, dm = (R)fn.den_m, cs = (R)fn.c_solid;
+        const R beta = k[2], dm = k[3], cs = k[4];
         p0 += solid_penalty<R>(d.x, beta, dm, cs);
         p1 += solid_penalty<R>(d.y, beta, dm, cs);
       }
@@ -341,6 +351,22 @@ template <>
 const float2* twx_of<float>(const FftPlan& p) {
   return p.twxf;
 }
+template <>
+const df2* twx_of<df64>(const FftPlan& p) {
+  return p.twxd;
+}
+
+// pot4 epilogue constants: df64 takes them split on the host (a device split
+// of a double issues conversions on the FP64 pipe)
+template <typename R>
+Pot4Args<R> pot4_args(const void* dencg, const void* den, const Functional& fn) {
+  Pot4Args<R> pa{static_cast<const R*>(dencg), static_cast<const R*>(den), fn};
+  if constexpr (std::is_same<R, df64>::value) {
+    const double k[5] = {fn.a0, fn.a1, fn.beta_solid, fn.den_m, fn.c_solid};
+    for (int i = 0; i < 5; ++i) pa.k[i] = df64(k[i]);
+  }
+  return pa;
+}
 
 // Shared memory of one block of each pass for a tile (lines per block for the
 // x passes, log2 of the kx columns for y/z); twiddles included.
@@ -385,10 +411,11 @@ void y_impl(const Grid& g, const FftPlan& p, void* const* specs, int nspec, int 
   }
 }
 
+// returns whether the register engine ran the convolution
 template <typename R>
-void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors,
+bool zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* outs, const void* const* factors,
                 int nout, double scale, const void* add, const ZExtra& zx, cudaStream_t s) {
-  if ((p.tiles.engine & ENGINE_Z) && reg_z<R>(g, p, in, outs, factors, nout, scale, add, zx, s)) return;
+  if ((p.tiles.engine & ENGINE_Z) && reg_z<R>(g, p, in, outs, factors, nout, scale, add, zx, s)) return true;
   const int ltx = p.tiles.ltx_z;
   const int TX = 1 << ltx;
   FactorList<R> fl{};
@@ -402,8 +429,9 @@ void zconv_impl(const Grid& g, const FftPlan& p, const void* in, void* const* ou
   const size_t smem = smem_of<R>(PASS_Z, p, ltx);
   set_smem(k_z_conv<R>, smem);
   dim3 grid((g.nxh + TX - 1) / TX, g.ny);
-  k_z_conv<R><<<grid, kThreads, smem, s>>>(g, p.z, static_cast<const C2<R>*>(in), fl, nout, (R)scale,
+  k_z_conv<R><<<grid, kThreads, smem, s>>>(g, p.z, static_cast<const C2<R>*>(in), fl, nout, R(scale),
                                            static_cast<const C2<R>*>(add), ltx);
+  return false;
 }
 
 template <typename R>
@@ -425,7 +453,7 @@ void c2r_impl(const Grid& g, const FftPlan& p, const void* const* ins, void* con
 template <typename R>
 void pot4_impl(const Grid& g, const FftPlan& p, const void* conv, const void* dencg, const void* den,
                const Functional& fn, void* pot4, cudaStream_t s) {
-  Pot4Args<R> pa{static_cast<const R*>(dencg), static_cast<const R*>(den), fn};
+  const Pot4Args<R> pa = pot4_args<R>(dencg, den, fn);
   const C2<R>* c = static_cast<const C2<R>*>(conv);
   R* o = static_cast<R*>(pot4);
   if ((p.tiles.engine & ENGINE_C2R) && reg_c2r<R>(g, p, twx_of<R>(p), EPI_POT4, c, c, o, o, 1, pa, s)) return;
@@ -441,19 +469,16 @@ void pot4_impl(const Grid& g, const FftPlan& p, const void* conv, const void* de
 }  // namespace
 
 // -------------------------------------------------------------- launchers
-// HE4G_PREC_DF64 runs the register engine only (its lengths are checked when
-// the run is created); its spectra are complex df64 and its real fields df64.
-namespace {
-const df2* twxd(const FftPlan& p) { return p.twxd; }
-}  // namespace
-
+// Each pass runs the register engine where the plan's engine bits and the
+// length allow it, else the generic kernels; HE4G_PREC_DF64 instantiates
+// both with complex df64 spectra and df64 real fields.
 void fft_x_r2c(const Grid& g, const FftPlan& p, int prec, const void* in, void* out, cudaStream_t s) {
   if (prec == HE4G_PREC_FP64)
     launch_r2c<double, PRO_PLAIN>(g, p, static_cast<const double*>(in), nullptr, 0.0, 0.0,
                                   static_cast<double2*>(out), s);
   else if (prec == HE4G_PREC_DF64)
-    reg_r2c<df64>(g, p, twxd(p), PRO_PLAIN, static_cast<const df64*>(in), nullptr, df64(0), df64(0),
-                  static_cast<df2*>(out), s);
+    launch_r2c<df64, PRO_PLAIN>(g, p, static_cast<const df64*>(in), nullptr, df64(0), df64(0),
+                                static_cast<df2*>(out), s);
   else
     launch_r2c<float, PRO_PLAIN>(g, p, static_cast<const float*>(in), nullptr, 0.f, 0.f,
                                  static_cast<float2*>(out), s);
@@ -464,8 +489,8 @@ void fft_x_r2c_corr(const Grid& g, const FftPlan& p, int prec, const void* den, 
     launch_r2c<double, PRO_CORR>(g, p, static_cast<const double*>(den), static_cast<const double*>(dencg), cp4,
                                  cpp4, static_cast<double2*>(out), s);
   else if (prec == HE4G_PREC_DF64)
-    reg_r2c<df64>(g, p, twxd(p), PRO_CORR, static_cast<const df64*>(den), static_cast<const df64*>(dencg),
-                  df64(cp4), df64(cpp4), static_cast<df2*>(out), s);
+    launch_r2c<df64, PRO_CORR>(g, p, static_cast<const df64*>(den), static_cast<const df64*>(dencg), df64(cp4),
+                               df64(cpp4), static_cast<df2*>(out), s);
   else
     launch_r2c<float, PRO_CORR>(g, p, static_cast<const float*>(den), static_cast<const float*>(dencg),
                                 (float)cp4, (float)cpp4, static_cast<float2*>(out), s);
@@ -476,8 +501,8 @@ void fft_x_r2c_prod(const Grid& g, const FftPlan& p, int prec, const void* a, co
     launch_r2c<double, PRO_PROD>(g, p, static_cast<const double*>(a), static_cast<const double*>(b), 0.0, 0.0,
                                  static_cast<double2*>(out), s);
   else if (prec == HE4G_PREC_DF64)
-    reg_r2c<df64>(g, p, twxd(p), PRO_PROD, static_cast<const df64*>(a), static_cast<const df64*>(b), df64(0),
-                  df64(0), static_cast<df2*>(out), s);
+    launch_r2c<df64, PRO_PROD>(g, p, static_cast<const df64*>(a), static_cast<const df64*>(b), df64(0), df64(0),
+                               static_cast<df2*>(out), s);
   else
     launch_r2c<float, PRO_PROD>(g, p, static_cast<const float*>(a), static_cast<const float*>(b), 0.f, 0.f,
                                 static_cast<float2*>(out), s);
@@ -486,7 +511,7 @@ void fft_y(const Grid& g, const FftPlan& p, int prec, void* const* specs, int ns
   if (prec == HE4G_PREC_FP64)
     y_impl<double>(g, p, specs, nspec, sign, s);
   else if (prec == HE4G_PREC_DF64)
-    reg_y<df64>(g, p, specs, nspec, sign, s);
+    y_impl<df64>(g, p, specs, nspec, sign, s);
   else
     y_impl<float>(g, p, specs, nspec, sign, s);
 }
@@ -499,8 +524,8 @@ int fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* 
     return 1;
   }
   if (prec == HE4G_PREC_DF64) {
-    reg_z<df64>(g, p, in, outs, factors, nout, scale, add, zx, s);
-    if (!(p.tiles.engine & ENGINE_ZSPLIT)) return 1;
+    if (!zconv_impl<df64>(g, p, in, outs, factors, nout, scale, add, zx, s) || !(p.tiles.engine & ENGINE_ZSPLIT))
+      return 1;
     return add2 ? 2 : 1 + nout;
   }
   zconv_impl<float>(g, p, in, outs, factors, nout, scale, add, zx, s);
@@ -508,30 +533,21 @@ int fft_z_conv(const Grid& g, const FftPlan& p, int prec, const void* in, void* 
 }
 void fft_x_c2r(const Grid& g, const FftPlan& p, int prec, const void* const* ins, void* const* outs, int nspec,
                cudaStream_t s) {
-  if (prec == HE4G_PREC_FP64) {
+  if (prec == HE4G_PREC_FP64)
     c2r_impl<double>(g, p, ins, outs, nspec, s);
-  } else if (prec == HE4G_PREC_DF64) {
-    const df2* i0 = static_cast<const df2*>(ins[0]);
-    df64* o0 = static_cast<df64*>(outs[0]);
-    reg_c2r<df64>(g, p, twxd(p), EPI_STORE, i0, nspec > 1 ? static_cast<const df2*>(ins[1]) : i0, o0,
-                  nspec > 1 ? static_cast<df64*>(outs[1]) : o0, nspec, Pot4Args<df64>{}, s);
-  } else {
+  else if (prec == HE4G_PREC_DF64)
+    c2r_impl<df64>(g, p, ins, outs, nspec, s);
+  else
     c2r_impl<float>(g, p, ins, outs, nspec, s);
-  }
 }
 void fft_x_c2r_pot4(const Grid& g, const FftPlan& p, int prec, const void* conv, const void* dencg,
                     const void* den, const Functional& fn, void* pot4, cudaStream_t s) {
-  if (prec == HE4G_PREC_FP64) {
+  if (prec == HE4G_PREC_FP64)
     pot4_impl<double>(g, p, conv, dencg, den, fn, pot4, s);
-  } else if (prec == HE4G_PREC_DF64) {
-    const Pot4Args<df64> pa{static_cast<const df64*>(dencg), static_cast<const df64*>(den), fn,
-                            {df64(fn.a0), df64(fn.a1), df64(fn.beta_solid), df64(fn.den_m), df64(fn.c_solid)}};
-    const df2* c = static_cast<const df2*>(conv);
-    df64* o = static_cast<df64*>(pot4);
-    reg_c2r<df64>(g, p, twxd(p), EPI_POT4, c, c, o, o, 1, pa, s);
-  } else {
+  else if (prec == HE4G_PREC_DF64)
+    pot4_impl<df64>(g, p, conv, dencg, den, fn, pot4, s);
+  else
     pot4_impl<float>(g, p, conv, dencg, den, fn, pot4, s);
-  }
 }
 
 bool fft_x_c2r_corr(const Grid& g, const FftPlan& p, int prec, void* spec, void* dencg, const void* den, double cp4,
@@ -541,7 +557,7 @@ bool fft_x_c2r_corr(const Grid& g, const FftPlan& p, int prec, void* spec, void*
     return reg_c2r_corr<double>(g, p, twx_of<double>(p), static_cast<double2*>(spec), static_cast<double*>(dencg),
                                 static_cast<const double*>(den), cp4, cpp4, s);
   if (prec == HE4G_PREC_DF64)
-    return reg_c2r_corr<df64>(g, p, twxd(p), static_cast<df2*>(spec), static_cast<df64*>(dencg),
+    return reg_c2r_corr<df64>(g, p, twx_of<df64>(p), static_cast<df2*>(spec), static_cast<df64*>(dencg),
                               static_cast<const df64*>(den), df64(cp4), df64(cpp4), s);
   return reg_c2r_corr<float>(g, p, twx_of<float>(p), static_cast<float2*>(spec), static_cast<float*>(dencg),
                              static_cast<const float*>(den), (float)cp4, (float)cpp4, s);
@@ -591,7 +607,7 @@ void fft_prepare(int prec, const FftPlan& p) {
   if (prec == HE4G_PREC_FP64) {
     prepare_impl<double>(p);
   } else if (prec == HE4G_PREC_DF64) {
-    prepare_reg<df64>(p);
+    prepare_impl<df64>(p);
   } else {
     prepare_impl<float>(p);
     if (p.tiles.engine & ENGINE_XY) {
@@ -610,7 +626,7 @@ int fft_reg_engines(int prec, const FftPlan& p) {
   if (fft_reg_supported(p.y.n)) e |= ENGINE_Y;
   if (fft_reg_supported(p.z.n)) e |= ENGINE_Z;
   if (prec == HE4G_PREC_MIXED && fft_xy_supported(p.xh.n, p.y.n)) e |= ENGINE_XY;
-  if (prec == HE4G_PREC_DF64) e |= ENGINE_ZSPLIT;
+  if (prec == HE4G_PREC_DF64 && fft_reg_supported(p.z.n)) e |= ENGINE_ZSPLIT;
   return e;
 }
 
@@ -631,7 +647,7 @@ FftTiles fft_default_tiles(int prec, const FftPlan& p) {
   // split z convolution of df64 is the default from nz = 192 on (at nz = 256
   // the fused kernel's two 64 KB line buffers leave one block per SM)
   t.engine = fft_reg_engines(prec, p) & ~(ENGINE_XY | ENGINE_ZSPLIT);
-  if (prec == HE4G_PREC_DF64 && p.z.n >= 192) t.engine |= ENGINE_ZSPLIT;
+  if (prec == HE4G_PREC_DF64 && p.z.n >= 192 && fft_reg_supported(p.z.n)) t.engine |= ENGINE_ZSPLIT;
   return t;
 }
 

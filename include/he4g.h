@@ -58,8 +58,9 @@ extern "C" {
  * uimp and the force) in paired-FP32 ("double-float", df64) arithmetic:
  * 48-bit significands, about 2^-48 relative rounding, at FP32 instruction
  * rates; the block partials of the sums and the impurity stay FP64. The ABI
- * takes and returns FP64 values as in HE4G_PREC_FP64. Core OT only; needs
- * nx/2, ny and nz in {16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 256}. */
+ * takes and returns FP64 values as in HE4G_PREC_FP64. Core OT only; the
+ * grids of the other forms (its FFT passes use the register engine where the
+ * length has a specialisation, the generic kernels elsewhere). */
 #define HE4G_PREC_FP64 0
 #define HE4G_PREC_MIXED 1
 #define HE4G_PREC_DF64 2
@@ -310,8 +311,8 @@ void he4g_batch_destroy(he4g_batch* batch);
  * only for lengths it is specialised for: 16, 20, 24, 32, 40, 48, 64, 80, 96,
  * 128, 160, 192, 256); bit 16 fuses the y passes with the x passes per z
  * plane on thread-block clusters (mixed precision, nx/2 x ny planes
- * 128 x 256 and 64 x 128); bit 32 (HE4G_PREC_DF64, which runs every pass on
- * the register engine) splits each z convolution into a forward pass and one
+ * 128 x 256 and 64 x 128); bit 32 (HE4G_PREC_DF64, with the z pass on the
+ * register engine) splits each z convolution into a forward pass and one
  * product-and-inverse pass per output. No reference counterpart (FFTW picks
  * its own plans in fft.f90:5-153).
  *

@@ -135,14 +135,47 @@ def test_df64_tracks_the_fp64_form():
     b.close()
 
 
-def test_lengths_without_a_register_pass_are_refused():
-    """nx/2 = 36 has no register specialisation: df64 refuses the grid at
-    creation instead of falling back to another arithmetic."""
+def test_lengths_without_a_register_pass_run_the_generic_kernels():
+    """nx/2 = 36 and nz = 72 have no register specialisation: those passes
+    run the generic Stockham kernels in df64 (ny = 64 keeps the register y
+    pass), and the run meets the oracle at the form's tolerances."""
     import he4gpu
-    cfg = he4gpu.default_config(72, 64, 64, 14.4, precision=DF64)
-    with pytest.raises(he4gpu.He4gError) as err:
-        he4gpu.Run(cfg)
-    assert err.value.code == he4gpu.abi.HE4G_EINVAL
+    from oracle import oracle
+    cfg = he4gpu.default_config(72, 64, 72, 14.4, 12.8, 14.4, precision=DF64)
+    c64 = he4gpu.default_config(72, 64, 72, 14.4, 12.8, 14.4)
+    for c in (cfg, c64):
+        c.deltat = 1.3092e-5
+    rng = np.random.default_rng(5)
+    x = -14.4 + 0.4 * np.arange(72)
+    y = -12.8 + 0.4 * np.arange(64)
+    z = -14.4 + 0.4 * np.arange(72)
+    r2 = z[:, None, None] ** 2 + y[None, :, None] ** 2 + x[None, None, :] ** 2
+    rho = 0.0218 / (1.0 + np.exp((np.sqrt(r2) - 8.0) / 0.8))
+    psi = np.sqrt(rho) * np.exp(1j * 1e-3 * rng.standard_normal(rho.shape))
+    # off the grid's axes: a distance that is an exact multiple of the table
+    # spacing is where the reference's int(r/d), mod(r,d)/d pair steps a node
+    # and the one-quotient lookup of this form does not
+    r, v = np.array([0.317, -0.243, -11.05]), np.array([0.0, 0.0, 2.0])
+    tk = {"selec": "Xe_He", "r_cutoff": 2.55, "umax": 2793.9365463}
+    g = gpu_run(cfg, tk, psi, r, v)
+    assert g.tiles[4] & 1 == 0 and g.tiles[4] & 8 == 0  # x and z passes: generic kernels
+    assert g.tiles[4] & 4  # y: register engine
+    o = oracle_run(c64, tk, psi, r, v)
+    assert rel_field(g.field("uimp"), o.field("uimp")) < UIMP_TOL
+    for name in ("dencg", "delj4", "pot4"):
+        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
+    g.step(6)
+    o.step(6)
+    assert rel_field(g.den, o.den) < STEP_TOL
+    assert rel_field(g.psi, o.psi) < STEP_TOL
+    eg, eo = g.energy(), o.energy()
+    for k in eo:
+        assert abs(eg[k] - eo[k]) <= STEP_TOL * max(abs(eo[k]), 1e-3), k
+    rg, vg, _ = g.impurity()
+    ro, vo, _ = o.impurity()
+    assert rel_vec(rg, ro) < STEP_TOL and rel_vec(vg, vo) < STEP_TOL
+    g.close()
+    o.close()
 
 
 def test_split_and_fused_z_convolutions_agree():
