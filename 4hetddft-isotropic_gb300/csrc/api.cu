@@ -439,6 +439,8 @@ void conv_dev(he4g_run* r, const void* a, const void* b, const void* tab, void* 
 void grad1_dev(he4g_run* r, int axis, const void* in, void* out) {
   if (mixed(r))
     launch_grad1_f(r->g, r->stf, axis, static_cast<const float*>(in), static_cast<float*>(out), r->s);
+  else if (dfm(r))
+    launch_grad1_df(r->g, r->std, axis, static_cast<const df64*>(in), static_cast<df64*>(out), r->s);
   else
     launch_grad1(r->g, r->st, axis, static_cast<const double*>(in), static_cast<double*>(out), r->s);
 }
@@ -446,12 +448,15 @@ void grad1_dev(he4g_run* r, int axis, const void* in, void* out) {
 // term_alfa (term_alfa.f90:5-117) and pot4 += ualphas (poten.f90:96-107)
 void alpha_s_dev(he4g_run* r) {
   const Grid& g = r->g;
-  const bool mp = mixed(r);
+  const bool mp = mixed(r), df = dfm(r);
+  const df64 inv_den0s = df_of(1.0L / static_cast<long double>(r->cfg.den0s));
   {
     Tick t(r, F_ALPHA_S);
     if (mp)
       launch_falfs_f(g, static_cast<const float*>(r->denalf), static_cast<float>(r->cfg.den0s),
                      static_cast<float*>(r->falfs), r->s);
+    else if (df)
+      launch_falfs_df(g, static_cast<const df64*>(r->denalf), inv_den0s, static_cast<df64*>(r->falfs), r->s);
     else
       launch_falfs(g, static_cast<const double*>(r->denalf), r->cfg.den0s, static_cast<double*>(r->falfs), r->s);
   }
@@ -465,6 +470,10 @@ void alpha_s_dev(he4g_run* r) {
                     static_cast<const float*>(r->dz), static_cast<const float*>(r->ix),
                     static_cast<const float*>(r->iy), static_cast<const float*>(r->iz), static_cast<float*>(r->t1),
                     r->s);
+    else if (df)
+      launch_dot3_df(g, static_cast<const df64*>(r->dx), static_cast<const df64*>(r->dy),
+                     static_cast<const df64*>(r->dz), static_cast<const df64*>(r->ix), static_cast<const df64*>(r->iy),
+                     static_cast<const df64*>(r->iz), static_cast<df64*>(r->t1), r->s);
     else
       launch_dot3(g, static_cast<const double*>(r->dx), static_cast<const double*>(r->dy),
                   static_cast<const double*>(r->dz), static_cast<const double*>(r->ix),
@@ -479,6 +488,11 @@ void alpha_s_dev(he4g_run* r) {
                          static_cast<const float*>(r->iy), static_cast<const float*>(r->iz),
                          static_cast<float*>(r->ualphas), static_cast<float*>(r->t1), static_cast<float*>(r->t2),
                          static_cast<float*>(r->t3), static_cast<float>(r->cfg.den0s), r->s);
+    } else if (df) {
+      launch_ualphas_a_df(g, static_cast<const df64*>(r->falfs), static_cast<const df64*>(r->ix),
+                          static_cast<const df64*>(r->iy), static_cast<const df64*>(r->iz),
+                          static_cast<df64*>(r->ualphas), static_cast<df64*>(r->t1), static_cast<df64*>(r->t2),
+                          static_cast<df64*>(r->t3), inv_den0s, r->s);
     } else {
       launch_ualphas_a(g, static_cast<const double*>(r->falfs), static_cast<const double*>(r->ix),
                        static_cast<const double*>(r->iy), static_cast<const double*>(r->iz),
@@ -493,6 +507,11 @@ void alpha_s_dev(he4g_run* r) {
                          static_cast<const float*>(r->t5), static_cast<const float*>(r->t6),
                          static_cast<float>(r->cfg.h2o2m4), static_cast<float>(r->cfg.alphas),
                          static_cast<float*>(r->pot4), r->s);
+    else if (df)
+      launch_ualphas_b_df(g, static_cast<df64*>(r->ualphas), static_cast<const df64*>(r->t4),
+                          static_cast<const df64*>(r->t5), static_cast<const df64*>(r->t6),
+                          df_of(static_cast<long double>(r->cfg.h2o2m4) * static_cast<long double>(r->cfg.alphas)),
+                          static_cast<df64*>(r->pot4), r->s);
     else
       launch_ualphas_b(g, static_cast<double*>(r->ualphas), static_cast<const double*>(r->t4),
                        static_cast<const double*>(r->t5), static_cast<const double*>(r->t6), r->cfg.h2o2m4,
@@ -1010,8 +1029,6 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   if (c.npot < 2 || !(c.delinter > 0)) return bad("bad potential table");
   if (c.precision != HE4G_PREC_FP64 && c.precision != HE4G_PREC_MIXED && c.precision != HE4G_PREC_DF64)
     return bad("unsupported precision");
-  if (c.precision == HE4G_PREC_DF64 && c.core == HE4G_CORE_OTC)
-    return bad("HE4G_PREC_DF64 supports core OT (the alpha_s term of core OTC runs in FP64 or mixed precision)");
   r->prec = c.precision;
   r->rs = mixed(r) ? 4 : 8;
   if (cudaStreamCreateWithFlags(&r->s, cudaStreamNonBlocking) != cudaSuccess) return bad("no CUDA device");
@@ -1898,10 +1915,12 @@ int he4g_get_field(he4g_run* r, int which, double* out) {
     case 5:
     case 6: {
       void* d = which == 4 ? r->dx : which == 5 ? r->dy : r->dz;
-      if (dfm(r)) {  // the FP64 stencil on the converted density; d is FP64
+      if (dfm(r)) {
+        // the FP64 stencil on the converted density, into the dencg mirror
+        // (a readback scratch): the df64 gradients of core OTC stay intact
         launch_df_to_f64(static_cast<const df64*>(r->den), r->m_den, r->g.n, r->s);
-        launch_grad1(r->g, r->st, which - 4, r->m_den, static_cast<double*>(d), r->s);
-        cudaError_t e = cudaMemcpyAsync(out, d, sizeof(double) * r->g.n, cudaMemcpyDeviceToHost, r->s);
+        launch_grad1(r->g, r->st, which - 4, r->m_den, r->m_dencg, r->s);
+        cudaError_t e = cudaMemcpyAsync(out, r->m_dencg, sizeof(double) * r->g.n, cudaMemcpyDeviceToHost, r->s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
         return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "get_field");
       }
@@ -2023,11 +2042,20 @@ int he4g_energy(he4g_run* r, he4g_energies* en) {
                            static_cast<const float*>(r->iz), r->xs, r->ys, r->zs, r->partials, r->s);
   } else {
     view = f64_view(r);
-    launch_energy_point(g, r->fn, view.den, view.dencg, view.delj4, view.uimp,
-                        otc ? static_cast<const double*>(r->falfs) : nullptr, static_cast<const double*>(r->dx),
-                        static_cast<const double*>(r->dy), static_cast<const double*>(r->dz),
-                        static_cast<const double*>(r->ix), static_cast<const double*>(r->iy),
-                        static_cast<const double*>(r->iz), r->xs, r->ys, r->zs, r->partials, r->s);
+    const void* ot[7] = {r->falfs, r->dx, r->dy, r->dz, r->ix, r->iy, r->iz};
+    const double* o64[7];
+    for (int i = 0; i < 7; ++i) o64[i] = static_cast<const double*>(ot[i]);
+    if (otc && dfm(r)) {
+      // the alpha_s inputs of E_alpha as FP64, in scratch arrays that the
+      // next poten rewrites (t1..t6 hold n values, spec2 at least n)
+      void* tmp[7] = {r->t1, r->t2, r->t3, r->t4, r->t5, r->t6, r->spec2};
+      for (int i = 0; i < 7; ++i) {
+        launch_df_to_f64(static_cast<const df64*>(ot[i]), static_cast<double*>(tmp[i]), g.n, r->s);
+        o64[i] = static_cast<const double*>(tmp[i]);
+      }
+    }
+    launch_energy_point(g, r->fn, view.den, view.dencg, view.delj4, view.uimp, otc ? o64[0] : nullptr, o64[1],
+                        o64[2], o64[3], o64[4], o64[5], o64[6], r->xs, r->ys, r->zs, r->partials, r->s);
   }
   launch_reduce(r->partials, r->pblocks, 12, r->small, r->s);
   cudaMemsetAsync(r->small + 40, 0, sizeof(double) * 3, r->s);

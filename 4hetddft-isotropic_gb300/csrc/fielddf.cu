@@ -500,6 +500,62 @@ __global__ void __launch_bounds__(256, 4) k_force_df(Grid g, StencilD st, const 
   }
 }
 
+// ------------------------------------------------------ alpha_s (core OTC)
+// term_alfa (term_alfa.f90:5-117) and pot4 += ualphas (poten.f90:96-107):
+// the operations of field.cu's FP64 kernels in df64. The divisions by den0s
+// are products with its df64 reciprocal and h2o2m4 * alphas is one df64
+// factor, both split on the host.
+__global__ void __launch_bounds__(256) k_grad1_df(Grid g, StencilD st, int axis, const df64* __restrict__ in,
+                                                   df64* out) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const long long s = axis == 0 ? 1 : axis == 1 ? (long long)g.nx : (long long)g.nx * g.ny;
+  const int c = axis == 0 ? t.i : axis == 1 ? t.j : t.k;
+  const int nl = axis == 0 ? g.nx : axis == 1 ? g.ny : g.nz;
+  const df64 zero(0.f, 0.f);
+  Acc acc{0.f, 0.f};
+#pragma unroll
+  for (int o = 1; o <= kStencilHalf; ++o) {
+    const df64 a = c - o >= 0 ? __ldg(in + t.p - o * s) : zero;
+    const df64 b = c + o < nl ? __ldg(in + t.p + o * s) : zero;
+    const df64 co = axis == 0 ? st.d1[0][o] : axis == 1 ? st.d1[1][o] : st.d1[2][o];
+    acc_pair<-1>(acc, co, a, b);
+  }
+  sts(out + t.p, acc_value(acc));
+}
+__global__ void k_falfs_df(Grid g, const df64* __restrict__ denalf, df64 inv_den0s, df64* falfs) {
+  const Pt t = point(g);
+  if (t.ok) sts(falfs + t.p, df64(1) - __ldg(denalf + t.p) * inv_den0s);
+}
+__global__ void k_dot3_df(Grid g, const df64* __restrict__ ax, const df64* __restrict__ ay,
+                          const df64* __restrict__ az, const df64* __restrict__ bx, const df64* __restrict__ by,
+                          const df64* __restrict__ bz, df64* out) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const df64 v = fma(__ldg(az + t.p), __ldg(bz + t.p),
+                     fma(__ldg(ay + t.p), __ldg(by + t.p), __ldg(ax + t.p) * __ldg(bx + t.p)));
+  sts(out + t.p, v);
+}
+__global__ void k_ualphas_a_df(Grid g, const df64* __restrict__ falfs, const df64* __restrict__ ix,
+                               const df64* __restrict__ iy, const df64* __restrict__ iz, df64* u, df64* s1, df64* s2,
+                               df64* s3, df64 inv_den0s) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const df64 f = __ldg(falfs + t.p);
+  sts(u + t.p, u[t.p] * inv_den0s);
+  sts(s1 + t.p, f * __ldg(ix + t.p));
+  sts(s2 + t.p, f * __ldg(iy + t.p));
+  sts(s3 + t.p, f * __ldg(iz + t.p));
+}
+__global__ void k_ualphas_b_df(Grid g, df64* u, const df64* __restrict__ s4, const df64* __restrict__ s5,
+                               const df64* __restrict__ s6, df64 h2alphas, df64* pot4) {
+  const Pt t = point(g);
+  if (!t.ok) return;
+  const df64 v = (((u[t.p] + __ldg(s4 + t.p)) + __ldg(s5 + t.p)) + __ldg(s6 + t.p)) * h2alphas;
+  sts(u + t.p, v);
+  sts(pot4 + t.p, pot4[t.p] + v);
+}
+
 // ------------------------------------------------------------ conversions
 __global__ void k_df_from_f64(const double* __restrict__ in, df64* __restrict__ out, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -574,6 +630,25 @@ int launch_force_df(const Grid& g, const StencilD& st, const df64* den, const Im
 
 void launch_potenimp_df(const Grid& g, const ImpTableD& tab, ImpState* imp, int sel, df64* uimp, cudaStream_t s) {
   k_potenimp_df<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, tab, imp, sel, uimp);
+}
+
+void launch_grad1_df(const Grid& g, const StencilD& st, int axis, const df64* in, df64* out, cudaStream_t s) {
+  k_grad1_df<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, st, axis, in, out);
+}
+void launch_falfs_df(const Grid& g, const df64* denalf, df64 inv_den0s, df64* falfs, cudaStream_t s) {
+  k_falfs_df<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, denalf, inv_den0s, falfs);
+}
+void launch_dot3_df(const Grid& g, const df64* ax, const df64* ay, const df64* az, const df64* bx, const df64* by,
+                    const df64* bz, df64* out, cudaStream_t s) {
+  k_dot3_df<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, ax, ay, az, bx, by, bz, out);
+}
+void launch_ualphas_a_df(const Grid& g, const df64* falfs, const df64* ix, const df64* iy, const df64* iz, df64* u,
+                         df64* s1, df64* s2, df64* s3, df64 inv_den0s, cudaStream_t s) {
+  k_ualphas_a_df<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, falfs, ix, iy, iz, u, s1, s2, s3, inv_den0s);
+}
+void launch_ualphas_b_df(const Grid& g, df64* u, const df64* s4, const df64* s5, const df64* s6, df64 h2alphas,
+                         df64* pot4, cudaStream_t s) {
+  k_ualphas_b_df<<<point_grid(g), dim3(kBX, kBY), 0, s>>>(g, u, s4, s5, s6, h2alphas, pot4);
 }
 
 void launch_df_from_f64(const double* in, df64* out, long long n, cudaStream_t s) {

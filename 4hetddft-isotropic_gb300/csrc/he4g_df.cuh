@@ -44,6 +44,16 @@ void launch_rk_stage_df(const Grid& g, const StencilD& st, df64 h2o2m4, const df
 int launch_force_df(const Grid& g, const StencilD& st, const df64* den, const ImpTableD& tab, ImpState* imp,
                     int sel, df64* uimp_out, double* partials, const ForceFinish& fin, cudaStream_t s);
 void launch_potenimp_df(const Grid& g, const ImpTableD& tab, ImpState* imp, int sel, df64* uimp, cudaStream_t s);
+// term_alfa in df64 (core OTC): one-axis first derivative, falfs = 1 -
+// denalf/den0s, the dot product, and the two pointwise stages of ualphas
+void launch_grad1_df(const Grid& g, const StencilD& st, int axis, const df64* in, df64* out, cudaStream_t s);
+void launch_falfs_df(const Grid& g, const df64* denalf, df64 inv_den0s, df64* falfs, cudaStream_t s);
+void launch_dot3_df(const Grid& g, const df64* ax, const df64* ay, const df64* az, const df64* bx, const df64* by,
+                    const df64* bz, df64* out, cudaStream_t s);
+void launch_ualphas_a_df(const Grid& g, const df64* falfs, const df64* ix, const df64* iy, const df64* iz, df64* u,
+                         df64* s1, df64* s2, df64* s3, df64 inv_den0s, cudaStream_t s);
+void launch_ualphas_b_df(const Grid& g, df64* u, const df64* s4, const df64* s5, const df64* s6, df64 h2alphas,
+                         df64* pot4, cudaStream_t s);
 // conversions of n values between FP64 and df64 arrays
 void launch_df_from_f64(const double* in, df64* out, long long n, cudaStream_t s);
 void launch_df_to_f64(const df64* in, double* out, long long n, cudaStream_t s);

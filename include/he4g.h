@@ -58,9 +58,9 @@ extern "C" {
  * uimp and the force) in paired-FP32 ("double-float", df64) arithmetic:
  * 48-bit significands, about 2^-48 relative rounding, at FP32 instruction
  * rates; the block partials of the sums and the impurity stay FP64. The ABI
- * takes and returns FP64 values as in HE4G_PREC_FP64. Core OT only; the
- * grids of the other forms (its FFT passes use the register engine where the
- * length has a specialisation, the generic kernels elsewhere). */
+ * takes and returns FP64 values as in HE4G_PREC_FP64. Cores OT and OTC,
+ * and the grids of the other forms (its FFT passes use the register engine
+ * where the length has a specialisation, the generic kernels elsewhere). */
 #define HE4G_PREC_FP64 0
 #define HE4G_PREC_MIXED 1
 #define HE4G_PREC_DF64 2

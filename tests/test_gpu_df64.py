@@ -112,13 +112,28 @@ def test_reference_routines_compose_like_the_driver():
     b.close()
 
 
-def test_otc_core_is_refused():
-    """The alpha_s term of core OTC has no df64 kernels: the form refuses it."""
-    import he4gpu
+def test_otc_alpha_s_matches_oracle():
+    """Core OTC (lsolid off) in df64: term_alfa and E_alpha (term_alfa.f90,
+    energy.f90:99-105) at the FP64 form's tolerances."""
     cfg, tk, psi, r, v, meta = make_case("he100_xe_32", core=1, lsolid=0, hcg=2.190323, precision=DF64)
-    with pytest.raises(he4gpu.He4gError) as err:
-        gpu_run(cfg, tk, psi, r, v)
-    assert err.value.code == he4gpu.abi.HE4G_EINVAL
+    g = gpu_run(cfg, tk, psi, r, v)
+    o = oracle_run(cfg, tk, psi, r, v)
+    for name in ("denalf", "ualphas", "pot4", "dencg"):
+        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
+    for name in ("dxden", "dyden", "dzden"):
+        assert rel_field(g.field(name), o.field(name)) < FIELD_TOL, name
+    eg, eo = g.energy(), o.energy()
+    assert eo["ealphas"] != 0.0
+    assert abs(eg["ealphas"] - eo["ealphas"]) <= 1e-11 * abs(eo["ealphas"])
+    g.step(5)
+    o.step(5)
+    assert rel_field(g.den, o.den) < STEP_TOL
+    assert rel_field(g.psi, o.psi) < STEP_TOL
+    eg, eo = g.energy(), o.energy()
+    for k in eo:
+        assert abs(eg[k] - eo[k]) <= STEP_TOL * max(abs(eo[k]), 1e-3), k
+    g.close()
+    o.close()
 
 
 def test_df64_tracks_the_fp64_form():
