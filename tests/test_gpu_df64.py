@@ -193,6 +193,24 @@ def test_lengths_without_a_register_pass_run_the_generic_kernels():
     o.close()
 
 
+def test_generic_and_register_passes_agree():
+    """Every pass on the generic kernels (tiles bits 0) against every pass on
+    the register engine (the default) on the same df64 run: the same
+    butterflies in another order, so equal to rounding."""
+    cfg, tk, psi, r, v, meta = make_case("he300_ar_48", precision=DF64)
+    a = gpu_run(cfg, tk, psi, r, v)
+    b = gpu_run(cfg, tk, psi, r, v)
+    assert a.tiles[4] & 15 == 15
+    b.tiles = b.tiles[:4] + (0,)
+    a.step(6)
+    b.step(6)
+    assert rel_field(b.psi, a.psi) < 1e-12
+    assert rel_field(b.field("pot4"), a.field("pot4")) < 1e-12
+    assert rel_vec(b.impurity()[0], a.impurity()[0]) < 1e-13
+    a.close()
+    b.close()
+
+
 def test_split_and_fused_z_convolutions_agree():
     """The z convolution as one fused kernel or as a forward pass plus one
     product-and-inverse pass per output (tiles bit 32): the same products,
