@@ -150,10 +150,15 @@ def test_step_before_state_is_an_error():
     assert e.value.code == he4gpu.abi.HE4G_ESTATE
 
 
-def test_zero_density_stops_like_steprk():
-    """A density that is not > 0 after an RK stage is an error (steprk.f90:89-92)."""
+FORMS = [0, 1, 2]  # FP64, mixed, df64
+
+
+@pytest.mark.parametrize("precision", FORMS)
+def test_zero_density_stops_like_steprk(precision):
+    """A density that is not > 0 after an RK stage is an error (steprk.f90:89-92),
+    in every arithmetic form (the check is on |psi|^2 in FP64 in each)."""
     import he4gpu
-    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", precision=precision)
     psi = psi.copy()
     # a slab of exact zeros deeper than the stencil half-width: its first plane
     # has only zero neighbours, so H.psi = 0 there and den stays 0
@@ -164,12 +169,13 @@ def test_zero_density_stops_like_steprk():
     assert e.value.code == he4gpu.abi.HE4G_EDENSITY
 
 
-def test_zero_density_stops_a_long_call_near_the_failing_step():
+@pytest.mark.parametrize("precision", FORMS)
+def test_zero_density_stops_a_long_call_near_the_failing_step(precision):
     """A he4g_step call of many steps stops within 2 * 8 steps of the step
     whose density check failed, and names that step (the reference STOPs in
     that step, steprk.f90:89-92)."""
     import he4gpu
-    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", precision=precision)
     psi = psi.copy()
     psi[0:8, :, :] = 0.0
     run = gpu_run(cfg, tk, psi, r, v)
@@ -180,9 +186,10 @@ def test_zero_density_stops_a_long_call_near_the_failing_step():
     assert "end of step 1 " in str(e.value)
 
 
-def test_impurity_beyond_table_is_an_error():
+@pytest.mark.parametrize("precision", FORMS)
+def test_impurity_beyond_table_is_an_error(precision):
     import he4gpu
-    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    cfg, tk, psi, r, v, meta = make_case("he100_xe_32", precision=precision)
     far = np.array([0.0, 0.0, -10.0 * meta["zmax"]])
     with pytest.raises(he4gpu.He4gError) as e:
         gpu_run(cfg, tk, psi, far, v)
