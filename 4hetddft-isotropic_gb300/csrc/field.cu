@@ -254,27 +254,6 @@ __device__ __forceinline__ double div_rn(double a, double d, double inv) {
   return __fma_rn(e, inv, q0);
 }
 
-// trunc(q) of a non-negative q, as an integer (returned) and as a double
-// (qt), from q's bits: the conversion instructions (and comparisons) of
-// doubles issue on the FP64 pipe, which bounds this kernel, and integer
-// operations do not. Negative, NaN, infinite and q >= 2^62 return -1, which
-// the table check rejects (a saturated conversion could overflow ir + 1).
-__device__ __forceinline__ long long trunc_nonneg(double q, double& qt) {
-  const long long b = __double_as_longlong(q);
-  const int e = (int)((b >> 52) & 0x7FF) - 1023;  // unbiased exponent
-  qt = 0.0;
-  if ((b << 1) == 0) return 0;  // +0 and -0
-  if (b < 0 || e >= 62) return -1;
-  if (e < 0) return 0;  // 0 < q < 1
-  const long long m = (b & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL;
-  if (e >= 52) {
-    qt = q;
-    return m << (e - 52);
-  }
-  qt = __longlong_as_double(b & ~((1LL << (52 - e)) - 1));
-  return m >> (52 - e);
-}
-
 // updatepoten (potenimp.f90:71-95): linear interpolation of the radial
 // table at r = |x - center|. Every rounding step is explicit so that uimp
 // matches a CPU evaluation of the same expression bit for bit. A thread

@@ -9,7 +9,50 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 namespace he4g {
+
+// bit patterns of doubles on either side
+__host__ __device__ __forceinline__ long long dbits(double d) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(d);
+#else
+  long long b;
+  std::memcpy(&b, &d, sizeof b);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ double dfrom(long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(b);
+#else
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+// trunc(q) of a non-negative q, as an integer (returned) and as a double
+// (qt), from q's bits: the conversion instructions of doubles issue on the
+// FP64 pipe, integer operations do not. Negative, NaN, infinite and
+// q >= 2^62 return -1 (qt = 0), which a table bounds check rejects; +0 and
+// -0 return 0.
+__host__ __device__ __forceinline__ long long trunc_nonneg(double q, double& qt) {
+  const long long b = dbits(q);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;  // unbiased exponent
+  qt = 0.0;
+  if ((b << 1) == 0) return 0;
+  if (b < 0 || e >= 62) return -1;
+  if (e < 0) return 0;  // 0 < q < 1
+  const long long m = (b & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL;
+  if (e >= 52) {
+    qt = q;
+    return m << (e - 52);
+  }
+  qt = dfrom(b & ~((1LL << (52 - e)) - 1));
+  return m >> (52 - e);
+}
 
 // double -> float, round to nearest even; |x| < 2^-126 gives signed zero,
 // overflow gives signed infinity, NaN stays NaN.
