@@ -1,0 +1,180 @@
+"""The oracle against a second, independent restatement in numpy of the same
+Fortran lines: the mean field (poten.f90:5-118 and, for core OTC,
+term_alfa.f90:5-117) and one whole Runge-Kutta-Gill step (steprk.f90:21-150,
+with updatepoten, poten and forceimp between its stages). The numpy side uses
+numpy's FFTs, the 13-point rows of blockds.f (tests/golden/stencil_rows.json)
+with zero padding (icon = 13), and the oracle's form-factor and impurity
+tables (pinned by their own known answers). Agreement to rounding rules out a
+slip in either restatement of the field formulas, the FFT scaling, the order
+of the convolutions, the Gill coefficients and the impurity update."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL = 1e-12  # relative to each field's maximum: FFT rounding of two implementations
+
+
+def _state(nx, ny, nz, h, seed):
+    rng = np.random.default_rng(seed)
+    x = (np.arange(nx) - nx // 2) * h
+    y = (np.arange(ny) - ny // 2) * h
+    z = (np.arange(nz) - nz // 2) * h
+    r = np.sqrt(z[:, None, None] ** 2 + y[None, :, None] ** 2 + x[None, None, :] ** 2)
+    rho = 0.0218 / (1.0 + np.exp((r - 0.3 * nx * h) / 0.8))
+    return np.sqrt(rho) * np.exp(1j * 1e-3 * rng.standard_normal(rho.shape))
+
+
+def _grad1(f, axis, h, row):
+    """13-point first derivative along numpy axis `axis`, zero padded."""
+    n = f.shape[axis]
+    pad = [(0, 0)] * 3
+    pad[axis] = (6, 6)
+    fp = np.pad(f, pad)
+    out = np.zeros_like(f)
+    for k, c in enumerate(row):
+        if c == 0.0:
+            continue
+        sl = [slice(None)] * 3
+        sl[axis] = slice(k, k + n)
+        out += c * fp[tuple(sl)]
+    return out / h
+
+
+def _mean_field(cfg, tabs, den, row):
+    shape = den.shape
+    nh = (shape[0], shape[1], shape[2] // 2 + 1)
+    wcgk = tabs["wcgk"].reshape(nh)
+    fvlj4 = tabs["fvlj4"].reshape(nh)
+    conv = lambda f, k: np.fft.irfftn(np.fft.rfftn(f) * k, s=shape, axes=(0, 1, 2))  # noqa: E731
+    fden = np.fft.rfftn(den)
+    dencg = np.fft.irfftn(fden * wcgk, s=shape, axes=(0, 1, 2))
+    delj4 = np.fft.irfftn(fden * fvlj4, s=shape, axes=(0, 1, 2))
+    g = den * dencg * (cfg.cp4 + cfg.cpp4 * dencg)
+    a0, a1 = cfg.cp4 / 2.0, cfg.cpp4 / 3.0
+    pot4 = delj4 + dencg ** 2 * (a0 + a1 * dencg) + conv(g, wcgk)
+    out = {"dencg": dencg, "delj4": delj4}
+    if cfg.core == 1:  # OTC: term_alfa
+        kalfs = tabs["kalfs"].reshape(nh)
+        h = [2 * cfg.xmax / cfg.nx, 2 * cfg.ymax / cfg.ny, 2 * cfg.zmax / cfg.nz]
+        grads = [_grad1(den, 2 - a, h[a], row) for a in range(3)]  # x, y, z
+        denalf = np.fft.irfftn(fden * kalfs, s=shape, axes=(0, 1, 2))
+        falfs = 1.0 - denalf / cfg.den0s
+        ints = [conv(falfs * gr, kalfs) for gr in grads]
+        s1 = sum(gr * it for gr, it in zip(grads, ints))
+        ua = conv(s1, kalfs) / cfg.den0s
+        div = sum(_grad1(falfs * ints[a], 2 - a, h[a], row) for a in range(3))
+        ualphas = (ua + div) * cfg.h2o2m4 * cfg.alphas
+        pot4 = pot4 + ualphas
+        out.update(denalf=denalf, ualphas=ualphas)
+    if cfg.lsolid:
+        t = np.tanh(cfg.beta_solid * (den - cfg.den_m))
+        pot4 = pot4 + cfg.c_solid * (1.0 + t + cfg.beta_solid * den * (1.0 - t * t))
+    out["pot4"] = pot4
+    return out
+
+
+@pytest.mark.parametrize("core,lsolid,dims", [(0, 1, (24, 20, 30)), (1, 0, (20, 24, 16)), (0, 0, (32, 32, 32))])
+def test_mean_field_matches_numpy(oracle_mod, he4gpu_mod, core, lsolid, dims):
+    nx, ny, nz = dims
+    h = 0.45
+    cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2, core=core, lsolid=lsolid)
+    tabs = oracle_mod.build_tables(cfg)
+    row = json.load(open(os.path.join(GOLDEN, "stencil_rows.json")))["d1"]["centre_row"]
+    psi = _state(nx, ny, nz, h, seed=11)
+    o = oracle_mod.OracleRun(cfg, tabs)
+    o.set_state(psi, np.array([0.31, -0.22, -0.4 * nz * h]), np.array([0.0, 0.0, 2.0]))
+    ref = _mean_field(cfg, tabs, np.abs(psi) ** 2, row)
+    # The penalty's 1 + tanh(beta (rho - rho_m)) cancels to ~1e-12 inside the
+    # droplet, where one ulp of tanh near -1 between two libm implementations
+    # moves C (1 + t + ...) by C * 2^-53: allowed on pot4 as an absolute term.
+    slack = {"pot4": 8 * 2.0 ** -53 * cfg.c_solid if lsolid else 0.0}
+    for name, want in ref.items():
+        got = o.field(name)
+        err = np.max(np.abs(got - want))
+        assert err < TOL * np.max(np.abs(want)) + slack.get(name, 0.0), (name, err)
+    o.close()
+
+
+def _grad2(f, axis, h, row):
+    """13-point second derivative along numpy axis `axis`, zero padded."""
+    return _grad1(f, axis, 1.0, row) / (h * h)
+
+
+def _uimp(cfg, tabs, rimp):
+    """updatepoten (potenimp.f90:71-95): int(r/d) and mod(r,d)/d."""
+    h = [2 * cfg.xmax / cfg.nx, 2 * cfg.ymax / cfg.ny, 2 * cfg.zmax / cfg.nz]
+    x = -cfg.xmax + h[0] * np.arange(cfg.nx)
+    y = -cfg.ymax + h[1] * np.arange(cfg.ny)
+    z = -cfg.zmax + h[2] * np.arange(cfg.nz)
+    zt = (z - rimp[2]) ** 2
+    yt = (y[None, :] - rimp[1]) ** 2 + zt[:, None]
+    r = np.sqrt((x[None, None, :] - rimp[0]) ** 2 + yt[:, :, None])
+    ir = (r / cfg.delinter).astype(np.int64)
+    w = np.fmod(r, cfg.delinter) / cfg.delinter
+    pot = tabs["potion"]
+    return pot[ir] * (1.0 - w) + pot[ir + 1] * w
+
+
+def _force(cfg, den, uimp, row):
+    """forceimp (potenimp.f90:24-55): -sum(grad(den) * uimp) * dxyz."""
+    h = [2 * cfg.xmax / cfg.nx, 2 * cfg.ymax / cfg.ny, 2 * cfg.zmax / cfg.nz]
+    dxyz = h[0] * h[1] * h[2]
+    return np.array([-np.sum(_grad1(den, 2 - a, h[a], row) * uimp) * dxyz for a in range(3)])
+
+
+def test_rk_gill_step_matches_numpy(oracle_mod, he4gpu_mod):
+    """One Runge-Kutta-Gill step (steprk.f90:21-150: four stages, the mean
+    field, uimp and the force re-evaluated after stages 1-3) restated in
+    numpy on the oracle's tables and timec, against the oracle's steprk."""
+    gold = json.load(open(os.path.join(GOLDEN, "stencil_rows.json")))
+    r1, r2 = gold["d1"]["centre_row"], gold["d2"]["centre_row"]
+    nx, ny, nz, h = 24, 20, 30, 0.45
+    cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2)
+    cfg.deltat = 1.3092e-5
+    tabs = oracle_mod.build_tables(cfg)
+    psi = _state(nx, ny, nz, h, seed=12)
+    rimp, vimp = np.array([0.31, -0.22, -5.2]), np.array([0.05, 0.0, 2.0])
+    o = oracle_mod.OracleRun(cfg, tabs)
+    o.set_state(psi, rimp, vimp)
+    timec = o.timec_array()
+    hs = [2 * cfg.xmax / nx, 2 * cfg.ymax / ny, 2 * cfg.zmax / nz]
+    mass = cfg.mimpur * 0.02061484  # mimpur * mp_u (modules.f90:315, DFT4He3d.f90:205)
+    # the state set_state leaves: the first evaluation, q = qr = qv = 0
+    uimp = _uimp(cfg, tabs, rimp)
+    den = np.abs(psi) ** 2
+    pot4 = _mean_field(cfg, tabs, den, r1)["pot4"]
+    aimp = _force(cfg, den, uimp, r1) / mass
+    q = np.zeros_like(psi)
+    qr, qv = np.zeros(3), np.zeros(3)
+    s2 = np.sqrt(2.0)
+    a = [0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 1.0 / 6.0]
+    b = [2.0, 1.0, 1.0, 2.0]
+    c = [0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 0.5]
+    dt = cfg.deltat
+    for j in range(4):
+        lap = sum(_grad2(psi, 2 - ax, hs[ax], r2) for ax in range(3))
+        s4 = timec * (lap * cfg.h2o2m4 - pot4 * psi) - 1j * uimp * psi
+        s1 = a[j] * (s4 - b[j] * q)
+        q = q + 3.0 * s1 - c[j] * s4
+        psi = psi + dt * s1
+        aux = a[j] * (vimp - b[j] * qr)
+        qr = qr + 3.0 * aux - c[j] * vimp
+        rimp = rimp + dt * aux
+        aux = a[j] * (aimp - b[j] * qv)
+        qv = qv + 3.0 * aux - c[j] * aimp
+        vimp = vimp + dt * aux
+        if j < 3:
+            den = np.abs(psi) ** 2
+            uimp = _uimp(cfg, tabs, rimp)
+            pot4 = _mean_field(cfg, tabs, den, r1)["pot4"]
+            aimp = _force(cfg, den, uimp, r1) / mass
+    o.steprk(dt)
+    assert np.max(np.abs(o.psi - psi)) < 1e-13 * np.max(np.abs(psi))
+    ro, vo, ao = o.impurity()
+    assert np.max(np.abs(ro - rimp)) < 1e-13 * np.max(np.abs(rimp))
+    assert np.max(np.abs(vo - vimp)) < 1e-12 * np.max(np.abs(vimp))
+    assert np.max(np.abs(ao - aimp)) < 1e-9 * np.max(np.abs(aimp))
+    o.close()
