@@ -1,7 +1,9 @@
 """The oracle against a second, independent restatement in numpy of the same
 Fortran lines: the mean field (poten.f90:5-118 and, for core OTC,
-term_alfa.f90:5-117) and one whole Runge-Kutta-Gill step (steprk.f90:21-150,
-with updatepoten, poten and forceimp between its stages). The numpy side uses
+term_alfa.f90:5-117), one whole Runge-Kutta-Gill step (steprk.f90:21-150,
+with updatepoten, poten and forceimp between its stages), and the driver loop
+(DFT4He3d.f90:834-852) over three RK-Gill and three Hamming PMC steps
+(steppc.f90:1-178) with their history arrays and index rotations. The numpy side uses
 numpy's FFTs, the 13-point rows of blockds.f (tests/golden/stencil_rows.json)
 with zero padding (icon = 13), and the oracle's form-factor and impurity
 tables (pinned by their own known answers). Agreement to rounding rules out a
@@ -177,4 +179,144 @@ def test_rk_gill_step_matches_numpy(oracle_mod, he4gpu_mod):
     assert np.max(np.abs(ro - rimp)) < 1e-13 * np.max(np.abs(rimp))
     assert np.max(np.abs(vo - vimp)) < 1e-12 * np.max(np.abs(vimp))
     assert np.max(np.abs(ao - aimp)) < 1e-9 * np.max(np.abs(aimp))
+    o.close()
+
+
+class _NumpyRun:
+    """The driver loop DFT4He3d.f90:834-852 (steprk for the first three
+    steps, steppc after, then potenimp/poten/forceimp at rimp) with the
+    history arrays and index rotations of steprk.f90 and steppc.f90,
+    Fortran slots 1..3 as list indices 0..2."""
+
+    def __init__(self, cfg, tabs, psi, rimp, vimp, rows):
+        self.cfg, self.tabs, self.r1, self.r2 = cfg, tabs, rows[0], rows[1]
+        self.h = [2 * cfg.xmax / cfg.nx, 2 * cfg.ymax / cfg.ny, 2 * cfg.zmax / cfg.nz]
+        self.mass = cfg.mimpur * 0.02061484
+        self.psi, self.rimp, self.vimp = psi.copy(), rimp.copy(), vimp.copy()
+        self.q = np.zeros_like(psi)
+        self.pc = np.zeros_like(psi)
+        self.psiold = [np.zeros_like(psi) for _ in range(3)]
+        self.hpsiold = [np.zeros_like(psi) for _ in range(2)]
+        self.qr, self.qv, self.pcr, self.pcv = (np.zeros(3) for _ in range(4))
+        self.rimpold = [np.zeros(3) for _ in range(3)]
+        self.vimpold = [np.zeros(3) for _ in range(3)]
+        self.aimpold = [np.zeros(3) for _ in range(2)]
+        self.ioldp, self.ioldr, self.ioldv = [0, 1, 2], [0, 1, 2], [0, 1, 2]
+        self.ioldh, self.iolda = [0, 1], [0, 1]
+        self.timec = None
+        self.nstep = 0
+        self.evaluate(self.rimp)
+
+    def evaluate(self, at):
+        den = np.abs(self.psi) ** 2
+        self.uimp = _uimp(self.cfg, self.tabs, at)
+        self.pot4 = _mean_field(self.cfg, self.tabs, den, self.r1)["pot4"]
+        self.aimp = _force(self.cfg, den, self.uimp, self.r1) / self.mass
+
+    def hpsi(self):
+        lap = sum(_grad2(self.psi, 2 - ax, self.h[ax], self.r2) for ax in range(3))
+        return self.timec * (lap * self.cfg.h2o2m4 - self.pot4 * self.psi) - 1j * self.uimp * self.psi
+
+    def steprk(self, dt):
+        s2 = np.sqrt(2.0)
+        a = [0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 1.0 / 6.0]
+        b = [2.0, 1.0, 1.0, 2.0]
+        c = [0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 0.5]
+        for j in range(4):
+            s4 = self.hpsi()
+            s1 = a[j] * (s4 - b[j] * self.q)
+            self.q = self.q + 3.0 * s1 - c[j] * s4
+            if j == 0:
+                self.hpsiold[1] = self.hpsiold[0]
+                self.hpsiold[0] = s4
+                self.psiold[2], self.psiold[1], self.psiold[0] = self.psiold[1], self.psiold[0], self.psi
+            self.psi = self.psi + dt * s1
+            aux = a[j] * (self.vimp - b[j] * self.qr)
+            self.qr = self.qr + 3.0 * aux - c[j] * self.vimp
+            if j == 0:
+                self.rimpold[2], self.rimpold[1], self.rimpold[0] = self.rimpold[1], self.rimpold[0], self.rimp
+            self.rimp = self.rimp + dt * aux
+            aux = a[j] * (self.aimp - b[j] * self.qv)
+            self.qv = self.qv + 3.0 * aux - c[j] * self.aimp
+            if j == 0:
+                self.aimpold[1], self.aimpold[0] = self.aimpold[0], self.aimp
+                self.vimpold[2], self.vimpold[1], self.vimpold[0] = self.vimpold[1], self.vimpold[0], self.vimp
+            self.vimp = self.vimp + dt * aux
+            if j < 3:
+                self.evaluate(self.rimp)
+        self.ioldp, self.ioldr, self.ioldv = [0, 1, 2], [0, 1, 2], [0, 1, 2]
+        self.ioldh, self.iolda = [0, 1], [0, 1]
+
+    def steppc(self, dt):
+        c112, c9, c4o3 = 112.0 / 121.0, 9.0 / 121.0, 4.0 / 3.0
+        P, H, R, V, A = self.ioldp, self.ioldh, self.ioldr, self.ioldv, self.iolda
+        s4 = self.hpsi()
+        s1 = self.psiold[P[2]] + c4o3 * dt * (2.0 * s4 - self.hpsiold[H[0]] + 2.0 * self.hpsiold[H[1]])
+        self.psiold[P[2]] = self.psi
+        self.psi = s1 - c112 * self.pc
+        self.pc = s1
+        self.hpsiold[H[1]] = s4
+        H[0], H[1] = H[1], H[0]
+        aux = self.rimpold[R[2]] + c4o3 * dt * (2.0 * self.vimp - self.vimpold[V[0]] + 2.0 * self.vimpold[V[1]])
+        self.rimpold[R[2]] = aux - c112 * self.pcr
+        self.pcr = aux
+        aux = self.vimpold[V[2]] + c4o3 * dt * (2.0 * self.aimp - self.aimpold[A[0]] + 2.0 * self.aimpold[A[1]])
+        self.vimpold[V[2]] = aux - c112 * self.pcv
+        self.pcv = aux
+        self.aimpold[A[1]] = self.aimp
+        A[0], A[1] = A[1], A[0]
+        self.evaluate(self.rimpold[R[2]])
+        s4 = self.hpsi()
+        s5 = 0.125 * (9.0 * self.psiold[P[2]] - self.psiold[P[1]]
+                      + 3.0 * dt * (s4 + 2.0 * self.hpsiold[H[0]] - self.hpsiold[H[1]]))
+        self.pc = self.pc - s5
+        self.psi = s5 + c9 * self.pc
+        P[0], P[1], P[2] = P[2], P[0], P[1]
+        aux = 0.125 * (9.0 * self.rimp - self.rimpold[R[1]]
+                       + 3.0 * dt * (self.vimpold[V[2]] + 2.0 * self.vimp - self.vimpold[V[0]]))
+        self.pcr = self.pcr - aux
+        self.rimpold[R[2]] = self.rimp
+        self.rimp = aux + c9 * self.pcr
+        R[0], R[1], R[2] = R[2], R[0], R[1]
+        aux = 0.125 * (9.0 * self.vimp - self.vimpold[V[1]]
+                       + 3.0 * dt * (self.aimp + 2.0 * self.aimpold[A[0]] - self.aimpold[A[1]]))
+        self.pcv = self.pcv - aux
+        self.vimpold[V[2]] = self.vimp
+        self.vimp = aux + c9 * self.pcv
+        V[0], V[1], V[2] = V[2], V[0], V[1]
+
+    def step(self, dt):
+        self.nstep += 1
+        if self.nstep <= 3:
+            self.steprk(dt)
+        else:
+            self.steppc(dt)
+        self.evaluate(self.rimp)
+
+
+def test_rk_and_pc_steps_match_numpy(oracle_mod, he4gpu_mod):
+    """Three Runge-Kutta-Gill steps and three Hamming predictor-modifier-
+    corrector steps (steppc.f90:1-178, the impurity predictor stored into
+    rimpold(:,ioldr(3)) and the field evaluated there) of the driver loop,
+    restated in numpy, against the oracle's step."""
+    gold = json.load(open(os.path.join(GOLDEN, "stencil_rows.json")))
+    rows = (gold["d1"]["centre_row"], gold["d2"]["centre_row"])
+    nx, ny, nz, h = 20, 24, 16, 0.45
+    cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2)
+    cfg.deltat = 1.3092e-5
+    tabs = oracle_mod.build_tables(cfg)
+    psi = _state(nx, ny, nz, h, seed=13)
+    rimp, vimp = np.array([0.27, -0.31, -2.9]), np.array([0.04, -0.02, 2.0])
+    o = oracle_mod.OracleRun(cfg, tabs)
+    o.set_state(psi, rimp, vimp)
+    ref = _NumpyRun(cfg, tabs, psi, rimp, vimp, rows)
+    ref.timec = o.timec_array()
+    for n in range(6):
+        ref.step(cfg.deltat)
+        o.step(1)
+        assert np.max(np.abs(o.psi - ref.psi)) < 1e-12 * np.max(np.abs(ref.psi)), n
+        ro, vo, ao = o.impurity()
+        assert np.max(np.abs(ro - ref.rimp)) < 1e-13 * np.max(np.abs(ref.rimp)), n
+        assert np.max(np.abs(vo - ref.vimp)) < 1e-11 * np.max(np.abs(ref.vimp)), n
+        assert np.max(np.abs(ao - ref.aimp)) < 1e-8 * np.max(np.abs(ref.aimp)), n
     o.close()
