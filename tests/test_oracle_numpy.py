@@ -3,7 +3,8 @@ Fortran lines: the mean field (poten.f90:5-118 and, for core OTC,
 term_alfa.f90:5-117), one whole Runge-Kutta-Gill step (steprk.f90:21-150,
 with updatepoten, poten and forceimp between its stages), and the driver loop
 (DFT4He3d.f90:834-852) over three RK-Gill and three Hamming PMC steps
-(steppc.f90:1-178) with their history arrays and index rotations. The numpy side uses
+(steppc.f90:1-178) with their history arrays and index rotations, and the
+energy components (energy.f90:12-144). The numpy side uses
 numpy's FFTs, the 13-point rows of blockds.f (tests/golden/stencil_rows.json)
 with zero padding (icon = 13), and the oracle's form-factor and impurity
 tables (pinned by their own known answers). Agreement to rounding rules out a
@@ -319,4 +320,63 @@ def test_rk_and_pc_steps_match_numpy(oracle_mod, he4gpu_mod):
         assert np.max(np.abs(ro - ref.rimp)) < 1e-13 * np.max(np.abs(ref.rimp)), n
         assert np.max(np.abs(vo - ref.vimp)) < 1e-11 * np.max(np.abs(ref.vimp)), n
         assert np.max(np.abs(ao - ref.aimp)) < 1e-8 * np.max(np.abs(ref.aimp)), n
+    o.close()
+
+
+def _energy(cfg, tabs, psi, rimp, vimp, r1):
+    """energy.f90:12-144 on a state (psi, impurity at rimp with velocity vimp)."""
+    h = [2 * cfg.xmax / cfg.nx, 2 * cfg.ymax / cfg.ny, 2 * cfg.zmax / cfg.nz]
+    dxyz = h[0] * h[1] * h[2]
+    den = np.abs(psi) ** 2
+    mf = _mean_field(cfg, tabs, den, r1)
+    dencg, delj4 = mf["dencg"], mf["delj4"]
+    e = {}
+    e["ekin4"] = cfg.h2o2m4 * sum(np.sum(np.abs(_grad1(psi, 2 - a, h[a], r1)) ** 2) for a in range(3)) * dxyz
+    e["elj4"] = 0.5 * np.sum(delj4 * den) * dxyz
+    e["ecor4"] = np.sum(den * dencg ** 2 * (0.5 * cfg.cp4 + cfg.cpp4 / 3.0 * dencg)) * dxyz
+    e["esolid"] = 0.0
+    if cfg.lsolid:
+        e["esolid"] = cfg.c_solid * np.sum(den * (1.0 + np.tanh(cfg.beta_solid * (den - cfg.den_m)))) * dxyz
+    e["ealphas"] = 0.0
+    if cfg.core == 1:
+        nh = (den.shape[0], den.shape[1], den.shape[2] // 2 + 1)
+        kalfs = tabs["kalfs"].reshape(nh)
+        fden = np.fft.rfftn(den)
+        denalf = np.fft.irfftn(fden * kalfs, s=den.shape, axes=(0, 1, 2))
+        falfs = 1.0 - denalf / cfg.den0s
+        grads = [_grad1(den, 2 - a, h[a], r1) for a in range(3)]
+        ints = [np.fft.irfftn(np.fft.rfftn(falfs * g) * kalfs, s=den.shape, axes=(0, 1, 2)) for g in grads]
+        e["ealphas"] = -cfg.h2o2m4 * 0.5 * cfg.alphas * np.sum(falfs * sum(g * i for g, i in zip(grads, ints))) * dxyz
+    e["eext"] = 0.0
+    e["etot4"] = e["ekin4"] + e["elj4"] + e["ecor4"] + e["esolid"] + e["ealphas"]
+    e["ekinx"] = 0.5 * cfg.mimpur * 0.02061484 * np.sum(vimp * vimp)
+    e["eHeX"] = np.sum(_uimp(cfg, tabs, rimp) * den) * dxyz
+    e["eimpu"] = e["ekinx"] + e["eHeX"]
+    e["etot"] = e["etot4"] + e["eimpu"]
+    return e, np.sum(den) * dxyz
+
+
+@pytest.mark.parametrize("core,lsolid", [(0, 1), (1, 0)])
+def test_energy_matches_numpy(oracle_mod, he4gpu_mod, core, lsolid):
+    """energy.f90 restated in numpy on the oracle's state, at set_state and
+    after 4 steps; each component to 1e-12 of its size (the solid term, whose
+    1 + tanh cancels to ~1e-12, to 8 ulps of C * N on the same libm argument)."""
+    gold = json.load(open(os.path.join(GOLDEN, "stencil_rows.json")))
+    r1 = gold["d1"]["centre_row"]
+    nx, ny, nz, h = 24, 20, 30, 0.45
+    cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2, core=core, lsolid=lsolid)
+    cfg.deltat = 1.3092e-5
+    tabs = oracle_mod.build_tables(cfg)
+    o = oracle_mod.OracleRun(cfg, tabs)
+    o.set_state(_state(nx, ny, nz, h, seed=14), np.array([0.21, 0.33, -5.0]), np.array([0.1, 0.0, 2.0]))
+    for steps in (0, 4):
+        if steps:
+            o.step(steps)
+        r, v, _ = o.impurity()
+        want, npart = _energy(cfg, tabs, o.psi, r, v, r1)
+        got = o.energy()
+        slack = 8 * 2.0 ** -53 * cfg.c_solid * npart if lsolid else 0.0
+        for k, w in want.items():
+            tol = 1e-12 * abs(w) + (slack if k in ("esolid", "etot4", "etot") else 0.0) + 1e-300
+            assert abs(got[k] - w) <= tol, (steps, k, got[k], w)
     o.close()
