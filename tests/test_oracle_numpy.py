@@ -3,8 +3,9 @@ Fortran lines: the mean field (poten.f90:5-118 and, for core OTC,
 term_alfa.f90:5-117), one whole Runge-Kutta-Gill step (steprk.f90:21-150,
 with updatepoten, poten and forceimp between its stages), and the driver loop
 (DFT4He3d.f90:834-852) over three RK-Gill and three Hamming PMC steps
-(steppc.f90:1-178) with their history arrays and index rotations, and the
-energy components (energy.f90:12-144). The numpy side uses
+(steppc.f90:1-178) with their history arrays and index rotations, the
+energy components (energy.f90:12-144) and the printed observables
+(DFT4He3d.f90:869-943, r_cm.f90:23-58). The numpy side uses
 numpy's FFTs, the 13-point rows of blockds.f (tests/golden/stencil_rows.json)
 with zero padding (icon = 13), and the oracle's form-factor and impurity
 tables (pinned by their own known answers). Agreement to rounding rules out a
@@ -379,4 +380,46 @@ def test_energy_matches_numpy(oracle_mod, he4gpu_mod, core, lsolid):
         for k, w in want.items():
             tol = 1e-12 * abs(w) + (slack if k in ("esolid", "etot4", "etot") else 0.0) + 1e-300
             assert abs(got[k] - w) <= tol, (steps, k, got[k], w)
+    o.close()
+
+
+def test_observables_match_numpy(oracle_mod, he4gpu_mod):
+    """The printed observables of DFT4He3d.f90:869-943: the particle number,
+    the centre of mass (r_cm.f90:23-58, divided by the namelist's n4), the
+    angular momentum <L> about it from the 13-point first derivatives of psi,
+    and <x^2>, <y^2>, <z^2>."""
+    gold = json.load(open(os.path.join(GOLDEN, "stencil_rows.json")))
+    r1 = gold["d1"]["centre_row"]
+    nx, ny, nz, h = 24, 20, 30, 0.45
+    cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2)
+    tabs = oracle_mod.build_tables(cfg)
+    psi = _state(nx, ny, nz, h, seed=15)
+    # a phase that carries angular momentum about an off-centre axis
+    x = -cfg.xmax + h * np.arange(nx)
+    y = -cfg.ymax + h * np.arange(ny)
+    z = -cfg.zmax + h * np.arange(nz)
+    psi = psi * np.exp(1j * 0.3 * (x[None, None, :] * 0.2 - y[None, :, None] * 0.5 + z[:, None, None] * 0.1))
+    o = oracle_mod.OracleRun(cfg, tabs)
+    o.set_state(psi, np.array([0.2, 0.1, -5.0]), np.array([0.0, 0.0, 2.0]))
+    n4 = 300.0
+    got = o.observables(n4)
+    den = np.abs(psi) ** 2
+    dxyz = h ** 3
+    cm = [np.sum(den * x[None, None, :]) * dxyz / n4, np.sum(den * y[None, :, None]) * dxyz / n4,
+          np.sum(den * z[:, None, None]) * dxyz / n4]
+    d = [_grad1(psi, 2 - a, h, r1) for a in range(3)]  # d/dx, d/dy, d/dz
+    X, Y, Z = x[None, None, :] - cm[0], y[None, :, None] - cm[1], z[:, None, None] - cm[2]
+    cps = np.conj(psi)
+    lz = np.sum(1j * cps * (Y * d[0] - X * d[1])) * dxyz
+    ly = np.sum(1j * cps * (X * d[2] - Z * d[0])) * dxyz
+    lx = np.sum(1j * cps * (Z * d[1] - Y * d[2])) * dxyz
+    r2 = [np.sum(den * x[None, None, :] ** 2) * dxyz, np.sum(den * y[None, :, None] ** 2) * dxyz,
+          np.sum(den * z[:, None, None] ** 2) * dxyz]
+    assert abs(got["npart"] - np.sum(den) * dxyz) < 1e-13 * np.sum(den) * dxyz
+    np.testing.assert_allclose(got["cm"], cm, rtol=1e-12, atol=1e-14)
+    lref = np.array([lx, ly, lz])
+    scale = np.max(np.abs(lref))
+    assert np.max(np.abs(np.array(got["ang"]) - lref.real)) < 1e-11 * scale
+    assert np.max(np.abs(np.array(got["ang_im"]) - lref.imag)) < 1e-11 * scale
+    np.testing.assert_allclose(got["r2"], r2, rtol=1e-12)
     o.close()
