@@ -1846,6 +1846,128 @@ int he4g_get_trajectory(he4g_run* r, double* rows, int cap, int* n) {
   return HE4G_OK;
 }
 
+// ----------------------------------------------------------- snapshots
+// A run's time-stepping state as one host blob: a header, then the device
+// arrays by role (psi, the three psi history slots, q, pc, the two H.psi
+// history slots, den, pot4, dencg, delj4, uimp, timec, the FP32 copy of psi
+// in the mixed form, the alpha_s fields of core OTC), the impurity state and
+// the trajectory ring. Roles, not buffers: the history slots rotate by
+// pointer, and a snapshot taken at any arrangement loads into any other.
+extern "C++" {
+namespace {
+struct SnapHeader {
+  char magic[8];
+  int version, prec, nx, ny, nz, otc;
+  int iter, cur32, delj4_valid, imp_bytes;
+  double xmax, ymax, zmax;
+  unsigned long long bytes;
+};
+constexpr char kSnapMagic[8] = {'H', 'E', '4', 'G', 'S', 'N', 'P', '1'};
+struct SnapPart {
+  void* dev;
+  size_t bytes;
+};
+std::vector<SnapPart> snapshot_parts(he4g_run* r) {
+  const size_t n = (size_t)r->g.n, rs = r->rs;
+  std::vector<SnapPart> v;
+  auto add = [&](void* p, size_t b) { v.push_back({p, b}); };
+  add(r->psi, 16 * n);
+  for (int i = 0; i < 3; ++i) add(r->old[i], 16 * n);
+  add(r->q, 16 * n);
+  add(r->pc, 16 * n);
+  for (int i = 0; i < 2; ++i) add(r->h[i], 2 * rs * n);
+  for (void* f : {r->den, r->pot4, r->dencg, r->delj4, r->uimp}) add(f, rs * n);
+  add(r->timec, 4 * n);
+  if (mixed(r)) add(r->psi32[r->cur32], 8 * n);
+  if (r->fn.otc)
+    for (void* f : {r->denalf, r->falfs, r->dx, r->dy, r->dz, r->ix, r->iy, r->iz, r->ualphas}) add(f, rs * n);
+  add(r->imp, sizeof(ImpState));
+  add(r->ring, sizeof(double) * kRingRows * kRingCols);
+  return v;
+}
+unsigned long long snapshot_total(he4g_run* r) {
+  unsigned long long b = sizeof(SnapHeader);
+  for (const SnapPart& p : snapshot_parts(r)) b += p.bytes;
+  return b;
+}
+}  // namespace
+}  // extern "C++"
+
+int he4g_snapshot_bytes(he4g_run* r, uint64_t* bytes) {
+  if (!r || !bytes) return HE4G_EINVAL;
+  *bytes = snapshot_total(r);
+  return HE4G_OK;
+}
+
+int he4g_save_snapshot(he4g_run* r, void* host, uint64_t bytes) {
+  int rc = check_ready(r);
+  if (rc) return rc;
+  if (!host || bytes < snapshot_total(r)) return fail(r, HE4G_EINVAL, "save_snapshot: buffer too small");
+  rc = he4g_wait_psi(r);
+  if (rc) return rc;
+  SnapHeader h{};
+  std::memcpy(h.magic, kSnapMagic, sizeof h.magic);
+  h.version = 1;
+  h.prec = r->prec;
+  h.nx = r->g.nx;
+  h.ny = r->g.ny;
+  h.nz = r->g.nz;
+  h.otc = r->fn.otc ? 1 : 0;
+  h.iter = r->iter;
+  h.cur32 = r->cur32;
+  h.delj4_valid = r->delj4_valid ? 1 : 0;
+  h.imp_bytes = (int)sizeof(ImpState);
+  h.xmax = r->cfg.xmax;
+  h.ymax = r->cfg.ymax;
+  h.zmax = r->cfg.zmax;
+  h.bytes = snapshot_total(r);
+  unsigned char* out = static_cast<unsigned char*>(host);
+  std::memcpy(out, &h, sizeof h);
+  size_t off = sizeof h;
+  cudaError_t e = cudaSuccess;
+  for (const SnapPart& p : snapshot_parts(r)) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out + off, p.dev, p.bytes, cudaMemcpyDeviceToHost, r->s);
+    off += p.bytes;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
+  return e == cudaSuccess ? HE4G_OK : cuda_fail(r, e, "save_snapshot");
+}
+
+int he4g_load_snapshot(he4g_run* r, const void* host, uint64_t bytes) {
+  if (!r || !host || bytes < sizeof(SnapHeader)) return HE4G_EINVAL;
+  SnapHeader h;
+  std::memcpy(&h, host, sizeof h);
+  if (std::memcmp(h.magic, kSnapMagic, sizeof h.magic) != 0 || h.version != 1)
+    return fail(r, HE4G_EINVAL, "load_snapshot: not a snapshot of this library");
+  if (h.prec != r->prec || h.nx != r->g.nx || h.ny != r->g.ny || h.nz != r->g.nz || h.otc != (r->fn.otc ? 1 : 0) ||
+      h.xmax != r->cfg.xmax || h.ymax != r->cfg.ymax || h.zmax != r->cfg.zmax ||
+      h.imp_bytes != (int)sizeof(ImpState) || h.iter < 0 || (h.cur32 != 0 && h.cur32 != 1))
+    return fail(r, HE4G_EINVAL, "load_snapshot: the snapshot belongs to another grid, box, core or form");
+  if (bytes < h.bytes) return fail(r, HE4G_EINVAL, "load_snapshot: truncated buffer");
+  if (h.bytes != snapshot_total(r)) return fail(r, HE4G_EINVAL, "load_snapshot: size mismatch");
+  int rc = he4g_wait_psi(r);
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(r->s);
+  if (e != cudaSuccess) return cuda_fail(r, e, "load_snapshot");
+  r->cur32 = h.cur32;  // before the parts: the mixed form's FP32 copy goes to psi32[cur32]
+  const unsigned char* in = static_cast<const unsigned char*>(host);
+  size_t off = sizeof h;
+  for (const SnapPart& p : snapshot_parts(r)) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p.dev, in + off, p.bytes, cudaMemcpyHostToDevice, r->s);
+    off += p.bytes;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(r->s);
+  if (e != cudaSuccess) return cuda_fail(r, e, "load_snapshot");
+  ImpState imp;
+  std::memcpy(&imp, in + off - sizeof(double) * kRingRows * kRingCols - sizeof(ImpState), sizeof imp);
+  r->iter = h.iter;
+  r->delj4_valid = h.delj4_valid != 0;
+  r->have_state = true;
+  r->ring_read = imp.ring_head;
+  r->hslot = r->hmarks = 0;
+  return HE4G_OK;
+}
+
 int he4g_get_psi(he4g_run* r, double* psi) {
   if (!r || !psi) return HE4G_EINVAL;
   const double2* src = r->psi;

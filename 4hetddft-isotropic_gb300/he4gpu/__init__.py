@@ -278,6 +278,20 @@ class Run:
                               time=time_ps, selec=selec, r_cutoff=r_cutoff, umax=umax, cm=o["cm"],
                               npart=o["npart"], energies=e, ang=o["ang"], r2=o["r2"])
 
+    def save_snapshot(self):
+        """The run's whole time-stepping state (he4g_save_snapshot) as a numpy
+        uint8 array; load_snapshot restores it into a run of the same grid,
+        box, core and form, which then continues bit for bit."""
+        n = C.c_uint64()
+        self._ck(self.lib.he4g_snapshot_bytes(self.h, C.byref(n)))
+        buf = np.empty(n.value, dtype=np.uint8)
+        self._ck(self.lib.he4g_save_snapshot(self.h, buf.ctypes.data_as(C.c_void_p), n.value))
+        return buf
+
+    def load_snapshot(self, buf):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        self._ck(self.lib.he4g_load_snapshot(self.h, buf.ctypes.data_as(C.c_void_p), buf.size))
+
     def read_state(self, path, mode=2):
         """set_state from a reference density / wave-function file (readenc
         modes 0, 2, 3); mode 0 densities become psi = sqrt(den)."""

@@ -373,6 +373,23 @@ int he4g_set_impurity(he4g_run* run, const double r[3], const double v[3], const
 /* Steps taken since the last set_state. */
 int he4g_steps_taken(const he4g_run* run);
 
+/* Checkpoint of a run's whole time-stepping state, taken between steps: psi,
+ * its three history slots, q, pc, the two H.psi history slots, den, pot4,
+ * dencg, delj4, uimp, timec, the impurity state with its integrator history
+ * and index rotations, the trajectory ring (and the FP32 copy of psi of the
+ * mixed form, the alpha_s fields of core OTC), in the run's own arithmetic
+ * form. he4g_snapshot_bytes gives the blob's size; he4g_save_snapshot writes
+ * it into a host buffer of at least that size; he4g_load_snapshot restores it
+ * into a run of the same grid, box, core and form (HE4G_EINVAL otherwise), and
+ * the run continues bit for bit as the saved run would have, in its
+ * predictor-corrector phase if it was there. No reference counterpart: the
+ * reference restarts from printoutc's psi, r and v (readenc mode 2,
+ * readenc.f90:104-113) with three RK-Gill steps (DFT4He3d.f90:840), which
+ * he4g_set_state reproduces. */
+int he4g_snapshot_bytes(he4g_run* run, uint64_t* bytes);
+int he4g_save_snapshot(he4g_run* run, void* host, uint64_t bytes);
+int he4g_load_snapshot(he4g_run* run, const void* host, uint64_t bytes);
+
 /* Average device time (ms) of the kernels of the last he4g_step call, per
  * kernel family; used by the benchmark to compute the roofline figures.
  * names/ms arrays of capacity cap; returns the number of families. */
