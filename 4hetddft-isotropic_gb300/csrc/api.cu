@@ -1619,6 +1619,14 @@ int he4g_set_tiles(he4g_run* r, const int tiles[HE4G_NTILES]) {
   return HE4G_OK;
 }
 
+int he4g_health(he4g_run* r) {
+  if (!r) return HE4G_EINVAL;
+  if (!r->have_state) return fail(r, HE4G_ESTATE, "set_state has not been called");
+  const cudaError_t e = cudaStreamSynchronize(r->s);
+  if (e != cudaSuccess) return cuda_fail(r, e, "health");
+  return health_check(r);
+}
+
 int he4g_step_many(he4g_run** runs, int n, int nsteps) {
   if (!runs || n < 0 || nsteps < 0) return HE4G_EINVAL;
   for (int i = 0; i < n; ++i) {

@@ -278,6 +278,13 @@ class Run:
                               time=time_ps, selec=selec, r_cutoff=r_cutoff, umax=umax, cm=o["cm"],
                               npart=o["npart"], energies=e, ang=o["ang"], r2=o["r2"])
 
+    def health(self):
+        """(code, message) of the run's checks after its queued work
+        (he4g_health): code 0 when healthy; does not raise."""
+        rc = self.lib.he4g_health(self.h)
+        msg = self.lib.he4g_last_error(self.h)
+        return rc, (msg.decode() if rc and msg else "")
+
     def save_snapshot(self):
         """The run's whole time-stepping state (he4g_save_snapshot) as a numpy
         uint8 array; load_snapshot restores it into a run of the same grid,

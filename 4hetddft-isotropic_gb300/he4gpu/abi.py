@@ -135,6 +135,7 @@ SIGNATURES = {
     "he4g_get_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "he4g_set_tiles": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "he4g_steps_taken": (C.c_int, [_P]),
+    "he4g_health": (C.c_int, [_P]),
     "he4g_snapshot_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "he4g_save_snapshot": (C.c_int, [_P, _P, C.c_uint64]),
     "he4g_load_snapshot": (C.c_int, [_P, _P, C.c_uint64]),

@@ -26,7 +26,7 @@ import time
 
 import numpy as np
 
-from . import Run, config_for_case, default_config, footprint, serve_stream, state_for, step_many
+from . import He4gError, Run, config_for_case, default_config, footprint, serve_stream, state_for, step_many
 
 MIXED = 1
 FP64 = 0
@@ -87,12 +87,17 @@ def final_state(run, meta):
     return {"etot": e["etot"], "escale": scale, "norm": run.observables(meta["n4"])["npart"]}
 
 
-def serve(stream, hbm_budget, max_active=64, chunk=16, precision=MIXED, keep_results=(0,)):
+def serve(stream, hbm_budget, max_active=64, chunk=16, precision=MIXED, keep_results=(0,), state_fn=state_for):
     """Runs the request loop over `stream` [(arrival_s, meta)] in wall-clock
     time; returns (report, results of the jobs listed in keep_results). The
-    report's "finals" holds every job's final energy and norm."""
+    report's "finals" holds every job's final energy and norm. state_fn(meta)
+    gives a job's (psi, rimp, vimp). A job whose density check or impurity
+    table check fails inside a chunk (he4g_step_many stops that run only) is
+    evicted and listed in the report's "failed" with its error; the other
+    jobs continue."""
     pending = list(enumerate(stream))
     finals = {}
+    failed = []
     max_resident = 0
     active = []  # dicts: id, run, left, arrival, admitted, bytes, points
     step_lat = []
@@ -111,8 +116,13 @@ def serve(stream, hbm_budget, max_active=64, chunk=16, precision=MIXED, keep_res
                 break
             pending.pop(0)
             run, cfg = make_run(meta, precision)
-            psi, r, v = state_for(meta)
-            run.set_state(psi, r, v)
+            psi, r, v = state_fn(meta)
+            try:
+                run.set_state(psi, r, v)
+            except He4gError as err:  # the first evaluation already fails
+                run.close()
+                failed.append({"id": jid, "code": err.code, "error": str(err)})
+                continue
             used += need
             active.append({"id": jid, "run": run, "left": meta["steps"], "arrival": arr,
                            "admitted": time.perf_counter() - t0, "bytes": need,
@@ -126,7 +136,22 @@ def serve(stream, hbm_budget, max_active=64, chunk=16, precision=MIXED, keep_res
             continue
         k = min(chunk, min(a["left"] for a in active))
         ts = time.perf_counter()
-        step_many([a["run"] for a in active], k)
+        try:
+            step_many([a["run"] for a in active], k)
+        except He4gError:
+            # evict the runs whose checks failed; the others took their k steps
+            bad = []
+            for a in active:
+                code, msg = a["run"].health()
+                if code:
+                    bad.append(a)
+                    failed.append({"id": a["id"], "code": code, "error": msg})
+            if not bad:
+                raise
+            for a in bad:
+                a["run"].close()
+                used -= a["bytes"]
+            active = [a for a in active if a not in bad]
         dt = time.perf_counter() - ts
         for a in active:
             a["left"] -= k
@@ -159,6 +184,7 @@ def serve(stream, hbm_budget, max_active=64, chunk=16, precision=MIXED, keep_res
         "precision": "mixed" if precision == MIXED else "fp64",
         "max_resident": max_resident,
         "finals": finals,
+        "failed": failed,
     }
     return rep, kept
 

@@ -277,6 +277,13 @@ int he4g_enable_graphs(he4g_run* run, int on);
  * uneven grids) overlap on the device; one host synchronisation at the end.
  * Returns the first error of any run. */
 int he4g_step_many(he4g_run** runs, int n, int nsteps);
+/* The health of one run after its queued work: HE4G_OK, or the error its
+ * checks saw (HE4G_EDENSITY, HE4G_ENAN, HE4G_ETABLE, with the failing step in
+ * he4g_last_error). he4g_step_many stops only the runs whose checks fail and
+ * returns the first error; this tells a host which runs to evict while the
+ * others continue. No reference counterpart (the reference STOPs,
+ * steprk.f90:89-92). */
+int he4g_health(he4g_run* run);
 
 /* A fixed set of runs stepped together with one CUDA graph per batch step.
  * No counterpart in the reference (it runs one collision per process). The

@@ -45,3 +45,31 @@ def test_serving_loop_admits_evicts_and_matches_runs_alone():
     drift = S.compare_finals(rep["finals"], base["finals"])
     assert drift["jobs_compared"] == len(stream)
     assert drift["dE_over_scale_max"] < 1e-5 and drift["norm_rel_max"] < 1e-8, drift
+
+
+def test_a_failing_job_is_evicted_and_the_others_finish():
+    """Host-side fault injection through the state upload: one job's psi has
+    a slab of exact zeros deeper than the stencil, so its density check fails
+    in its first Runge-Kutta stage (steprk.f90:89-92). The loop evicts that
+    job with HE4G_EDENSITY and its memory; the other jobs, which shared the
+    GPU with it, finish with the results they give alone."""
+    import he4gpu
+    from he4gpu import serve as S
+    from he4gpu.initial import state_for
+    stream = _stream()[:4]
+    bad_meta = stream[1][1]
+
+    def state_fn(meta):
+        psi, r, v = state_for(meta)
+        if meta is bad_meta:
+            psi = psi.copy()
+            psi[0:8, :, :] = 0.0
+        return psi, r, v
+
+    need = max(he4gpu.footprint(S.job_config(m, S.MIXED)) for _, m in stream)
+    rep, kept = S.serve(stream, 2 * need, chunk=4, keep_results=(0, 2, 3), state_fn=state_fn)
+    assert [f["id"] for f in rep["failed"]] == [1], rep["failed"]
+    assert rep["failed"][0]["code"] == he4gpu.abi.HE4G_EDENSITY
+    assert rep["jobs"] == 3
+    check = S.alone_vs_mix(stream, kept)
+    assert all(v["identical"] for v in check.values()), check
