@@ -1178,24 +1178,12 @@ int he4g_create(const he4g_config* cfg, const double* fvlj4, const double* wcgk,
   upload_field(r, r->potion, potion, c.npot);
   // grids (DFT4He3d.f90:303-313) and the absorber (:689-699), its real part
   // rounded to single precision as the reference's default-kind CMPLX does
-  std::vector<double> x(c.nx), y(c.ny), z(c.nz), tx(c.nx), ty(c.ny), tz(c.nz);
+  std::vector<double> x(c.nx), y(c.ny), z(c.nz);
   for (int i = 0; i < c.nx; ++i) x[i] = -c.xmax + g.hx * static_cast<double>(i);
   for (int i = 0; i < c.ny; ++i) y[i] = -c.ymax + g.hy * static_cast<double>(i);
   for (int i = 0; i < c.nz; ++i) z[i] = -c.zmax + g.hz * static_cast<double>(i);
-  for (int i = 0; i < c.nx; ++i) tx[i] = std::tanh((std::fabs(x[i]) - c.txmean) / c.txsurf);
-  for (int i = 0; i < c.ny; ++i) ty[i] = std::tanh((std::fabs(y[i]) - c.tymean) / c.tysurf);
-  for (int i = 0; i < c.nz; ++i) tz[i] = std::tanh((std::fabs(z[i]) - c.tzmean) / c.tzsurf);
   std::vector<float> tc(n);
-  for (int k = 0; k < c.nz; ++k)
-    for (int j = 0; j < c.ny; ++j)
-      for (int i = 0; i < c.nx; ++i) {
-        double sv = 1.0 + tx[i];
-        sv = sv + 1.0;
-        sv = sv + ty[j];
-        sv = sv + 1.0;
-        sv = sv + tz[k];
-        tc[((size_t)k * c.ny + j) * c.nx + i] = static_cast<float>(c.lambdah * sv);
-      }
+  he4g_build_timec(&c, tc.data());
   // every upload is ordered on the run's stream after the zeroing memsets
   cudaMemcpyAsync(r->xs, x.data(), sizeof(double) * c.nx, cudaMemcpyHostToDevice, r->s);
   cudaMemcpyAsync(r->ys, y.data(), sizeof(double) * c.ny, cudaMemcpyHostToDevice, r->s);

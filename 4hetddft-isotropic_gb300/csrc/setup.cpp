@@ -360,6 +360,32 @@ double morse_tio2_3d(double x, double y, double z) {
 
 }  // namespace
 
+// The real part of the absorber timec (DFT4He3d.f90:689-699) on the grid:
+// lambdah*(1 + tanh((|x| - txmean)/txsurf) + 1 + tanh(...y...) + 1 +
+// tanh(...z...)) summed in that order, rounded to single precision as the
+// reference's default-kind CMPLX rounds it; the imaginary part is 1.
+extern "C" int he4g_build_timec(const he4g_config* c, float* tc) {
+  if (!c || !tc || c->nx <= 0 || c->ny <= 0 || c->nz <= 0) return HE4G_EINVAL;
+  const int nx = c->nx, ny = c->ny, nz = c->nz;
+  const double hx = 2.0 * std::fabs(c->xmax) / nx, hy = 2.0 * std::fabs(c->ymax) / ny,
+               hz = 2.0 * std::fabs(c->zmax) / nz;
+  std::vector<double> tx(nx), ty(ny), tz(nz);
+  for (int i = 0; i < nx; ++i) tx[i] = std::tanh((std::fabs(-c->xmax + hx * static_cast<double>(i)) - c->txmean) / c->txsurf);
+  for (int i = 0; i < ny; ++i) ty[i] = std::tanh((std::fabs(-c->ymax + hy * static_cast<double>(i)) - c->tymean) / c->tysurf);
+  for (int i = 0; i < nz; ++i) tz[i] = std::tanh((std::fabs(-c->zmax + hz * static_cast<double>(i)) - c->tzmean) / c->tzsurf);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        double sv = 1.0 + tx[i];
+        sv = sv + 1.0;
+        sv = sv + ty[j];
+        sv = sv + 1.0;
+        sv = sv + tz[k];
+        tc[(static_cast<size_t>(k) * ny + j) * nx + i] = static_cast<float>(c->lambdah * sv);
+      }
+  return HE4G_OK;
+}
+
 // uext of DFT4He3d.f90:760-784: min(3000 K, surface potential at z - zsurf)
 // on the grid x(ix) = -xmax + hx*(ix-1) etc. (DFT4He3d.f90:274-290)
 extern "C" int he4g_build_uext(const he4g_config* c, int lsurf3d, double zsurf, double* uext) {

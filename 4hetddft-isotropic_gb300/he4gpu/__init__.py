@@ -90,6 +90,17 @@ def build_uext(cfg, lsurf3d=False, zsurf=-25.0):
     return out
 
 
+def build_timec(cfg):
+    """The real part of the absorber timec (DFT4He3d.f90:689-699) that
+    he4g_create builds, float32 of shape (nz, ny, nx); the imaginary part is 1."""
+    lib = abi.load()
+    out = np.empty((cfg.nz, cfg.ny, cfg.nx), dtype=np.float32)
+    rc = lib.he4g_build_timec(C.byref(cfg), out.ctypes.data_as(C.POINTER(C.c_float)))
+    if rc:
+        raise He4gError(rc, "build_timec")
+    return out
+
+
 def read_namelist_int(path, name):
     """he4g_read_namelist_int: an integer of a namelist file, or None."""
     lib = abi.load()

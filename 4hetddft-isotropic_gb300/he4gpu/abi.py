@@ -144,6 +144,7 @@ SIGNATURES = {
     "he4g_set_timec": (C.c_int, [_P, _D]),
     "he4g_set_uext": (C.c_int, [_P, _D]),
     "he4g_build_uext": (C.c_int, [C.POINTER(Config), C.c_int, C.c_double, _D]),
+    "he4g_build_timec": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_float)]),
     "he4g_read_namelist_int": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_int)]),
     "he4g_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(_P)]),
     "he4g_batch_step": (C.c_int, [_P, C.c_int]),

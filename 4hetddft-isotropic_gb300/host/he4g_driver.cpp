@@ -14,7 +14,13 @@
 //    (printoutc.f90:52-77; DFT4He3d.f90:972-994), psi read back with
 //    he4g_get_psi_async so that the copy overlaps the next steps;
 //  - with lsurf, the TiO2 surface potential (lsurf3D, Zsurf;
-//    DFT4He3d.f90:760-784) in the energy blocks.
+//    DFT4He3d.f90:760-784) in the energy blocks, and uext.dat (:785-792);
+//  - DFT4He3d.namelist.read, the echo of the &input group (:195-196), from
+//    which the Fortran wrappers read their loop cadence;
+//  - timec.dat, the absorber's real part in the y = 0 plane (:704-711);
+//  - the hedenini-*.dat and uimp-*.dat cuts through the box centre of the
+//    initial density and of uimp after the first evaluation (respar.f90,
+//    :391, :649).
 //
 //   he4g_driver input.nml [--precision fp64|mixed|df64] [--parse]
 //
@@ -218,6 +224,52 @@ void write_density(const std::string& path, const std::vector<double>& psi, cons
   std::fclose(f);
 }
 
+// DFT4He3d.namelist.read: the &input group as read (DFT4He3d.f90:195-196),
+// one NAME=value per line; literals as given, strings quoted
+void write_namelist_echo(const std::map<std::string, std::string>& nl) {
+  std::FILE* f = std::fopen("DFT4He3d.namelist.read", "w");
+  if (!f) die("cannot write DFT4He3d.namelist.read");
+  std::fprintf(f, "&INPUT\n");
+  for (const auto& kv : nl) {
+    std::string key = kv.first;
+    for (char& c : key) c = static_cast<char>(std::toupper(static_cast<unsigned char>(c)));
+    std::string v = kv.second, e = v;
+    for (char& c : e)
+      if (c == 'd' || c == 'D') c = 'e';
+    char* end = nullptr;
+    std::strtod(e.c_str(), &end);
+    const std::string l = lower(v);
+    const bool literal = (!e.empty() && end == e.c_str() + e.size()) || l == ".true." || l == ".false." ||
+                         l == "t" || l == "f" || l == ".t." || l == ".f.";
+    std::fprintf(f, " %s=%s%s%s,\n", key.c_str(), literal ? "" : "'", v.c_str(), literal ? "" : "'");
+  }
+  std::fprintf(f, " /\n");
+  std::fclose(f);
+}
+
+// respar.f90: fun(x, y = 0, z = 0), fun(0, y, 0) and fun(0, 0, z) at the box
+// centre (ix = nx/2+1 etc.) into name-x/y/z.dat, format (1x,1P,2E14.5), with
+// values below 1e-40 in magnitude written as 0
+void write_cuts(const std::string& name, const std::vector<double>& fun, const he4g_config& c) {
+  const int nx = c.nx, ny = c.ny, nz = c.nz;
+  const double h[3] = {2 * c.xmax / nx, 2 * c.ymax / ny, 2 * c.zmax / nz};
+  const double lo[3] = {-c.xmax, -c.ymax, -c.zmax};
+  const int n[3] = {nx, ny, nz};
+  const char* ax = "xyz";
+  for (int a = 0; a < 3; ++a) {
+    const std::string path = name + "-" + ax[a] + ".dat";
+    std::FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) die("cannot write " + path);
+    for (int t = 0; t < n[a]; ++t) {
+      const int i = a == 0 ? t : nx / 2, j = a == 1 ? t : ny / 2, k = a == 2 ? t : nz / 2;
+      double v = fun[(static_cast<size_t>(k) * ny + j) * nx + i];
+      if (std::fabs(v) < 1e-40) v = 0.0;
+      std::fprintf(f, " %s%s\n", fe(lo[a] + h[a] * t, 14, 5).c_str(), fe(v, 14, 5).c_str());
+    }
+    std::fclose(f);
+  }
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -274,6 +326,7 @@ int main(int argc, char** argv) {
   double rimp[3] = {num("ximp", 0), num("yimp", 0), num("zimp", 0)};
   double vimp[3] = {num("vximp", 0) * kPsToK, num("vyimp", 0) * kPsToK, num("vzimp", 0) * kPsToK};
 
+  if (!parse_only) write_namelist_echo(nl);
   if (parse_only) {
     std::printf("nx=%d ny=%d nz=%d xmax=%.17g ymax=%.17g zmax=%.17g deltat=%.17g deltatps=%.17g niter=%lld "
                 "pener=%lld pcurr=%lld mode=%d lsolid=%d core=%d lrk=%d selec=%s r_cutoff=%.17g umax=%.17g "
@@ -346,13 +399,43 @@ int main(int argc, char** argv) {
         "he4g_build_tables", nullptr);
   he4g_run* run = nullptr;
   check(he4g_create(&c, nullptr, nullptr, nullptr, potion.data(), &run), "he4g_create", nullptr);
+  {
+    // timec.dat (DFT4He3d.f90:704-711): x, z and the absorber's real part at iy = ny/2+1
+    std::vector<float> tc(n);
+    check(he4g_build_timec(&c, tc.data()), "he4g_build_timec", nullptr);
+    std::FILE* f = std::fopen("timec.dat", "w");
+    if (!f) die("cannot write timec.dat");
+    const double hx = 2 * c.xmax / nx, hz = 2 * c.zmax / nz;
+    for (int k = 0; k < nz; ++k) {
+      for (int i = 0; i < nx; ++i)
+        std::fprintf(f, " %24.16E %24.16E %16.8E\n", -c.xmax + hx * i, -c.zmax + hz * k,
+                     static_cast<double>(tc[(static_cast<size_t>(k) * ny + ny / 2) * nx + i]));
+      std::fprintf(f, " \n");
+    }
+    std::fclose(f);
+  }
   check(he4g_set_state(run, psi.data(), rimp, vimp), "he4g_set_state", run);
+  {
+    // the initial density (DFT4He3d.f90:391) and uimp after the first evaluation (:649)
+    std::vector<double> field(n);
+    check(he4g_get_den(run, field.data()), "he4g_get_den", run);
+    write_cuts("hedenini", field, c);
+    check(he4g_get_field(run, 3, field.data()), "he4g_get_field", run);
+    write_cuts("uimp", field, c);
+  }
   // the TiO2 surface (DFT4He3d.f90:760-784): uext enters the energy only
   if (has("lsurf") && flog(nl.at("lsurf"))) {
     std::vector<double> uext(n);
     const bool l3d = has("lsurf3d") && flog(nl.at("lsurf3d"));
     check(he4g_build_uext(&c, l3d ? 1 : 0, num("zsurf", -25.0), uext.data()), "he4g_build_uext", run);
     check(he4g_set_uext(run, uext.data()), "he4g_set_uext", run);
+    // uext.dat (DFT4He3d.f90:785-792): z and uext(3,5,iz)
+    std::FILE* f = std::fopen("uext.dat", "w");
+    if (!f) die("cannot write uext.dat");
+    const double hz = 2 * c.zmax / nz;
+    for (int k = 0; k < nz; ++k)
+      std::fprintf(f, " %24.16E %24.16E\n", -c.zmax + hz * k, uext[(static_cast<size_t>(k) * ny + 4) * nx + 2]);
+    std::fclose(f);
   }
 
   std::FILE* fo[3] = {std::fopen(str("filerimp", "rimp.out").c_str(), "w"),

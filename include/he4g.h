@@ -139,6 +139,12 @@ int he4g_build_tables(const he4g_config* cfg, const char* selec, double r_cutoff
  * order). Host arithmetic only; hand the result to he4g_set_uext. */
 int he4g_build_uext(const he4g_config* cfg, int lsurf3d, double zsurf, double* uext);
 
+/* The real part of the absorber timec of DFT4He3d.f90:689-699 on the config's
+ * grid, nx*ny*nz floats (x fastest): the single-precision values he4g_create
+ * builds (the imaginary part is 1). For hosts that write the reference's
+ * timec.dat (DFT4He3d.f90:704-711). */
+int he4g_build_timec(const he4g_config* cfg, float* timec_real);
+
 /* Reads the integer `name = value` of a namelist file (first assignment,
  * name case-insensitive) into *value; HE4G_EINVAL when the file or the name
  * is missing. The Fortran wrappers read the loop cadence (iter0, niter,

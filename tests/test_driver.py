@@ -134,3 +134,24 @@ def test_driver_outputs_match_the_python_mirror(tmp_path):
     got = dump["psi"].transpose(2, 1, 0).reshape(run.shape)
     assert np.array_equal(got, run.psi)
     run.close()
+
+    # the reference's other files: the namelist echo the Fortran wrappers read
+    # their cadence from, timec.dat, and the respar cuts of the start
+    echo = tmp_path / "DFT4He3d.namelist.read"
+    assert {k: he4gpu.read_namelist_int(echo, k) for k in ("iter0", "niter", "pener", "pcurr", "nx")} == \
+        {"iter0": 0, "niter": niter, "pener": pener, "pcurr": pcurr, "nx": nx}
+    lines = (tmp_path / "timec.dat").read_text().splitlines()
+    assert len(lines) == nx * (nx + 1)
+    rows = np.array([[float(t) for t in ln.split()] for ln in lines if ln.strip()])
+    tc = he4gpu.build_timec(cfg)[:, nx // 2, :]  # (z, x) at iy = ny/2 + 1
+    assert np.array_equal(rows[:, 2].astype(np.float32), tc.reshape(-1))
+    first = he4gpu.Run(cfg, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463, device_tables=True)
+    first.set_state(psi, r, v)
+    for name, field in (("hedenini", first.den), ("uimp", first.field("uimp"))):
+        c = nx // 2
+        for ax, line in (("x", field[c, c, :]), ("y", field[c, :, c]), ("z", field[:, c, c])):
+            cut = np.loadtxt(tmp_path / f"{name}-{ax}.dat")
+            assert cut.shape == (nx, 2)
+            want = np.where(np.abs(line) < 1e-40, 0.0, line)
+            np.testing.assert_allclose(cut[:, 1], want, rtol=1e-5, atol=0)
+    first.close()

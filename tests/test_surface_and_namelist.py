@@ -69,3 +69,16 @@ def test_read_namelist_int(he4gpu_mod, tmp_path):
     q = tmp_path / "quoted.nml"
     q.write_text("&INPUT TITLE='pener=7', PENER=9 /\n")
     assert he4gpu_mod.read_namelist_int(q, "pener") == 9
+
+
+def test_timec_builder_matches_the_oracle(he4gpu_mod, oracle_mod):
+    """he4g_build_timec (the absorber he4g_create uploads and the host driver
+    writes to timec.dat) equals the oracle's single-precision real part."""
+    cfg = he4gpu_mod.default_config(24, 28, 32, 12.0, 13.0, 14.0, lambdah=2.0, txmean=9.0, txsurf=1.5,
+                                    tymean=10.0, tysurf=2.0, tzmean=11.0, tzsurf=2.5)
+    got = he4gpu_mod.build_timec(cfg)
+    o = oracle_mod.OracleRun(cfg, oracle_mod.build_tables(cfg))
+    want = o.timec_array()
+    assert np.array_equal(got.astype(np.float64), want.real)
+    assert np.all(want.imag == 1.0)
+    o.close()
