@@ -31,6 +31,8 @@
 #include <vector>
 
 #include "df64.cuh"
+
+#include <nvtx3/nvToolsExt.h>
 #include "setup_math.h"
 #include "he4g_df.cuh"
 #include "he4g_internal.cuh"
@@ -190,6 +192,16 @@ struct he4g_batch {
 namespace {
 
 bool mixed(const he4g_run* r) { return r->prec == HE4G_PREC_MIXED; }
+
+// NVTX ranges around the host-side phases of a call (steps, evaluations,
+// energies, snapshots): a profiler shows them on its timeline; with none
+// attached each costs a branch
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range&) = delete;
+  Range& operator=(const Range&) = delete;
+};
 bool dfm(const he4g_run* r) { return r->prec == HE4G_PREC_DF64; }
 
 // df64 split of a long double: hi = RN(v), lo = RN(v - hi)
@@ -660,6 +672,7 @@ void force_dev(he4g_run* r, int store_accel, int sel = 1, bool store_uimp = fals
 // potenimp(centre sel); poten(); forceimp(rimp, aimp); aimp /= m;
 // record: the step's trajectory row after the force
 void evaluate_at(he4g_run* r, int sel, bool record = false) {
+  Range range("he4g evaluation");
   if (mixed(r) || dfm(r)) {
     poten_dev(r);  // does not read uimp
     force_dev(r, 1, sel, true, record);
@@ -921,6 +934,7 @@ bool pc_step_graph(he4g_run* r) {
 
 int one_step(he4g_run* r) {
   const int iteraux = r->iter + 1;
+  Range range(iteraux <= 3 || r->cfg.lrk ? "he4g RK-Gill step" : "he4g predictor-corrector step");
   if (iteraux <= 3 || r->cfg.lrk) {
     steprk_dev(r, r->cfg.deltat);
     evaluate_dev(r);
@@ -1764,6 +1778,7 @@ bool batch_health_seen(he4g_batch* b) {
 }  // extern "C++"
 
 int he4g_batch_step(he4g_batch* b, int nsteps) {
+  Range range("he4g batch step");
   if (!b || nsteps < 0) return HE4G_EINVAL;
   if (b->dead) return HE4G_ESTATE;
   for (he4g_run* r : b->runs) {
@@ -1896,6 +1911,7 @@ int he4g_snapshot_bytes(he4g_run* r, uint64_t* bytes) {
 }
 
 int he4g_save_snapshot(he4g_run* r, void* host, uint64_t bytes) {
+  Range range("he4g save snapshot");
   int rc = check_ready(r);
   if (rc) return rc;
   if (!host || bytes < snapshot_total(r)) return fail(r, HE4G_EINVAL, "save_snapshot: buffer too small");
@@ -2144,6 +2160,7 @@ F64View f64_view(he4g_run* r) {
 }  // namespace
 
 int he4g_energy(he4g_run* r, he4g_energies* en) {
+  Range range("he4g energy");
   int rc = check_ready(r);
   if (rc) return rc;
   if (!en) return HE4G_EINVAL;
