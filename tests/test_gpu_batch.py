@@ -87,10 +87,26 @@ def test_batch_graph_matches_runs_alone(precision):
 @pytest.mark.parametrize("engine", [0, 15])
 @pytest.mark.parametrize("precision", [0, 1, 2])
 def test_tile_shapes_give_identical_results(precision, engine):
-    """Every generic tile shape transforms each line with the same arithmetic."""
+    """Every generic tile shape transforms each line with the same arithmetic:
+    three fixed shapes and three drawn at random (seeded) from those that fit."""
+    import he4gpu
     cfg, tk, psi, r, v, meta = make_case("he200_xe_40x48x64", precision=precision)
+    rng = np.random.default_rng(1000 * precision + engine)
+    shapes = [(32, 32, 3, 3), (1, 3, 0, 1), (4, 64, 5, 2)]
+    probe = gpu_run(cfg, tk, psi, r, v)
+    for _ in range(200):
+        if len(shapes) == 6:
+            break
+        t = (int(2 ** rng.integers(0, 7)), int(rng.integers(1, 65)), int(rng.integers(0, 6)), int(rng.integers(0, 6)))
+        try:
+            probe.tiles = t + (engine,)
+        except he4gpu.He4gError:
+            continue  # does not fit in shared memory
+        shapes.append(t)
+    assert len(shapes) == 6
+    probe.close()
     runs = []
-    for t in [(32, 32, 3, 3), (1, 3, 0, 1), (4, 64, 5, 2)]:
+    for t in shapes:
         x = gpu_run(cfg, tk, psi, r, v)
         x.tiles = t + (engine,)
         x.enable_graphs(True)
