@@ -4,8 +4,9 @@ nx (so every half-length nx/2 of the x passes' packed complex lines, odd ones
 included) and every length as ny or nz (the y lines and the z convolution
 columns), with nx = 2 mod 4 among them (the mixed form's scalar force
 kernel). On each grid the library's mean-field
-evaluation and two Runge-Kutta-Gill steps (steprk.f90:21-150, poten.f90:5-118)
-are compared with the FP64 oracle:
+evaluation and five steps (three Runge-Kutta-Gill, two predictor-corrector:
+steprk.f90:21-150, steppc.f90:1-178, poten.f90:5-118) are compared with the
+FP64 oracle:
 - FP64 with the default passes (register engine where a length has a
   specialisation, the generic mixed-radix kernels elsewhere) and with the
   generic kernels for every pass;
@@ -26,6 +27,7 @@ STEP_TOL = 1e-10
 DF64_UIMP_TOL = 2e-12
 MIXED_TOL = 1e-5
 H = 0.4
+NSTEPS = 5
 XE = {"selec": "Xe_He", "r_cutoff": 2.55, "umax": 2793.9365463}
 
 
@@ -70,12 +72,12 @@ def test_grids_cover_every_length_in_every_role():
     assert all(n in ys | zs for n in (25, 27, 45, 75, 81, 125, 135, 225, 243))
 
 
-def droplet(nx, ny, nz, seed):
+def droplet(nx, ny, nz, seed, h=(H, H, H)):
     rng = np.random.default_rng(seed)
-    ext = (0.5 * H * nx, 0.5 * H * ny, 0.5 * H * nz)
-    x = -ext[0] + H * np.arange(nx)
-    y = -ext[1] + H * np.arange(ny)
-    z = -ext[2] + H * np.arange(nz)
+    ext = (0.5 * h[0] * nx, 0.5 * h[1] * ny, 0.5 * h[2] * nz)
+    x = -ext[0] + h[0] * np.arange(nx)
+    y = -ext[1] + h[1] * np.arange(ny)
+    z = -ext[2] + h[2] * np.arange(nz)
     r = np.sqrt(z[:, None, None] ** 2 + y[None, :, None] ** 2 + x[None, None, :] ** 2)
     rho = 0.0218 / (1.0 + np.exp((r - 8.0) / 2.0))
     psi = np.sqrt(rho) * np.exp(1j * 1e-3 * rng.standard_normal(rho.shape))
@@ -98,7 +100,7 @@ def test_grid_matches_oracle(grid):
     o = oracle_run(config(grid, ext, FP64), XE, psi, r, v)
     ref = {name: o.field(name) for name in ("uimp", "dencg", "delj4", "pot4")}
     ref_energy = o.energy()
-    o.step(2)
+    o.step(NSTEPS)
     ref_den, ref_psi, ref_pot4 = o.den, o.psi, o.field("pot4")
     ref_r, ref_v, _ = o.impurity()
     o.close()
@@ -125,7 +127,7 @@ def test_grid_matches_oracle(grid):
             e = g.energy()
             for k in ref_energy:
                 assert abs(e[k] - ref_energy[k]) <= 1e-11 * max(abs(ref_energy[k]), 1e-6), (what, k)
-        g.step(2)
+        g.step(NSTEPS)
         assert rel_field(g.den, ref_den) < step_tol, what
         assert rel_field(g.psi, ref_psi) < step_tol, what
         assert rel_field(g.field("pot4"), ref_pot4) < step_tol, what
@@ -158,7 +160,7 @@ def test_otc_grid_matches_oracle(grid):
     ref = {name: o.field(name) for name in names}
     ref_ealphas = o.energy()["ealphas"]
     assert ref_ealphas != 0.0
-    o.step(2)
+    o.step(NSTEPS)
     ref_den = o.den
     o.close()
     for prec in (FP64, DF64, MIXED):
@@ -170,6 +172,80 @@ def test_otc_grid_matches_oracle(grid):
             assert rel_field(g.field(name), ref[name]) < tol, (grid, prec, name)
         etol = 1e-4 if prec == MIXED else 1e-11
         assert abs(g.energy()["ealphas"] - ref_ealphas) <= etol * abs(ref_ealphas), (grid, prec)
-        g.step(2)
+        g.step(NSTEPS)
         assert rel_field(g.den, ref_den) < (MIXED_TOL if prec == MIXED else STEP_TOL), (grid, prec)
+        g.close()
+
+
+# hx, hy and hz all different (the reference takes xmax, ymax and zmax apart):
+# the stencils' per-axis coefficients and the form factors of a non-cubic
+# momentum grid
+SPACED = [((32, 32, 32), (0.4, 0.45, 0.35)), ((40, 48, 64), (0.45, 0.35, 0.4)),
+          ((54, 20, 25), (0.35, 0.4, 0.45)), ((96, 24, 18), (0.42, 0.38, 0.44))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("grid,h", SPACED, ids=lambda x: "x".join(map(str, x)))
+def test_unequal_spacing_matches_oracle(grid, h):
+    import he4gpu
+    psi, r, v, ext = droplet(*grid, seed=sum(grid) + 2, h=h)
+    o = oracle_run(config(grid, ext, FP64), XE, psi, r, v)
+    ref = {name: o.field(name) for name in ("uimp", "dencg", "delj4", "pot4")}
+    o.step(NSTEPS + 1)
+    ref_den, ref_psi = o.den, o.psi
+    ref_r, ref_v, _ = o.impurity()
+    ref_energy = o.energy()
+    o.close()
+    for prec in (FP64, DF64, MIXED):
+        what = f"{grid} h={h} precision {prec}"
+        g = he4gpu.Run(config(grid, ext, prec), **XE)
+        g.set_state(psi, r, v)
+        tol = MIXED_TOL if prec == MIXED else FIELD_TOL
+        if prec == FP64:
+            assert np.array_equal(g.field("uimp"), ref["uimp"]), what
+        for name in ("dencg", "delj4", "pot4"):
+            assert rel_field(g.field(name), ref[name]) < tol, (what, name)
+        g.step(NSTEPS + 1)
+        tol = MIXED_TOL if prec == MIXED else STEP_TOL
+        assert rel_field(g.den, ref_den) < tol, what
+        assert rel_field(g.psi, ref_psi) < tol, what
+        rg, vg, _ = g.impurity()
+        assert rel_vec(rg, ref_r) < (1e-8 if prec == MIXED else STEP_TOL), what
+        assert rel_vec(vg, ref_v) < (1e-6 if prec == MIXED else STEP_TOL), what
+        e = g.energy()
+        for k in ("etot", "ekin4", "elj4", "ecor4", "eHeX"):
+            assert abs(e[k] - ref_energy[k]) <= tol * max(abs(ref_energy[k]), 1.0), (what, k)
+        g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("grid", [(48, 30, 27), (250, 120, 27)], ids=lambda g: "x".join(map(str, g)))
+def test_ot_without_the_solid_penalty(grid):
+    """Core OT with lsolid off: pot4 without the penalty term (poten.f90:110-114)
+    and the energy without E_solid."""
+    import he4gpu
+    psi, r, v, ext = droplet(*grid, seed=sum(grid) + 3)
+
+    def cfg_of(prec):
+        c = config(grid, ext, prec)
+        c.lsolid = 0
+        return c
+
+    o = oracle_run(cfg_of(FP64), XE, psi, r, v)
+    ref_pot4 = o.field("pot4")
+    o.step(NSTEPS)
+    ref_den = o.den
+    ref_energy = o.energy()
+    o.close()
+    for prec in (FP64, DF64, MIXED):
+        g = he4gpu.Run(cfg_of(prec), **XE)
+        g.set_state(psi, r, v)
+        tol = MIXED_TOL if prec == MIXED else FIELD_TOL
+        assert rel_field(g.field("pot4"), ref_pot4) < tol, (grid, prec)
+        g.step(NSTEPS)
+        tol = MIXED_TOL if prec == MIXED else STEP_TOL
+        assert rel_field(g.den, ref_den) < tol, (grid, prec)
+        e = g.energy()
+        for k in ref_energy:
+            assert abs(e[k] - ref_energy[k]) <= tol * max(abs(ref_energy[k]), 1.0), (grid, prec, k)
         g.close()
