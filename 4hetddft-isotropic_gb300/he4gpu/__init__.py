@@ -284,7 +284,9 @@ class Run:
         from . import formats
         e, o = self.energy(), self.observables(n4)
         r, v, _ = self.impurity()
-        formats.write_density(path, self.psi, r, v, self.cfg.xmax, self.cfg.ymax, self.cfg.zmax,
+        # the run's arrays are (nz, ny, nx) with x fastest; the file helpers
+        # take (nx, ny, nz) arrays in Fortran order, the same memory
+        formats.write_density(path, self.psi.transpose(2, 1, 0), r, v, self.cfg.xmax, self.cfg.ymax, self.cfg.zmax,
                               iteration=self.steps_taken, dtps=self.cfg.deltat * formats.PS_PER_KELVIN_UNIT,
                               time=time_ps, selec=selec, r_cutoff=r_cutoff, umax=umax, cm=o["cm"],
                               npart=o["npart"], energies=e, ang=o["ang"], r2=o["r2"])
@@ -318,7 +320,8 @@ class Run:
         if (d["nx"], d["ny"], d["nz"]) != (self.cfg.nx, self.cfg.ny, self.cfg.nz):
             raise He4gError(-1, f"{path}: grid {d['nx']}x{d['ny']}x{d['nz']} does not match the run")
         psi = d["psi"] if "psi" in d else np.sqrt(np.maximum(d["den"], 0.0)).astype(np.complex128)
-        self.set_state(psi, d["rimp"], d.get("vimp", np.zeros(3)))
+        # (nx, ny, nz) in Fortran order -> the run's (nz, ny, nx), x fastest
+        self.set_state(psi.transpose(2, 1, 0), d["rimp"], d.get("vimp", np.zeros(3)))
         return d
 
     def impurity(self):

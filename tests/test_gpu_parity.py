@@ -227,13 +227,40 @@ def test_config1_short_run():
 def test_restart_through_the_reference_file_format(tmp_path):
     """A state written in printoutc's format and read back as readenc mode 2
     reads it restores psi and the impurity's position and velocity bit for
-    bit."""
-    cfg, tk, psi, r, v, meta = make_case("he100_xe_32")
+    bit. On a grid with three different lengths the file holds the grid
+    record nx ny nz and psi with x fastest (printoutc.f90:52-77), as the
+    reference writes and reads it."""
+    from he4gpu import formats
+    cfg, tk, psi, r, v, meta = make_case("he200_xe_40x48x64")
     a = gpu_run(cfg, tk, psi, r, v)
     a.step(4)
     path = tmp_path / "den.out"
     a.write_density(path, meta["n4"])
+    d = formats.read_density(path, mode=2)
+    assert (d["nx"], d["ny"], d["nz"]) == (cfg.nx, cfg.ny, cfg.nz)
+    # the file's value k is psi(i, j, l) with k = i + nx*(j + ny*l)
+    flat = d["psi"].reshape(-1, order="F")
+    assert np.array_equal(flat, a.psi.reshape(-1))
     b = gpu_run(cfg, tk, psi, r, v)
     b.read_state(path, mode=2)
     assert np.array_equal(a.psi, b.psi)
     assert all(np.array_equal(x, y) for x, y in zip(a.impurity()[:2], b.impurity()[:2]))
+
+
+def test_mode0_density_file_sets_the_state_in_x_fastest_order(tmp_path):
+    """readenc mode 0 (readenc.f90:85-100): the grid record with limp and the
+    impurity, then den with x fastest; the run starts from psi = sqrt(den)."""
+    cfg, tk, psi, r, v, meta = make_case("he200_xe_40x48x64")
+    den = np.abs(psi) ** 2  # (nz, ny, nx)
+    hx, hy, hz = 2 * cfg.xmax / cfg.nx, 2 * cfg.ymax / cfg.ny, 2 * cfg.zmax / cfg.nz
+    head = " ".join(f"{x:.17E}" for x in (cfg.xmax, cfg.ymax, cfg.zmax, hx, hy, hz))
+    lines = ["# a density", f"{head} {cfg.nx} {cfg.ny} {cfg.nz} T " + " ".join(f"{x:.17E}" for x in r)]
+    flat = den.reshape(-1)  # x fastest
+    lines += [" ".join(f"{x:.17E}" for x in flat[k:k + 6]) for k in range(0, flat.size, 6)]
+    path = tmp_path / "den0.in"
+    path.write_text("\n".join(lines) + "\n")
+    g = gpu_run(cfg, tk, psi, r, v)
+    g.read_state(path, mode=0)
+    assert rel_field(g.psi, np.sqrt(den)) == 0.0
+    assert np.array_equal(g.impurity()[0], r)
+    g.close()
