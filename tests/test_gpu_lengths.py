@@ -28,6 +28,8 @@ DF64_UIMP_TOL = 2e-12
 MIXED_TOL = 1e-5
 H = 0.4
 NSTEPS = 5
+# the evaluation's fields and the density gradients of forceimp (derden.f90:26-28)
+FIELDS = ("dencg", "delj4", "pot4", "dxden", "dyden", "dzden")
 XE = {"selec": "Xe_He", "r_cutoff": 2.55, "umax": 2793.9365463}
 
 
@@ -98,7 +100,7 @@ def test_grid_matches_oracle(grid):
     import he4gpu
     psi, r, v, ext = droplet(*grid, seed=sum(grid))
     o = oracle_run(config(grid, ext, FP64), XE, psi, r, v)
-    ref = {name: o.field(name) for name in ("uimp", "dencg", "delj4", "pot4")}
+    ref = {name: o.field(name) for name in ("uimp",) + FIELDS}
     ref_energy = o.energy()
     o.step(NSTEPS)
     ref_den, ref_psi, ref_pot4 = o.den, o.psi, o.field("pot4")
@@ -121,7 +123,7 @@ def test_grid_matches_oracle(grid):
         else:
             uimp_tol = MIXED_TOL if prec == MIXED else DF64_UIMP_TOL
             assert rel_field(uimp, ref["uimp"]) < uimp_tol, what
-        for name in ("dencg", "delj4", "pot4"):
+        for name in FIELDS:
             assert rel_field(g.field(name), ref[name]) < field_tol, (what, name)
         if prec == FP64 and not generic:
             e = g.energy()
