@@ -80,7 +80,10 @@ def _mean_field(cfg, tabs, den, row):
     return out
 
 
-@pytest.mark.parametrize("core,lsolid,dims", [(0, 1, (24, 20, 30)), (1, 0, (20, 24, 16)), (0, 0, (32, 32, 32))])
+# the odd lengths (27, 25, 45, and nx/2 = 15, 9) take the oracle's radix-3 and
+# radix-5 passes on odd lines
+@pytest.mark.parametrize("core,lsolid,dims", [(0, 1, (24, 20, 30)), (1, 0, (20, 24, 16)), (0, 0, (32, 32, 32)),
+                                              (0, 1, (30, 27, 25)), (1, 0, (18, 45, 20))])
 def test_mean_field_matches_numpy(oracle_mod, he4gpu_mod, core, lsolid, dims):
     nx, ny, nz = dims
     h = 0.45
@@ -296,14 +299,16 @@ class _NumpyRun:
         self.evaluate(self.rimp)
 
 
-def test_rk_and_pc_steps_match_numpy(oracle_mod, he4gpu_mod):
+@pytest.mark.parametrize("dims", [(20, 24, 16), (18, 27, 25)])
+def test_rk_and_pc_steps_match_numpy(oracle_mod, he4gpu_mod, dims):
     """Three Runge-Kutta-Gill steps and three Hamming predictor-modifier-
     corrector steps (steppc.f90:1-178, the impurity predictor stored into
     rimpold(:,ioldr(3)) and the field evaluated there) of the driver loop,
-    restated in numpy, against the oracle's step."""
+    restated in numpy, against the oracle's step (also on odd lengths)."""
     gold = json.load(open(os.path.join(GOLDEN, "stencil_rows.json")))
     rows = (gold["d1"]["centre_row"], gold["d2"]["centre_row"])
-    nx, ny, nz, h = 20, 24, 16, 0.45
+    nx, ny, nz = dims
+    h = 0.45
     cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2)
     cfg.deltat = 1.3092e-5
     tabs = oracle_mod.build_tables(cfg)
