@@ -32,11 +32,11 @@ NAMELIST = """ &input
  umax = 2.7939365463E+03
  filedenin  = '{filein}'
  nx = {nx}
- ny = {nx}
- nz = {nx}
+ ny = {ny}
+ nz = {nz}
  xmax = {xmax}d0
- ymax = {xmax}d0
- zmax = {xmax}d0
+ ymax = {ymax}d0
+ zmax = {zmax}d0
  npd=13
  core4='OT'
  niter={niter}
@@ -61,7 +61,8 @@ def driver():
 
 
 def test_parse_matches_the_python_reader(tmp_path):
-    text = NAMELIST.format(mode=0, filein="den.in", nx=192, xmax=38.4, niter=99999999, pener=200, pcurr=2000)
+    text = NAMELIST.format(mode=0, filein="den.in", nx=192, ny=192, nz=192, xmax=38.4, ymax=38.4, zmax=38.4,
+                           niter=99999999, pener=200, pcurr=2000)
     nml = tmp_path / "input.nml"
     nml.write_text(text)
     out = subprocess.run([driver(), str(nml), "--parse"], capture_output=True, text=True, check=True).stdout
@@ -93,21 +94,24 @@ def fortran_rows(path):
 
 
 @pytest.mark.gpu
-def test_driver_outputs_match_the_python_mirror(tmp_path):
-    psi, r, v, meta = he4gpu.collision_case("he100_xe_32")
-    nx, xmax = meta["nx"], meta["xmax"]
-    psi_f = psi.reshape(nx, nx, nx).transpose(2, 1, 0)  # (nx, ny, nz), x fastest in memory order F
+@pytest.mark.parametrize("case", ["he100_xe_32", "he200_xe_40x48x64"])
+def test_driver_outputs_match_the_python_mirror(tmp_path, case):
+    psi, r, v, meta = he4gpu.collision_case(case)
+    nx, ny, nz = meta["nx"], meta["ny"], meta["nz"]
+    xmax, ymax, zmax = meta["xmax"], meta["ymax"], meta["zmax"]
+    psi_f = psi.reshape(nz, ny, nx).transpose(2, 1, 0)  # (nx, ny, nz), x fastest in memory order F
     den_in = tmp_path / "den.in"
-    formats.write_density(str(den_in), psi_f, r, v, xmax, xmax, xmax)
+    formats.write_density(str(den_in), psi_f, r, v, xmax, ymax, zmax)
     niter, pener, pcurr = 8, 4, 8
-    (tmp_path / "input.nml").write_text(NAMELIST.format(mode=2, filein=str(den_in), nx=nx, xmax=xmax, niter=niter,
-                                                        pener=pener, pcurr=pcurr))
+    (tmp_path / "input.nml").write_text(NAMELIST.format(mode=2, filein=str(den_in), nx=nx, ny=ny, nz=nz, xmax=xmax,
+                                                        ymax=ymax, zmax=zmax, niter=niter, pener=pener,
+                                                        pcurr=pcurr))
     res = subprocess.run([driver(), "input.nml"], capture_output=True, text=True, cwd=tmp_path)
     assert res.returncode == 0, res.stderr
 
     # the same run through the Python mirror (device-built tables, as the driver's)
     kw, tk = he4gpu.config_for_case(dict(meta, dt_ps=1e-4, imp="Xe"))
-    cfg = he4gpu.default_config(nx, nx, nx, xmax, lambdah=2.0, tzmean=49.2, tzsurf=2.0, **kw)
+    cfg = he4gpu.default_config(nx, ny, nz, xmax, ymax, zmax, lambdah=2.0, tzmean=49.2, tzsurf=2.0, **kw)
     run = he4gpu.Run(cfg, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463, device_tables=True)
     run.set_state(psi, r, v)
     want_r, energies = [run.impurity()[0]], {}
@@ -138,20 +142,23 @@ def test_driver_outputs_match_the_python_mirror(tmp_path):
     # the reference's other files: the namelist echo the Fortran wrappers read
     # their cadence from, timec.dat, and the respar cuts of the start
     echo = tmp_path / "DFT4He3d.namelist.read"
-    assert {k: he4gpu.read_namelist_int(echo, k) for k in ("iter0", "niter", "pener", "pcurr", "nx")} == \
-        {"iter0": 0, "niter": niter, "pener": pener, "pcurr": pcurr, "nx": nx}
+    assert {k: he4gpu.read_namelist_int(echo, k) for k in ("iter0", "niter", "pener", "pcurr", "nx", "nz")} == \
+        {"iter0": 0, "niter": niter, "pener": pener, "pcurr": pcurr, "nx": nx, "nz": nz}
     lines = (tmp_path / "timec.dat").read_text().splitlines()
-    assert len(lines) == nx * (nx + 1)
+    assert len(lines) == nz * (nx + 1)
     rows = np.array([[float(t) for t in ln.split()] for ln in lines if ln.strip()])
-    tc = he4gpu.build_timec(cfg)[:, nx // 2, :]  # (z, x) at iy = ny/2 + 1
+    tc = he4gpu.build_timec(cfg)[:, ny // 2, :]  # (z, x) at iy = ny/2 + 1
     assert np.array_equal(rows[:, 2].astype(np.float32), tc.reshape(-1))
+    hx, hz = 2 * xmax / nx, 2 * zmax / nz
+    np.testing.assert_allclose(rows[:nx, 0], -xmax + hx * np.arange(nx), rtol=0, atol=1e-12)
+    np.testing.assert_allclose(rows[::nx, 1], -zmax + hz * np.arange(nz), rtol=0, atol=1e-12)
     first = he4gpu.Run(cfg, selec="Xe_He", r_cutoff=2.55, umax=2793.9365463, device_tables=True)
     first.set_state(psi, r, v)
     for name, field in (("hedenini", first.den), ("uimp", first.field("uimp"))):
-        c = nx // 2
-        for ax, line in (("x", field[c, c, :]), ("y", field[c, :, c]), ("z", field[:, c, c])):
+        cx, cy, cz = nx // 2, ny // 2, nz // 2
+        for ax, line in (("x", field[cz, cy, :]), ("y", field[cz, :, cx]), ("z", field[:, cy, cx])):
             cut = np.loadtxt(tmp_path / f"{name}-{ax}.dat")
-            assert cut.shape == (nx, 2)
+            assert cut.shape == (len(line), 2)
             want = np.where(np.abs(line) < 1e-40, 0.0, line)
             np.testing.assert_allclose(cut[:, 1], want, rtol=1e-5, atol=0)
     first.close()
