@@ -60,15 +60,17 @@ def driver():
     return build.DRIVER
 
 
-def test_parse_matches_the_python_reader(tmp_path):
-    text = NAMELIST.format(mode=0, filein="den.in", nx=192, ny=192, nz=192, xmax=38.4, ymax=38.4, zmax=38.4,
-                           niter=99999999, pener=200, pcurr=2000)
+@pytest.mark.parametrize("n,ext", [((192, 192, 192), (38.4, 38.4, 38.4)), ((40, 48, 64), (9.0, 9.6, 12.8))])
+def test_parse_matches_the_python_reader(tmp_path, n, ext):
+    text = NAMELIST.format(mode=0, filein="den.in", nx=n[0], ny=n[1], nz=n[2], xmax=ext[0], ymax=ext[1],
+                           zmax=ext[2], niter=99999999, pener=200, pcurr=2000)
     nml = tmp_path / "input.nml"
     nml.write_text(text)
     out = subprocess.run([driver(), str(nml), "--parse"], capture_output=True, text=True, check=True).stdout
     got = dict(kv.split("=", 1) for kv in out.split())
     cfg, over, table, rimp, vimp, loop = formats.run_from_namelist(formats.read_namelist(str(nml)))
-    assert int(got["nx"]) == cfg["nx"] == 192 and float(got["xmax"]) == cfg["xmax"]
+    assert (int(got["nx"]), int(got["ny"]), int(got["nz"])) == (cfg["nx"], cfg["ny"], cfg["nz"]) == n
+    assert (float(got["xmax"]), float(got["ymax"]), float(got["zmax"])) == (cfg["xmax"], cfg["ymax"], cfg["zmax"])
     assert float(got["deltat"]) == over["deltat"]
     assert float(got["mimpur"]) == over["mimpur"] and float(got["tzmean"]) == over["tzmean"]
     assert float(got["lambdah"]) == over["lambdah"]
