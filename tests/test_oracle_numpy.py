@@ -362,14 +362,15 @@ def _energy(cfg, tabs, psi, rimp, vimp, r1):
     return e, np.sum(den) * dxyz
 
 
-@pytest.mark.parametrize("core,lsolid", [(0, 1), (1, 0)])
-def test_energy_matches_numpy(oracle_mod, he4gpu_mod, core, lsolid):
+@pytest.mark.parametrize("core,lsolid,dims", [(0, 1, (24, 20, 30)), (1, 0, (24, 20, 30)), (0, 1, (30, 27, 25))])
+def test_energy_matches_numpy(oracle_mod, he4gpu_mod, core, lsolid, dims):
     """energy.f90 restated in numpy on the oracle's state, at set_state and
     after 4 steps; each component to 1e-12 of its size (the solid term, whose
     1 + tanh cancels to ~1e-12, to 8 ulps of C * N on the same libm argument)."""
     gold = json.load(open(os.path.join(GOLDEN, "stencil_rows.json")))
     r1 = gold["d1"]["centre_row"]
-    nx, ny, nz, h = 24, 20, 30, 0.45
+    nx, ny, nz = dims
+    h = 0.45
     cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2, core=core, lsolid=lsolid)
     cfg.deltat = 1.3092e-5
     tabs = oracle_mod.build_tables(cfg)
@@ -388,14 +389,16 @@ def test_energy_matches_numpy(oracle_mod, he4gpu_mod, core, lsolid):
     o.close()
 
 
-def test_observables_match_numpy(oracle_mod, he4gpu_mod):
+@pytest.mark.parametrize("dims", [(24, 20, 30), (30, 27, 25)])
+def test_observables_match_numpy(oracle_mod, he4gpu_mod, dims):
     """The printed observables of DFT4He3d.f90:869-943: the particle number,
     the centre of mass (r_cm.f90:23-58, divided by the namelist's n4), the
     angular momentum <L> about it from the 13-point first derivatives of psi,
     and <x^2>, <y^2>, <z^2>."""
     gold = json.load(open(os.path.join(GOLDEN, "stencil_rows.json")))
     r1 = gold["d1"]["centre_row"]
-    nx, ny, nz, h = 24, 20, 30, 0.45
+    nx, ny, nz = dims
+    h = 0.45
     cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2)
     tabs = oracle_mod.build_tables(cfg)
     psi = _state(nx, ny, nz, h, seed=15)
