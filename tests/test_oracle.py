@@ -183,3 +183,31 @@ def test_rk_then_pc_history(oracle_mod, he4gpu_mod):
     eh, ei = o.step(1)
     assert 0 < eh < 1e-8
     assert ei >= 0
+
+
+def test_results_do_not_depend_on_the_thread_count(oracle_mod, he4gpu_mod):
+    """The oracle's sums are compensated per z plane and combined in plane
+    order, so a run on one thread and on several gives the same bits: psi,
+    the density, every energy component and the impurity after RK and PC
+    steps (the CPU baseline may use any core count)."""
+    import he4gpu
+    psi, r, v, meta = he4gpu.collision_case("he100_xe_32")
+    kw, tk = he4gpu.config_for_case(meta)
+    cfg = he4gpu.default_config(meta["nx"], meta["ny"], meta["nz"], meta["xmax"], **kw)
+    tabs = oracle_mod.build_tables(cfg, tk["selec"], tk["r_cutoff"], tk["umax"])
+    lib = oracle_mod.load()
+    out = []
+    try:
+        for threads in (1, max(2, os.cpu_count() or 2)):
+            lib.orc_set_threads(threads)
+            o = oracle_mod.OracleRun(cfg, tabs)
+            o.set_state(psi, r, v)
+            o.step(5)
+            out.append((o.psi, o.den, o.energy(), o.impurity()))
+            o.close()
+    finally:
+        lib.orc_set_threads(os.cpu_count() or 1)
+    (pa, da, ea, ia), (pb, db, eb, ib) = out
+    assert np.array_equal(pa, pb) and np.array_equal(da, db)
+    assert ea == eb
+    assert all(np.array_equal(x, y) for x, y in zip(ia, ib))
