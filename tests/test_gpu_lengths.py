@@ -3,18 +3,18 @@
 nx (so every half-length nx/2 of the x passes' packed complex lines, odd ones
 included) and every length as ny or nz (the y lines and the z convolution
 columns), with nx = 2 mod 4 among them (the mixed form's scalar force
-kernel). On each grid the library's mean-field
-evaluation and five steps (three Runge-Kutta-Gill, two predictor-corrector:
-steprk.f90:21-150, steppc.f90:1-178, poten.f90:5-118) are compared with the
-FP64 oracle:
+kernel). On each grid the mean-field evaluation and five steps (three
+Runge-Kutta-Gill, two predictor-corrector: steprk.f90:21-150,
+steppc.f90:1-178, poten.f90:5-118) are compared with the FP64 oracle:
 - FP64 with the default passes (register engine where a length has a
   specialisation, the generic mixed-radix kernels elsewhere) and with the
   generic kernels for every pass;
 - df64 (its tolerances equal FP64's, uimp to 2e-12 of its maximum);
 - mixed (FP32 fields: 1e-5).
-The states are a seeded Woods-Saxon density (R = 8, a = 2 Angstrom, cut by
-the smaller boxes) with random phases, and the impurity sits off the grid's
-axes inside the box.
+Some grids also run core OTC, hx, hy and hz all different, or core OT
+without the solid penalty, in all three forms. The states are a seeded
+Woods-Saxon density (R = 8, a = 2 Angstrom, cut by the smaller boxes) with
+random phases, and the impurity sits off the grid's axes inside the box.
 """
 import numpy as np
 import pytest
