@@ -299,17 +299,19 @@ class _NumpyRun:
         self.evaluate(self.rimp)
 
 
-@pytest.mark.parametrize("dims", [(20, 24, 16), (18, 27, 25)])
-def test_rk_and_pc_steps_match_numpy(oracle_mod, he4gpu_mod, dims):
+@pytest.mark.parametrize("dims,core", [((20, 24, 16), 0), ((18, 27, 25), 0), ((20, 24, 16), 1)])
+def test_rk_and_pc_steps_match_numpy(oracle_mod, he4gpu_mod, dims, core):
     """Three Runge-Kutta-Gill steps and three Hamming predictor-modifier-
     corrector steps (steppc.f90:1-178, the impurity predictor stored into
     rimpold(:,ioldr(3)) and the field evaluated there) of the driver loop,
-    restated in numpy, against the oracle's step (also on odd lengths)."""
+    restated in numpy, against the oracle's step (also on odd lengths, and
+    with core OTC: lsolid off, the alpha_s term in every evaluation)."""
     gold = json.load(open(os.path.join(GOLDEN, "stencil_rows.json")))
     rows = (gold["d1"]["centre_row"], gold["d2"]["centre_row"])
     nx, ny, nz = dims
     h = 0.45
-    cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2)
+    otc = {"core": 1, "lsolid": 0, "hcg": 2.190323} if core else {}
+    cfg = he4gpu_mod.default_config(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2, **otc)
     cfg.deltat = 1.3092e-5
     tabs = oracle_mod.build_tables(cfg)
     psi = _state(nx, ny, nz, h, seed=13)
